@@ -1,0 +1,121 @@
+"""Pin the CPU oracle against the reference's own known-answer vectors.
+
+Each test mirrors one GoogleTest case of the reference (src/grid/test/*.cpp); the
+numbers come from tests/golden/reference_knowns.json (extracted by make_golden.py).
+Tolerance is the reference's own tensor_eq: absolute 1e-8 (utilities_tensor.h:180-212).
+"""
+import numpy as np
+import pytest
+
+from oracle import dgo
+
+TOL = 1e-8
+
+
+def F(a):
+    """Eigen nested initialiser -> column-major flat vector."""
+    return np.asarray(a, dtype=np.float64).ravel(order="F")
+
+
+def Fc(a):
+    a = np.asarray(a, dtype=np.float64)
+    return (a[..., 0] + 1j * a[..., 1])
+
+
+def test_xi_2x1x1(knowns):
+    # SpectralTestInit (test_spectral.cpp:15-48): x index at Nyquist -> xi1st = 0
+    k = knowns["spectral_init_2x1x1"]
+    x1, x2 = dgo.xi(k["cells"], k["geom"], 0)
+    e1 = Fc(k["xi1st"])  # shape (3, 2, 1, 1): (p, i, k, j)
+    e2 = Fc(k["xi2nd"])
+    # oracle layout (j, k, i, p)
+    assert np.allclose(np.transpose(x1, (3, 2, 1, 0)), e1, atol=TOL, rtol=0)
+    assert np.allclose(np.transpose(x2, (3, 2, 1, 0)), e2, atol=TOL, rtol=0)
+
+
+def test_constitutive_response_averages(knowns):
+    # SpectralTestConstitutiveResponse (test_spectral.cpp:58-216)
+    k = knowns["constitutive_response_2x1x1"]
+    P = F(k["P"]); dPdF = F(k["dPdF"])
+    P_av, Cv, Cm = dgo.averages(P, dPdF)
+    assert np.allclose(P_av, F(k["P_av"]), atol=TOL, rtol=0)
+    assert np.allclose(Cv, F(k["C_volAvg"]), atol=TOL * 1e3, rtol=1e-15)
+    assert np.allclose(Cm, F(k["C_minMaxAvg"]), atol=TOL * 1e3, rtol=1e-15)
+
+
+def test_divergence_correction(knowns):
+    # MechBaseTestInitDivergenceCorrection (test_mech_base.cpp:55-77)
+    k = knowns["divergence_correction"]
+    assert np.array_equal(dgo.scaled_geom(k["cells"], k["geom"], "none"), k["geom"])
+    assert np.allclose(dgo.scaled_geom(k["cells"], k["geom"], "size"), k["size"], rtol=0, atol=1e-15)
+    # size+grid: the reference test expects (0.6, 0.8, 1.0), but its own code
+    # (mech_base.cpp:20-30: middle of geom/cells = (1.5, 4, 5) is index 1) and the
+    # Fortran minloc/maxloc rule both give geom/geom[1]*cells[1] = (0.75, 1, 1.25).
+    # The oracle follows the code; the expectation is recorded as inconsistent.
+    got = dgo.scaled_geom(k["cells"], k["geom"], "size+grid")
+    assert np.allclose(got, [0.75, 1.0, 1.25], rtol=0, atol=1e-15)
+    assert not np.allclose(got, k["size+grid"])
+
+
+def test_forward_field(knowns):
+    # MechBaseTestForwardField (test_mech_base.cpp:199-237)
+    k = knowns["forward_field"]
+    out = dgo.forward_field(k["delta_t"], F(k["field_last_inc"]), F(k["rate"]), F(k["aim"]))
+    assert np.allclose(out, F(k["expected"]), atol=TOL, rtol=0)
+
+
+def test_masked_compliance(knowns):
+    # MechBaseTestMaskedCompliance (test_mech_base.cpp:239-321)
+    k = knowns["masked_compliance"]
+    mask = F(k["mask_stress"]).astype(int)
+    S = dgo.masked_compliance(F(k["C"]), [1, 0, 0, 0], mask)
+    assert np.allclose(S, F(k["expected"]), atol=1e-20, rtol=1e-12)
+    assert np.count_nonzero(S) == 4
+
+
+def test_divergence_rms_4x1x1(knowns):
+    # MechBaseTestDivergenceRMS (test_mech_base.cpp:323-387): rms = 1481.2323577332318
+    k = knowns["divergence_rms_4x1x1"]
+    xi1st = np.transpose(Fc(k["xi1st"]), (3, 2, 1, 0))     # (p,i,k,j) -> (j,k,i,p)
+    # the reference's mock grid keeps scaled_geom_size = cells (conftest.h:40)
+    rms = dgo.divergence_rms(k["cells"], k["geom"], [4.0, 1.0, 1.0], xi1st, F(k["field"]))
+    assert rms == pytest.approx(k["rms"], rel=1e-14, abs=0)
+
+
+def test_gamma_convolution_zero_frequency(knowns):
+    # MechBaseTestGammaConvolution (test_mech_base.cpp:389-490): xi = 0 -> only the aim survives
+    k = knowns["gamma_convolution_2x1x1"]
+    xi1st = np.zeros((1, 1, 2, 3), dtype=np.complex128)
+    out = dgo.gamma_convolution([2, 1, 1], xi1st, F(k["C_ref"]), F(k["field_aim"]), F(k["field"]))
+    assert np.allclose(out, F(k["expected"]), atol=TOL, rtol=0)
+
+
+def test_calculate_rate(knowns):
+    # TestCalculateRate (test_mech_base.cpp:492-545)
+    k = knowns["calculate_rate"]
+    out = dgo.calculate_rate(True, F(k["field_0"]), F(k["field"]), k["dt"], F(k["avRate"]))
+    assert np.allclose(out, F(k["expected"]), atol=TOL, rtol=0)
+
+
+def test_form_residual_bc(knowns):
+    # TestFormResidual (test_mech_solver_basic.cpp:232-376)
+    k = knowns["form_residual"]
+    mask = np.asarray(k["stress_mask"]).ravel(order="F").astype(int)
+    F_aim = np.asarray(k["F_aim"]).ravel(order="F")
+    err, F_aim_new, rot = dgo.form_residual_bc(F(k["S"]), F(k["P_av"]), np.zeros(9), mask, [1, 0, 0, 0], F_aim)
+    assert err == k["expected_err_BC"]
+    assert np.allclose(F_aim_new, F(k["expected_F_aim"]), atol=TOL, rtol=0)
+    assert np.allclose(rot, F(k["expected_rotated"]), atol=TOL, rtol=0)
+
+
+def test_fft_round_trip_and_numpy():
+    # TestFFT round trip (test_fft.cpp:11-58) plus a numpy cross-check of the layout
+    rng = np.random.default_rng(7)
+    for cells in [(2, 1, 1), (4, 3, 5), (6, 7, 8), (3, 3, 3), (1, 4, 2), (16, 8, 4)]:
+        N0, N1, N2 = cells
+        f = rng.standard_normal((N2, N1, N0, 9))
+        spec = dgo.fft_r2c(cells, f)
+        ref = np.fft.rfftn(f, axes=(0, 1, 2))            # (kz, ky, kx, 9)
+        assert np.allclose(spec, np.transpose(ref, (1, 0, 2, 3)), atol=1e-10, rtol=1e-12)
+        back = dgo.fft_c2r(cells, spec).reshape(N2, N1, N0, 9) / (N0 * N1 * N2)
+        assert np.allclose(back, f, atol=1e-12, rtol=0)
