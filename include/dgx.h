@@ -1,0 +1,151 @@
+/*
+ * dgx.h -- C ABI of the GB300 (sm_103a) DAMASK_grid spectral-basic solver.
+ *
+ * Plain C types only (pointers, sizes, int32/double); every call returns a
+ * dgx_status.  All tensors at this boundary use the reference's layout:
+ * column-major 3x3 (component i + 3*j), fields (3,3,N) with the cell index
+ * cell = x + N0*(y + N1*z) slowest, i.e. value(i,j,cell) = a[(i + 3*j) + 9*cell],
+ * and 3x3x3x3 tangents a[i + 3j + 9k + 27l] per cell.  Host pointers unless the
+ * function name ends in _device.
+ *
+ * Each entry point names the reference interface it replaces (reference paths).
+ */
+#ifndef DGX_H
+#define DGX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t dgx_status;
+enum {
+  DGX_OK = 0,
+  DGX_ERR_ARG = -1,          /* invalid argument / size */
+  DGX_ERR_CUDA = -2,         /* CUDA runtime error (message: dgx_last_error) */
+  DGX_ERR_NOMEM = -3,        /* device allocation failed */
+  DGX_ERR_UNSUPPORTED = -4,  /* option not implemented on this path */
+  DGX_ERR_NOT_CONVERGED = -5,/* load case: no solution after max cut-backs */
+  DGX_ERR_STATE = -6         /* call out of order (e.g. solve before init) */
+};
+
+/* phenopowerlaw cF phase + crystallite numerics.
+ * Replaces material.yaml/numerics parsing of phase_mechanical_plastic_phenopowerlaw.f90:75-290,
+ * phase_mechanical_elastic.f90:74-104 and phase_mechanical.f90:280-290. */
+typedef struct dgx_material {
+  double C11, C12, C44;
+  double xi_0, xi_inf, h_0, n, dot_gamma_0, a, c_1, c_2;
+  double h_sl_sl[7];
+  double atol_xi, atol_gamma;
+  double r_cutback_min, r_cutback, r_increase, eps_rel_state;
+  int32_t N_iter_state_max, N_iter_Lp_max;
+  double r_linesearch_Lp, eps_rel_Lp, eps_abs_Lp;
+  int32_t f_update_jacobi_Lp;
+} dgx_material;
+
+/* grid solver numerics.  Replaces Config::Numerics (src/grid/config.h:50-78). */
+typedef struct dgx_numerics {
+  int32_t itmin, itmax, update_gamma;
+  double eps_abs_div, eps_rel_div, eps_abs_P, eps_rel_P;
+  int32_t divergence_correction;  /* 0 none, 1 size, 2 size+grid */
+  int32_t derivative;             /* 0 continuous, 1 central_difference (2 FWBW: unsupported) */
+  int32_t stag_iter_max, max_cut_back;
+  int32_t solver;                 /* 0 NGMRES (PETSc SNESNGMRES defaults), 1 fixed point */
+  int32_t ngmres_m, snes_max_it;
+  int32_t precision;              /* 0 FP64 everywhere, 1 mixed: FP32 FFT/Gamma */
+  int32_t lazy_tangent;           /* 1: tangent only where C_volAvg/C_minMaxAvg are consumed */
+} dgx_numerics;
+
+void dgx_material_default(dgx_material* m);
+void dgx_numerics_default(dgx_numerics* n);
+
+/* One load step (Config::LoadStep, src/grid/config.h:86-97; parse_load config.cpp:247-358).
+ * Masks are column-major, 1 where the load yaml has 'x'. */
+typedef struct dgx_loadstep {
+  int32_t def_type;   double def_values[9];    int32_t def_mask[9];    /* 0 F, 1 dot_F, 2 L */
+  int32_t stress_type; double stress_values[9]; int32_t stress_mask[9]; /* 0 P, 1 dot_P */
+  double rot_q[4];                                                     /* w, x, y, z */
+  double t;  int32_t N;  double r;  int32_t estimate_rate;  int32_t f_out;
+} dgx_loadstep;
+
+typedef struct dgx_inc_record {
+  double t, dt;
+  double P_av[9], F_aim[9], F_av[9];
+  int32_t iterations, evaluations, converged, cutbacks;
+  double err_div, err_BC;
+  double seconds;                 /* wall time of the increment */
+} dgx_inc_record;
+
+typedef struct dgx_rve dgx_rve;
+
+/* Create an RVE on the current CUDA device: grid + material map + orientations.
+ * Replaces f_materialpoint_initBase/initDamask (src/grid/main.cpp:9-13,
+ * materialpoint.f90:68-156) and DiscretizationGrid::init (discretization_grid.cpp:8-84).
+ * material_at: N0*N1*N2 0-based material indices; orientations: 4 doubles
+ * (w,x,y,z) per material. */
+dgx_status dgx_rve_create(const int32_t cells[3], const double size[3], const int32_t* material_at,
+                          int32_t n_materials, const double* orientations, const dgx_material* mat,
+                          const dgx_numerics* num, dgx_rve** out);
+void dgx_rve_destroy(dgx_rve* rve);
+const char* dgx_last_error(void);
+int64_t dgx_rve_points(const dgx_rve* rve);
+/* device bytes held by the RVE (fields, state, NGMRES history, scratch) */
+int64_t dgx_rve_device_bytes(const dgx_rve* rve);
+
+/* Per-cell constitutive response for cells [first, first+count) of F, with P and
+ * (optionally) dPdF out; terminally_ill set if any cell failed.
+ * Replaces f_homogenization_mechanical_response + f_homogenization_mechanical_response2
+ * (src/grid/spectral.h:20-22; homogenization.f90:219-324).  The current
+ * implementation evaluates whole RVEs: first must be 0 and count N. */
+dgx_status dgx_constitutive_response(dgx_rve* rve, const double* F, double dt, int32_t first, int32_t count,
+                                     double* P, double* dPdF, int32_t* terminally_ill);
+/* Volume averages of the last response: replaces the reductions of
+ * Spectral::constitutive_response (src/grid/spectral.cpp:160-217). */
+dgx_status dgx_averages(dgx_rve* rve, double P_av[9], double C_volAvg[81], double C_minMaxAvg[81]);
+/* Commit the increment (state0 <- state).  Replaces f_materialpoint_forward
+ * (src/grid/damask_grid.h:17; materialpoint.f90:208-215). */
+dgx_status dgx_commit_increment(dgx_rve* rve);
+
+/* Divergence RMS of a stress field.  Replaces MechBase::calculate_divergence_rms
+ * (src/grid/mech_base.cpp:302-398). */
+dgx_status dgx_divergence_rms(dgx_rve* rve, const double* P, double* rms);
+/* In place Gamma convolution with zero frequency <- aim, using C_ref.
+ * Replaces MechBase::gamma_convolution (src/grid/mech_base.cpp:400-477). */
+dgx_status dgx_gamma_convolution(dgx_rve* rve, double* field, const double aim[9]);
+/* Set the reference stiffness C_ref = C / wgt (MechBase::update_gamma, mech_base.cpp:156-157). */
+dgx_status dgx_update_gamma(dgx_rve* rve, const double C[81]);
+/* Forward FFT of a (3,3,N) field into the reference's transposed-out half spectrum
+ * (3,3,N0/2+1,N2,N1) as interleaved (re,im) (FFT<5>::forward, src/grid/fft.h:37-47). */
+dgx_status dgx_fft_forward(dgx_rve* rve, const double* field, double* spectrum);
+
+/* Solver (MechSolverBasic + DamaskGrid, src/grid/mech_solver_basic.cpp, damask_grid.cpp) */
+dgx_status dgx_solver_init(dgx_rve* rve);                                   /* MechSolverBasic::init :19-108 */
+dgx_status dgx_solver_forward(dgx_rve* rve, int32_t cutback, int32_t guess, double dt, double dt_old,
+                              double t_remaining, const dgx_loadstep* ls);  /* forward :163-220 */
+dgx_status dgx_solver_solve(dgx_rve* rve, int32_t* converged, int32_t* iterations,
+                            int32_t* terminally_ill);                      /* calculate_solution :110-161 */
+/* DamaskGrid::loop_over_loadcase (damask_grid.cpp:82-196): runs all steps from
+ * solver init; records[k] per increment (up to max_records). */
+dgx_status dgx_run_loadcase(dgx_rve* rve, int32_t nsteps, const dgx_loadstep* steps,
+                            dgx_inc_record* records, int32_t max_records, int32_t* n_records);
+/* incremental variant: dgx_solver_init once, then one increment per call
+ * (state carried on the device between calls) */
+dgx_status dgx_run_increment(dgx_rve* rve, const dgx_loadstep* step, int32_t step_index, int32_t inc,
+                             dgx_inc_record* record);
+
+/* Copy a per-point field out in the reference layout.  name: "F", "P", "Fp", "Lp",
+ * "Fe", "S" (9 per cell), "xi", "gamma" (12 per cell), "dPdF" (81 per cell, last
+ * response with dPdF), or averages "P_av", "F_aim", "C_volAvg", "C_minMaxAvg",
+ * "C_ref", "S_compliance". */
+dgx_status dgx_get(dgx_rve* rve, const char* name, double* out);
+
+/* Work counters since creation: [0] residual evaluations, [1] constitutive
+ * state (FPI) iterations, [2] Lp Newton iterations, [3] tangent evaluations,
+ * [4] kernel launches issued by the library. */
+dgx_status dgx_counters(const dgx_rve* rve, int64_t out[5]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

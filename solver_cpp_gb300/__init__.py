@@ -1,0 +1,192 @@
+"""GB300-native DAMASK_grid spectral-basic solver (phenopowerlaw cF) -- host API.
+
+Thin Python view of the C ABI (include/dgx.h, libdgx.so).  Method names follow
+the reference's operator surface: ``Spectral::constitutive_response``,
+``MechBase::calculate_divergence_rms`` / ``gamma_convolution`` / ``update_gamma``,
+``MechSolverBasic::init`` / ``forward`` / ``calculate_solution`` and
+``DamaskGrid::loop_over_loadcase`` (reference src/grid/*.cpp).  All tensors use
+the reference layout: (N, 3, 3) per cell with numpy row/column meaning [i][j],
+cells ordered x fastest.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import dgx as _d
+from .dgx import DgxError  # noqa: F401
+from .loadcase import load_step, parse_load_yaml, parse_numerics_yaml  # noqa: F401
+
+__all__ = ["RVE", "material", "numerics", "load_step", "DgxError"]
+
+
+def material(**kw):
+    m = _d.Material()
+    _d.lib().dgx_material_default(C.byref(m))
+    for k, v in kw.items():
+        if k == "h_sl_sl":
+            for i, x in enumerate(v):
+                m.h_sl_sl[i] = float(x)
+        else:
+            setattr(m, k, v)
+    return m
+
+
+def numerics(**kw):
+    n = _d.Numerics()
+    _d.lib().dgx_numerics_default(C.byref(n))
+    names = {"none": 0, "size": 1, "size+grid": 2, "grid+size": 2,
+             "continuous": 0, "central_difference": 1, "FWBW_difference": 2,
+             "ngmres": 0, "fixed_point": 1, "fp64": 0, "mixed": 1}
+    for k, v in kw.items():
+        if isinstance(v, str):
+            v = names[v]
+        setattr(n, k, v)
+    return n
+
+
+def _f9(a):
+    """(N,3,3) numpy -> reference (3,3,N) column-major flat array."""
+    a = np.asarray(a, dtype=np.float64)
+    return np.ascontiguousarray(np.swapaxes(a, -1, -2)).reshape(-1)
+
+
+def _unf9(v, n):
+    return np.swapaxes(np.asarray(v).reshape(n, 3, 3), -1, -2)
+
+
+class RVE:
+    """One representative volume element resident on the current CUDA device."""
+
+    def __init__(self, cells, size, material_at, orientations, mat=None, num=None):
+        L = _d.lib()
+        self.cells = tuple(int(c) for c in cells)
+        self.N = int(np.prod(self.cells))
+        ma = np.ascontiguousarray(np.asarray(material_at, dtype=np.int32).ravel())
+        if ma.size != self.N:
+            raise ValueError("material_at must have N0*N1*N2 entries")
+        q = np.ascontiguousarray(np.asarray(orientations, dtype=np.float64).reshape(-1, 4))
+        self.mat = mat if mat is not None else material()
+        self.num = num if num is not None else numerics()
+        h = C.c_void_p()
+        cells_c = (C.c_int32 * 3)(*self.cells)
+        size_c = (C.c_double * 3)(*[float(s) for s in size])
+        _d.check(L.dgx_rve_create(cells_c, size_c, ma.ctypes.data_as(C.POINTER(C.c_int32)), q.shape[0],
+                                  _d.dptr(q), C.byref(self.mat), C.byref(self.num), C.byref(h)), "dgx_rve_create")
+        self.h = h
+        self.size = tuple(float(s) for s in size)
+
+    def close(self):
+        if getattr(self, "h", None):
+            _d.lib().dgx_rve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_bytes(self):
+        return int(_d.lib().dgx_rve_device_bytes(self.h))
+
+    # ------------------------------------------------------------ reference operators
+    def constitutive_response(self, F, dt, want_dPdF=False):
+        """Spectral::constitutive_response for F (N,3,3): returns P (N,3,3) [, dPdF (N,3,3,3,3)]."""
+        F9 = _f9(F)
+        P = np.zeros(9 * self.N)
+        dP = np.zeros(81 * self.N) if want_dPdF else None
+        ill = C.c_int32(0)
+        _d.check(_d.lib().dgx_constitutive_response(self.h, _d.dptr(F9), float(dt), 0, self.N, _d.dptr(P),
+                                                    _d.dptr(dP) if dP is not None else None, C.byref(ill)),
+                 "dgx_constitutive_response")
+        self.terminally_ill = bool(ill.value)
+        Pn = _unf9(P, self.N)
+        if want_dPdF:
+            d = dP.reshape(self.N, 3, 3, 3, 3, order="C")
+            # flat index i + 3j + 9k + 27l per cell -> array [cell][l][k][j][i]
+            return Pn, np.transpose(d, (0, 4, 3, 2, 1))
+        return Pn
+
+    def averages(self):
+        P = np.zeros(9); Cv = np.zeros(81); Cm = np.zeros(81)
+        _d.check(_d.lib().dgx_averages(self.h, _d.dptr(P), _d.dptr(Cv), _d.dptr(Cm)), "dgx_averages")
+        return (_unf9(P, 1)[0], Cv.reshape(3, 3, 3, 3, order="F"), Cm.reshape(3, 3, 3, 3, order="F"))
+
+    def commit(self):
+        _d.check(_d.lib().dgx_commit_increment(self.h), "dgx_commit_increment")
+
+    def calculate_divergence_rms(self, P):
+        r = C.c_double(0.0)
+        P9 = _f9(P)
+        _d.check(_d.lib().dgx_divergence_rms(self.h, _d.dptr(P9), C.byref(r)), "dgx_divergence_rms")
+        return r.value
+
+    def update_gamma(self, C4):
+        c = np.ascontiguousarray(np.asarray(C4, dtype=np.float64).reshape(3, 3, 3, 3).ravel(order="F"))
+        _d.check(_d.lib().dgx_update_gamma(self.h, _d.dptr(c)), "dgx_update_gamma")
+
+    def gamma_convolution(self, field, aim):
+        f = _f9(field).copy()
+        a = _f9(np.asarray(aim).reshape(1, 3, 3))
+        _d.check(_d.lib().dgx_gamma_convolution(self.h, _d.dptr(f), _d.dptr(a)), "dgx_gamma_convolution")
+        return _unf9(f, self.N)
+
+    def fft_forward(self, field):
+        """FFT<5>::forward: (N,3,3) -> complex (N1, N2, N0//2+1, 3, 3) in the transposed-out order."""
+        N0, N1, N2 = self.cells
+        out = np.zeros(2 * 9 * (N0 // 2 + 1) * N1 * N2)
+        f = _f9(field)
+        _d.check(_d.lib().dgx_fft_forward(self.h, _d.dptr(f), _d.dptr(out)), "dgx_fft_forward")
+        z = out[0::2] + 1j * out[1::2]
+        z = z.reshape(N1, N2, N0 // 2 + 1, 9)
+        return np.swapaxes(z.reshape(N1, N2, N0 // 2 + 1, 3, 3), -1, -2)
+
+    def init(self):
+        """MechSolverBasic::init: F = I, constitutive response at dt = 0, C_ref."""
+        _d.check(_d.lib().dgx_solver_init(self.h), "dgx_solver_init")
+
+    def forward(self, cutback, guess, dt, dt_old, t_remaining, step):
+        _d.check(_d.lib().dgx_solver_forward(self.h, int(cutback), int(guess), float(dt), float(dt_old),
+                                             float(t_remaining), C.byref(step)), "dgx_solver_forward")
+
+    def calculate_solution(self):
+        conv = C.c_int32(0); it = C.c_int32(0); ill = C.c_int32(0)
+        _d.check(_d.lib().dgx_solver_solve(self.h, C.byref(conv), C.byref(it), C.byref(ill)), "dgx_solver_solve")
+        return dict(converged=bool(conv.value), required_iterations=it.value, terminally_ill=bool(ill.value))
+
+    def loop_over_loadcase(self, steps, max_records=100000):
+        arr = (_d.LoadStep * len(steps))(*steps)
+        nrec = sum(int(s.N) for s in steps)
+        recs = (_d.IncRecord * max(1, min(nrec, max_records)))()
+        n = C.c_int32(0)
+        _d.check(_d.lib().dgx_run_loadcase(self.h, len(steps), arr, recs, len(recs), C.byref(n)), "dgx_run_loadcase")
+        return [_record(r) for r in recs[:n.value]]
+
+    def run_increment(self, step, step_index, inc):
+        rec = _d.IncRecord()
+        _d.check(_d.lib().dgx_run_increment(self.h, C.byref(step), int(step_index), int(inc), C.byref(rec)),
+                 "dgx_run_increment")
+        return _record(rec)
+
+    def get(self, name):
+        width = {"xi": 12, "gamma": 12}.get(name, 9)
+        scalars = {"P_av": 9, "F_aim": 9, "C_volAvg": 81, "C_minMaxAvg": 81, "C_ref": 81, "S_compliance": 81}
+        if name in scalars:
+            out = np.zeros(scalars[name])
+            _d.check(_d.lib().dgx_get(self.h, name.encode(), _d.dptr(out)), "dgx_get")
+            return _unf9(out, 1)[0] if scalars[name] == 9 else out.reshape(3, 3, 3, 3, order="F")
+        out = np.zeros(width * self.N)
+        _d.check(_d.lib().dgx_get(self.h, name.encode(), _d.dptr(out)), "dgx_get")
+        return _unf9(out, self.N) if width == 9 else out.reshape(self.N, width)
+
+    def counters(self):
+        a = (C.c_int64 * 5)()
+        _d.check(_d.lib().dgx_counters(self.h, a), "dgx_counters")
+        return dict(evaluations=a[0], state_iterations=a[1], lp_iterations=a[2], tangents=a[3], launches=a[4])
+
+
+def _record(r):
+    return dict(t=r.t, dt=r.dt, P_av=_unf9(np.array(r.P_av[:]), 1)[0], F_aim=_unf9(np.array(r.F_aim[:]), 1)[0],
+                F_av=_unf9(np.array(r.F_av[:]), 1)[0], iterations=r.iterations, evaluations=r.evaluations,
+                cutbacks=r.cutbacks, err_div=r.err_div, err_BC=r.err_BC, seconds=r.seconds)

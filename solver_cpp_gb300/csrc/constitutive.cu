@@ -1,0 +1,678 @@
+// constitutive.cu -- per-material-point phenopowerlaw cF response on sm_103a (FP64).
+//
+// One thread integrates one material point.  The algorithm is DAMASK's
+// (reference paths):
+//   src/phase_mechanical.f90:1013-1100  sub-step cut-back driver
+//   src/phase_mechanical.f90:611-693    fixed-point state integration with damper
+//   src/phase_mechanical.f90:380-604    Lp Newton-Raphson with line search
+//   src/phase_mechanical.f90:1137-1258  analytic consistent tangent dP/dF
+//   src/phase_mechanical_elastic.f90:157-195, phase_mechanical_plastic_phenopowerlaw.f90:298-483
+//   src/homogenization.f90:219-324      per-cell restore / partition / homogenise (1 constituent)
+// GB300-specific restatement: FP64 is the scarce pipe on this part, so the
+// literal 3x3x3x3 algebra is replaced by exact rank-12 forms.  With Fi = I (no
+// eigenstrain kinematics) and dLp/dS = sum_a |dgamma_a/dtau_a| P_a (x) P_a:
+//   Jacobian  J = I + dt sum_a |dg_a| vec(P_a) vec(W Q_a)^T,  W = A^T Fe,  Q_a = C : P_a
+//   tangent   lhs = dt sum_a |dg_a| vec(C : U_a) vec(P_a)^T,  U_a = Fe^T (F Fp0^-1) P_a
+// which are algebraically identical to the reference's contractions.
+#include "dgx_internal.cuh"
+
+namespace dgx {
+
+// ------------------------------------------------------------------ 3x3 helpers (column-major)
+__device__ __forceinline__ void mm(const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      C[i + 3 * j] = A[i] * B[3 * j] + A[i + 3] * B[1 + 3 * j] + A[i + 6] * B[2 + 3 * j];
+}
+// C = A^T B
+__device__ __forceinline__ void mtm(const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      C[i + 3 * j] = A[3 * i] * B[3 * j] + A[1 + 3 * i] * B[1 + 3 * j] + A[2 + 3 * i] * B[2 + 3 * j];
+}
+// C = A B^T
+__device__ __forceinline__ void mmt(const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      C[i + 3 * j] = A[i] * B[j] + A[i + 3] * B[j + 3] + A[i + 6] * B[j + 6];
+}
+__device__ __forceinline__ bool inv33(const double* __restrict__ A, double* __restrict__ I, double* det = nullptr) {
+  double c0 = A[4] * A[8] - A[7] * A[5];
+  double c1 = -A[1] * A[8] + A[7] * A[2];
+  double c2 = A[1] * A[5] - A[4] * A[2];
+  double D = A[0] * c0 + A[3] * c1 + A[6] * c2;
+  if (det) *det = D;
+  if (fabs(D) <= 2.2250738585072014e-307) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) I[k] = 0.0;
+    return false;
+  }
+  double r = 1.0 / D;
+  I[0] = c0 * r; I[1] = c1 * r; I[2] = c2 * r;
+  I[3] = (-A[3] * A[8] + A[6] * A[5]) * r;
+  I[4] = (A[0] * A[8] - A[6] * A[2]) * r;
+  I[5] = (-A[0] * A[5] + A[3] * A[2]) * r;
+  I[6] = (A[3] * A[7] - A[6] * A[4]) * r;
+  I[7] = (-A[0] * A[7] + A[6] * A[1]) * r;
+  I[8] = (A[0] * A[4] - A[3] * A[1]) * r;
+  return true;
+}
+__device__ __forceinline__ double nrm9(const double* a) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) s = fma(a[k], a[k], s);
+  return sqrt(s);
+}
+
+// x^n for small integer n by binary powering, x^(q/4) via square roots
+__device__ __forceinline__ double pow_n(double x, const MatParams& mp) {
+  if (mp.n_int > 0) {
+    int e = mp.n_int;
+    double r = 1.0, b = x;
+    while (e) { if (e & 1) r *= b; b *= b; e >>= 1; }
+    return r;
+  }
+  return pow(x, mp.n);
+}
+__device__ __forceinline__ double pow_a(double y, const MatParams& mp) {
+  if (mp.a_quarters > 0) {
+    int q = mp.a_quarters;
+    int e = q >> 2, f = q & 3;
+    double r = 1.0, b = y;
+    while (e) { if (e & 1) r *= b; b *= b; e >>= 1; }
+    if (f) {
+      double s2 = sqrt(y), s4 = sqrt(s2);
+      if (f == 1) r *= s4;
+      else if (f == 2) r *= s2;
+      else r *= s2 * s4;
+    }
+    return r;
+  }
+  return pow(y, mp.a);
+}
+
+// Hooke: S = C : E(Fe), E = (Fe^T Fe - I)/2, S symmetric (Voigt)
+__device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, double* S) {
+  double e6[6];
+  double E00 = 0.5 * (Fe[0] * Fe[0] + Fe[1] * Fe[1] + Fe[2] * Fe[2] - 1.0);
+  double E11 = 0.5 * (Fe[3] * Fe[3] + Fe[4] * Fe[4] + Fe[5] * Fe[5] - 1.0);
+  double E22 = 0.5 * (Fe[6] * Fe[6] + Fe[7] * Fe[7] + Fe[8] * Fe[8] - 1.0);
+  double E12 = 0.5 * (Fe[3] * Fe[6] + Fe[4] * Fe[7] + Fe[5] * Fe[8]);
+  double E02 = 0.5 * (Fe[0] * Fe[6] + Fe[1] * Fe[7] + Fe[2] * Fe[8]);
+  double E01 = 0.5 * (Fe[0] * Fe[3] + Fe[1] * Fe[4] + Fe[2] * Fe[5]);
+  e6[0] = E00; e6[1] = E11; e6[2] = E22; e6[3] = 2.0 * E12; e6[4] = 2.0 * E02; e6[5] = 2.0 * E01;
+  double s6[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) s = fma(mp.C66[i + 6 * j], e6[j], s);
+    s6[i] = s;
+  }
+  S[0] = s6[0]; S[4] = s6[1]; S[8] = s6[2];
+  S[5] = S[7] = s6[3]; S[2] = S[6] = s6[4]; S[1] = S[3] = s6[5];
+}
+
+// resolved shear, slip rates and |d gdot / d tau| on the 12 systems (Mp = S)
+__device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, const double* rxi,
+                                         double* gdot, double* dg) {
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) {
+    double tau = mp.Psym[a][0] * S[0] + mp.Psym[a][1] * S[4] + mp.Psym[a][2] * S[8]
+               + mp.Psym[a][3] * S[5] + mp.Psym[a][4] * S[2] + mp.Psym[a][5] * S[1];
+    double t = fabs(tau);
+    double g = mp.gdot0 * pow_n(t * rxi[a], mp);
+    gdot[a] = tau > 0.0 ? g : -g;
+    if (dg) dg[a] = (g > 2.2250738585072014e-307) ? g * mp.n / t : 0.0;   // |dgdot/dtau|
+  }
+}
+
+// phenopowerlaw dotState: [dot xi (12), |gdot| (12)]
+__device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, double* dot) {
+  double rxi[NSLIP], g[NSLIP];
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / xi[a];
+  kinetics(mp, S, rxi, g, nullptr);
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) g[a] = fabs(g[a]);
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) {
+    double x = 1.0 - xi[a] / mp.xi_inf;
+    double left = copysign(pow_a(fabs(x), mp), x);
+    double hs = 0.0;
+#pragma unroll
+    for (int b = 0; b < NSLIP; ++b) hs = fma(mp.h[a][b], g[b], hs);
+    dot[a] = mp.h0 * left * hs;
+    dot[NSLIP + a] = g[a];
+  }
+}
+
+// LU with partial pivoting of a 9x9 row-major matrix M[r][c], solving M x = b
+// for nrhs right-hand sides stored column by column in B (B[c * 9 + r]).
+__device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) {
+  int piv[9];
+  for (int k = 0; k < 9; ++k) {
+    int p = k;
+    double mx = fabs(M[9 * k + k]);
+    for (int i = k + 1; i < 9; ++i) {
+      double v = fabs(M[9 * i + k]);
+      if (v > mx) { mx = v; p = i; }
+    }
+    piv[k] = p;
+    if (M[9 * p + k] == 0.0) return false;
+    if (p != k)
+      for (int j = 0; j < 9; ++j) { double t = M[9 * k + j]; M[9 * k + j] = M[9 * p + j]; M[9 * p + j] = t; }
+    double r = 1.0 / M[9 * k + k];
+    for (int i = k + 1; i < 9; ++i) {
+      double l = M[9 * i + k] * r;
+      M[9 * i + k] = l;
+      for (int j = k + 1; j < 9; ++j) M[9 * i + j] = fma(-l, M[9 * k + j], M[9 * i + j]);
+    }
+  }
+  for (int c = 0; c < nrhs; ++c) {
+    double* x = B + 9 * c;
+    for (int k = 0; k < 9; ++k) { int p = piv[k]; if (p != k) { double t = x[k]; x[k] = x[p]; x[p] = t; } }
+    for (int i = 1; i < 9; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s = fma(-M[9 * i + j], x[j], s); x[i] = s; }
+    for (int i = 8; i >= 0; --i) {
+      double s = x[i];
+      for (int j = i + 1; j < 9; ++j) s = fma(-M[9 * i + j], x[j], s);
+      x[i] = s / M[9 * i + i];
+    }
+  }
+  return true;
+}
+
+// integrateStress with Fi = I.  Returns true if broken.  On success writes
+// P, S, Lp, Fp (regularised), Fe.
+__device__ bool integrate_stress(const MatParams& mp, const double* F, const double* Fp0, double dt,
+                                 const double* xi, double* Lp, double* S, double* P, double* Fp, double* Fe,
+                                 unsigned* lp_iters) {
+  double invFp0[9], A[9];
+  if (!inv33(Fp0, invFp0)) return true;
+  mm(F, invFp0, A);
+  double rxi[NSLIP];
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / xi[a];
+
+  double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
+  double res_old_n = 0.0, step = 1.0;
+  int jaco = 0;
+  for (int it = 1;; ++it) {
+    if (it > mp.N_iter_Lp_max) return true;
+    (*lp_iters)++;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B[k] = ((k % 4) == 0 ? 1.0 : 0.0) - dt * Lpg[k];
+    mm(A, B, Fe_);
+    hooke_S(mp, Fe_, S);
+    double gdot[NSLIP], dg[NSLIP];
+    kinetics(mp, S, rxi, gdot, dg);
+    double Lpc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      double s = 0.0;
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) s = fma(gdot[a], mp.P[a][k], s);
+      Lpc[k] = s;
+    }
+    double res[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) res[k] = Lpg[k] - Lpc[k];
+    double nLg = nrm9(Lpg), nLc = nrm9(Lpc), nr = nrm9(res);
+    double atol = fmax(mp.eps_rel_Lp * fmax(nLg, nLc), mp.eps_abs_Lp);
+    if (isnan(nr)) return true;
+    if (nr < atol) break;
+    if (it == 1 || nr < res_old_n) {
+      res_old_n = nr;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
+      step = 1.0;
+    } else {
+      step *= mp.r_linesearch_Lp;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg_old[k]);
+      continue;
+    }
+    if (jaco % mp.f_update_jacobi_Lp == 0) {
+      ++jaco;
+      // J[3k+l][3p+q] = delta + dt |dg_a| P_a(k,l) (W Q_a)(p,q), W = A^T Fe
+      double W[9];
+      mtm(A, Fe_, W);
+      double J[81];
+#pragma unroll
+      for (int k = 0; k < 81; ++k) J[k] = (k % 10) == 0 ? 1.0 : 0.0;
+      for (int a = 0; a < NSLIP; ++a) {
+        double c = dt * dg[a];
+        if (c == 0.0) continue;
+        double V[9];
+        mm(W, mp.Q[a], V);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l) {
+            double pc = c * mp.P[a][k + 3 * l];
+            if (pc == 0.0) continue;
+#pragma unroll
+            for (int p = 0; p < 3; ++p)
+#pragma unroll
+              for (int q = 0; q < 3; ++q) J[9 * (3 * k + l) + 3 * p + q] = fma(pc, V[p + 3 * q], J[9 * (3 * k + l) + 3 * p + q]);
+          }
+      }
+      double x[9];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) x[3 * k + l] = res[k + 3 * l];
+      if (!lu_solve9(J, x, 1)) return true;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) dLp[k + 3 * l] = -x[3 * k + l];
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg[k]);
+  }
+  double invFp_new[9], Fp_new[9], t1[9], t2[9], det;
+  mm(invFp0, B, invFp_new);
+  if (!inv33(invFp_new, Fp_new, &det)) return true;
+  mm(F, invFp_new, t1);
+  mmt(S, invFp_new, t2);
+  mm(t1, t2, P);
+  double dFp = Fp_new[0] * (Fp_new[4] * Fp_new[8] - Fp_new[7] * Fp_new[5])
+             - Fp_new[3] * (Fp_new[1] * Fp_new[8] - Fp_new[7] * Fp_new[2])
+             + Fp_new[6] * (Fp_new[1] * Fp_new[5] - Fp_new[4] * Fp_new[2]);
+  double s = pow(dFp, 1.0 / 3.0);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { Fp[k] = Fp_new[k] / s; Lp[k] = Lpg[k]; Fe[k] = t1[k]; }
+  return false;
+}
+
+__device__ __forceinline__ double damper(const double* o0, const double* o1, const double* o2) {
+  double d12 = 0.0, d22 = 0.0, d01 = 0.0;
+#pragma unroll
+  for (int i = 0; i < 2 * NSLIP; ++i) {
+    double a = o0[i] - o1[i], b = o1[i] - o2[i];
+    d12 = fma(a, b, d12); d22 = fma(b, b, d22); d01 = fma(o0[i], o1[i], d01);
+  }
+  if (fmin(d01, d12) < 0.0 && d22 > 0.0) return 0.75 + 0.25 * tanh(2.0 + 4.0 * d12 / d22);
+  return 1.0;
+}
+
+// integrateStateFPI; returns true if broken.  S on entry: stress used for the
+// first dot state (restored committed stress); state in/out.
+__device__ bool integrate_state(const MatParams& mp, const double* F, const double* Fp0, const double* state0,
+                                double dt, double* state, double* Lp, double* S, double* P, double* Fp,
+                                double* Fe, unsigned* lp_iters, unsigned* st_iters) {
+  double dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
+  (*st_iters)++;
+  dot_state(mp, S, state, dot);
+#pragma unroll
+  for (int i = 0; i < 2 * NSLIP; ++i) {
+    if (isnan(dot[i])) return true;
+  }
+#pragma unroll
+  for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(dot[i], dt, state0[i]);
+  bool broken = true;
+  for (int it = 1; it <= mp.N_iter_state_max; ++it) {
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) { last2[i] = it > 1 ? last1[i] : 0.0; last1[i] = dot[i]; }
+    broken = integrate_stress(mp, F, Fp0, dt, state, Lp, S, P, Fp, Fe, lp_iters);
+    if (broken) break;
+    dot_state(mp, S, state, dot);
+    bool nan = false;
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) nan |= isnan(dot[i]);
+    if (nan) break;
+    double z = damper(dot, last1, last2);
+    bool conv = true;
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) {
+      double d = dot[i] * z + last1[i] * (1.0 - z);
+      double r = state[i] - state0[i] - d * dt;
+      state[i] = state[i] - r;
+      double atol = i < NSLIP ? mp.atol_xi : mp.atol_gamma;
+      conv &= fabs(r) <= fmax(atol, mp.eps_rel_state * fabs(state[i]));
+      dot[i] = d;
+    }
+    if (conv) { broken = false; break; }
+  }
+  return broken;
+}
+
+__device__ __forceinline__ double ldp(const double* p, int64_t ld, int c, int64_t e) { return p[c * ld + e]; }
+
+// Per-point constitutive response (restore, cut-back driver, FPI, P) plus the
+// block partial sums of P for P_av.  One thread per point.
+__global__ void __launch_bounds__(128)
+k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int64_t ldF, double dt,
+               double* __restrict__ Ppart, int* __restrict__ ill, ConsCounters* cnt) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double P[9];
+  unsigned lp_iters = 0, st_iters = 0;
+  bool ok = true;
+  if (e < ps.n) {
+    double F[9], F0c[9], Fphase0[9], Fp0[9], Lp[9], Lp0[9], S[9], S0[9], state0[2 * NSLIP], state[2 * NSLIP];
+    double Fp[9], Fe[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      F[k] = Fin[k * ldF + e];
+      Fphase0[k] = ldp(ps.F0, ps.ld, k, e);
+      Fp0[k] = ldp(ps.Fp0, ps.ld, k, e);
+      Lp[k] = ldp(ps.Lp, ps.ld, k, e);
+      S0[k] = ldp(ps.S0, ps.ld, k, e);
+      F0c[k] = Fphase0[k];
+      Lp0[k] = ldp(ps.Lp0, ps.ld, k, e);
+      Fp[k] = Fp0[k];
+      Fe[k] = 0.0;
+      P[k] = 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) { state0[i] = ldp(ps.st0, ps.ld, i, e); state[i] = state0[i]; }
+    // phase_mechanical_constitutive: pretend a failed step of 1/r_cutback
+    double stepFrac = 0.0, step = 1.0 / mp.r_cutback, Fsub[9];
+    bool converged = false, todo = true;
+    int passes = 0;
+    while (todo) {
+      if (++passes > 4096) { converged = false; break; }   // hard cap: a point never loops unbounded
+      if (converged) {
+        stepFrac += step;
+        step = fmin(1.0 - stepFrac, mp.r_increase * step);
+        todo = step > 0.0;
+        if (todo) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) { F0c[k] = Fsub[k]; Lp0[k] = Lp[k]; Fp0[k] = Fp[k]; }
+#pragma unroll
+          for (int i = 0; i < 2 * NSLIP; ++i) state0[i] = state[i];
+        }
+      } else {
+        step = mp.r_cutback * step;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) { Fp[k] = Fp0[k]; S[k] = S0[k]; if (step < 1.0) Lp[k] = Lp0[k]; }
+#pragma unroll
+        for (int i = 0; i < 2 * NSLIP; ++i) state[i] = state0[i];
+        todo = step > mp.r_cutback_min;
+      }
+      if (todo) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
+        converged = !integrate_state(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &st_iters);
+      }
+    }
+    ok = converged;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      ps.F[k * ps.ld + e] = F[k];
+      ps.Fp[k * ps.ld + e] = Fp[k];
+      ps.Lp[k * ps.ld + e] = Lp[k];
+      ps.S[k * ps.ld + e] = S[k];
+      ps.Fe[k * ps.ld + e] = Fe[k];
+      ps.P[k * ps.ld + e] = P[k];
+    }
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) ps.st[i * ps.ld + e] = state[i];
+    ps.status[e] = ok ? 0 : 1;
+    if (!ok) atomicOr(ill, 1);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) P[k] = 0.0;
+  }
+  // deterministic block reduction of P (fixed tree)
+  __shared__ double red[9][128];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) red[k][threadIdx.x] = P[k];
+  __syncthreads();
+  for (int s = 64; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int k = 0; k < 9; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 9) Ppart[blockIdx.x * 9 + threadIdx.x] = red[threadIdx.x][0];
+  if (cnt) {
+    // per-warp aggregation of the work counters
+    unsigned lp = lp_iters, st = st_iters;
+    for (int o = 16; o > 0; o >>= 1) { lp += __shfl_down_sync(0xffffffffu, lp, o); st += __shfl_down_sync(0xffffffffu, st, o); }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&cnt->lp_iters, (unsigned long long)lp);
+      atomicAdd(&cnt->state_iters, (unsigned long long)st);
+    }
+  }
+}
+
+// Analytic consistent tangent (Fi = I) for one point; writes dPdF (col-major 3333).
+__device__ void tangent_point(const MatParams& mp, const double* F, const double* Fe, const double* Fp,
+                              const double* Fp0, const double* S, const double* xi, double dt, double* dPdF) {
+  double invFp[9], invFp0[9];
+  inv33(Fp, invFp);
+  inv33(Fp0, invFp0);
+  double rxi[NSLIP], gdot[NSLIP], d[NSLIP];
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / xi[a];
+  kinetics(mp, S, rxi, gdot, d);
+  double t2[9], Y[9];
+  mm(F, invFp0, t2);
+  mtm(Fe, t2, Y);                          // Fe^T (F Fp0^-1)
+  // M = I + dt sum_a d_a vec(C:U_a) vec(P_a)^T, rows (p,o) cols (p',o'), MAPPLAIN order
+  double M[81];
+#pragma unroll
+  for (int k = 0; k < 81; ++k) M[k] = (k % 10) == 0 ? 1.0 : 0.0;
+  for (int a = 0; a < NSLIP; ++a) {
+    double c = dt * d[a];
+    if (c == 0.0) continue;
+    double U[9];
+    mm(Y, mp.P[a], U);
+    double e6[6] = {U[0], U[4], U[8], U[5] + U[7], U[2] + U[6], U[1] + U[3]};
+    double s6[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      double s = 0.0;
+#pragma unroll
+      for (int j = 0; j < 6; ++j) s = fma(mp.C66[i + 6 * j], e6[j], s);
+      s6[i] = c * s;
+    }
+    double CU[9] = {s6[0], s6[5], s6[4], s6[5], s6[1], s6[3], s6[4], s6[3], s6[2]};
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int o = 0; o < 3; ++o)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+            M[9 * (3 * p + o) + 3 * q + r] = fma(CU[p + 3 * o], mp.P[a][q + 3 * r], M[9 * (3 * p + o) + 3 * q + r]);
+  }
+  // rhs(p,o,k,l) = (Fe C_po invFp^T)(k,l); stored B[(3k+l)*9 + (3p+o)] (9 rhs columns)
+  double Bm[81];
+  {
+    double C3[81];   // full stiffness from Voigt
+    const int vi[3][3] = {{0, 5, 4}, {5, 1, 3}, {4, 3, 2}};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l) C3[i + 3 * j + 9 * k + 27 * l] = mp.C66[vi[i][j] + 6 * vi[k][l]];
+    for (int p = 0; p < 3; ++p)
+      for (int o = 0; o < 3; ++o) {
+        double Cpo[9], T[9], R[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Cpo[k] = C3[p + 3 * o + 9 * k];
+        mm(Fe, Cpo, T);
+        mmt(T, invFp, R);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l) Bm[(3 * k + l) * 9 + 3 * p + o] = R[k + 3 * l];
+      }
+  }
+  lu_solve9(M, Bm, 9);   // Bm <- dSdF: Bm[(3k+l)*9 + 3p+o] = dS_po/dF_kl
+  // R_a = invFp0 P_a
+  double u1[9], u2[9], u3[9], w[9];
+  mmt(S, invFp, u1);                      // S invFp^T
+  mm(F, invFp, u2);
+  mm(u2, S, u3);
+  mm(invFp, u1, w);                       // invFp S invFp^T
+#pragma unroll
+  for (int k = 0; k < 81; ++k) dPdF[k] = 0.0;
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int l = 0; l < 3; ++l) dPdF[p + 3 * j + 9 * p + 27 * l] = w[l + 3 * j];
+  for (int kk = 0; kk < 3; ++kk)
+    for (int ll = 0; ll < 3; ++ll) {
+      const double* dS = Bm + (3 * kk + ll) * 9;    // dS(p,o) at row 3p+o
+      double dSm[9];
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int o = 0; o < 3; ++o) dSm[p + 3 * o] = dS[3 * p + o];
+      // D = -dt sum_a d_a (P_a : dS) invFp0 P_a
+      double G[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) G[k] = 0.0;
+      for (int a = 0; a < NSLIP; ++a) {
+        double wa = mp.P[a][0] * dSm[0];
+#pragma unroll
+        for (int k = 1; k < 9; ++k) wa = fma(mp.P[a][k], dSm[k], wa);
+        double c = -dt * d[a] * wa;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) G[k] = fma(c, mp.P[a][k], G[k]);
+      }
+      double D[9], X[9], Xa[9], Yb[9], Yc[9], Z[9];
+      mm(invFp0, G, D);
+      mm(F, D, X); mm(X, u1, Xa);
+      mm(u2, dSm, Yb); mmt(Yb, invFp, Yc);
+      mmt(u3, D, Z);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dPdF[k + 9 * (kk + 3 * ll)] += Xa[k] + Yc[k] + Z[k];
+    }
+}
+
+// Consistent tangent for all points with fused C_volAvg / C_minMaxAvg partials.
+// dPdF_out (81 planes, ld) may be null.
+__global__ void __launch_bounds__(64)
+k_tangent(MatParams mp, PointState ps, double dt, double* __restrict__ dPdF_out, int64_t ld_out,
+          TangentPartial* __restrict__ part) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  __shared__ double s_sum[81];
+  __shared__ double s_nmax[64], s_nmin[64];
+  __shared__ long long s_imax[64], s_imin[64];
+  if (threadIdx.x < 81) s_sum[threadIdx.x] = 0.0;
+  if (threadIdx.x + 64 < 81) s_sum[threadIdx.x + 64] = 0.0;
+  double dPdF[81];
+  double nrm = 0.0;
+  bool valid = e < ps.n;
+  if (valid) {
+    double F[9], Fe[9], Fp[9], Fp0[9], S[9], xi[NSLIP];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      F[k] = ps.F[k * ps.ld + e]; Fe[k] = ps.Fe[k * ps.ld + e]; Fp[k] = ps.Fp[k * ps.ld + e];
+      Fp0[k] = ps.Fp0[k * ps.ld + e]; S[k] = ps.S[k * ps.ld + e];
+    }
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) xi[a] = ps.st[a * ps.ld + e];
+    tangent_point(mp, F, Fe, Fp, Fp0, S, xi, dt, dPdF);
+    for (int k = 0; k < 81; ++k) nrm = fma(dPdF[k], dPdF[k], nrm);
+    if (dPdF_out)
+      for (int k = 0; k < 81; ++k) dPdF_out[k * ld_out + e] = dPdF[k];
+  }
+  s_nmax[threadIdx.x] = valid ? nrm : -1.0;
+  s_nmin[threadIdx.x] = valid ? nrm : 1.7976931348623157e308;
+  s_imax[threadIdx.x] = valid ? e : (long long)1 << 62;
+  s_imin[threadIdx.x] = valid ? e : (long long)1 << 62;
+  __syncthreads();
+  // argmax / argmin with first-index tie break
+  for (int s = 32; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      int o = threadIdx.x + s;
+      if (s_nmax[o] > s_nmax[threadIdx.x] || (s_nmax[o] == s_nmax[threadIdx.x] && s_imax[o] < s_imax[threadIdx.x])) {
+        s_nmax[threadIdx.x] = s_nmax[o]; s_imax[threadIdx.x] = s_imax[o];
+      }
+      if (s_nmin[o] < s_nmin[threadIdx.x] || (s_nmin[o] == s_nmin[threadIdx.x] && s_imin[o] < s_imin[threadIdx.x])) {
+        s_nmin[threadIdx.x] = s_nmin[o]; s_imin[threadIdx.x] = s_imin[o];
+      }
+    }
+    __syncthreads();
+  }
+  TangentPartial* bp = part + blockIdx.x;
+  if (valid && e == s_imax[0]) for (int k = 0; k < 81; ++k) bp->dmax[k] = dPdF[k];
+  if (valid && e == s_imin[0]) for (int k = 0; k < 81; ++k) bp->dmin[k] = dPdF[k];
+  if (threadIdx.x == 0) { bp->nmax = s_nmax[0]; bp->nmin = s_nmin[0]; bp->imax = s_imax[0]; bp->imin = s_imin[0]; }
+  // column sums of dPdF over the block: fixed tree per component
+  __shared__ double s_red[64];
+  for (int k = 0; k < 81; ++k) {
+    s_red[threadIdx.x] = valid ? dPdF[k] : 0.0;
+    __syncthreads();
+    for (int s = 32; s > 0; s >>= 1) {
+      if (threadIdx.x < s) s_red[threadIdx.x] += s_red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) bp->sum[k] = s_red[0];
+    __syncthreads();
+  }
+}
+
+// Final reduction of tangent partials (single block, fixed order).
+__global__ void k_tangent_finish(const TangentPartial* __restrict__ part, int nblocks, double wgt,
+                                 double* __restrict__ Cvol, double* __restrict__ Cminmax) {
+  __shared__ int bmax, bmin;
+  if (threadIdx.x == 0) {
+    int im = 0, in = 0;
+    for (int b = 1; b < nblocks; ++b) {
+      if (part[b].nmax > part[im].nmax || (part[b].nmax == part[im].nmax && part[b].imax < part[im].imax)) im = b;
+      if (part[b].nmin < part[in].nmin || (part[b].nmin == part[in].nmin && part[b].imin < part[in].imin)) in = b;
+    }
+    bmax = im; bmin = in;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < 81; k += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += part[b].sum[k];
+    Cvol[k] = s * wgt;
+    double mx = part[bmax].nmax > 0.0 ? part[bmax].dmax[k] : 0.0;
+    Cminmax[k] = 0.5 * (mx + part[bmin].dmin[k]);
+  }
+}
+
+// P_av from block partials (single block, fixed order).
+__global__ void k_pav_finish(const double* __restrict__ part, int nblocks, double wgt, double* __restrict__ Pav) {
+  if (threadIdx.x < 9) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += part[b * 9 + threadIdx.x];
+    Pav[threadIdx.x] = s * wgt;
+  }
+}
+
+}  // namespace dgx
+
+// ------------------------------------------------------------------ host launchers
+namespace dgx {
+void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
+                         double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st) {
+  int nb = (int)((ps.n + 127) / 128);
+  k_constitutive<<<nb, 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+}
+void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st) {
+  k_pav_finish<<<1, 32, 0, st>>>(Ppart, nblocks, wgt, Pav);
+}
+void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,
+                    TangentPartial* part, cudaStream_t st) {
+  int nb = (int)((ps.n + 63) / 64);
+  k_tangent<<<nb, 64, 0, st>>>(mp, ps, dt, dPdF, ld_out, part);
+}
+void launch_tangent_finish(const TangentPartial* part, int nblocks, double wgt, double* Cvol, double* Cmm,
+                           cudaStream_t st) {
+  k_tangent_finish<<<1, 96, 0, st>>>(part, nblocks, wgt, Cvol, Cmm);
+}
+}  // namespace dgx

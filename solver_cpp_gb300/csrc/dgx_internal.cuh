@@ -1,0 +1,66 @@
+// dgx_internal.cuh -- shared device/host definitions of the GB300 spectral solver.
+//
+// Layout in HBM (all FP64 unless stated):
+//   * a "field" of n material points with w components is stored component-planar:
+//     value(c, cell) = ptr[c * ld + cell], cell = x + N0 * (y + N1 * z), ld >= n.
+//     3x3 components use the reference's column-major index c = i + 3 * j.
+//   * per-point constitutive state is a set of such planes (structure of arrays).
+// The C ABI converts to and from the reference's interleaved (3,3,N) layout.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dgx {
+
+constexpr int NSLIP = 12;
+
+// Constitutive parameters of one phenopowerlaw cF phase, passed by value as a
+// kernel parameter (constant bank, broadcast to all threads).
+struct MatParams {
+  double C66[36];            // column-major 6x6, Voigt 11,22,33,23,13,12
+  double P[NSLIP][9];        // Schmid matrices d (x) n, column-major 3x3
+  double Psym[NSLIP][6];     // P11, P22, P33, P23+P32, P13+P31, P12+P21
+  double Q[NSLIP][9];        // C : P_alpha  (column-major 3x3)
+  double h[NSLIP][NSLIP];    // slip-slip interaction, h[reacting][acting]
+  double xi_inf, h0, n, gdot0, a, c1, c2;
+  double atol_xi, atol_gamma;
+  double r_cutback_min, r_cutback, r_increase, eps_rel_state;
+  double r_linesearch_Lp, eps_rel_Lp, eps_abs_Lp;
+  int N_iter_state_max, N_iter_Lp_max, f_update_jacobi_Lp;
+  int n_int;                 // n if it is an integer in [1, 64], else -1
+  int a_quarters;            // 4a if it is an integer in [1, 256], else -1
+};
+
+// Planes of the per-point constitutive state.  All pointers address component
+// planes with stride `ld`.
+struct PointState {
+  int64_t n, ld;
+  double* F;     // 9   current deformation gradient (phase F)
+  double* F0;    // 9   committed F (sub-step interpolation after a cut-back)
+  double* Fp0;   // 9   committed plastic deformation gradient
+  double* Lp0;   // 9   committed Lp
+  double* S0;    // 9   committed 2nd PK stress
+  double* st0;   // 24  committed state: xi (12) then gamma (12)
+  double* Fp;    // 9   out
+  double* Lp;    // 9   in: warm start, out: result
+  double* S;     // 9   out
+  double* Fe;    // 9   out
+  double* st;    // 24  out
+  double* P;     // 9   out: first Piola-Kirchhoff stress
+  int32_t* status;  // 0 converged, 1 terminally ill
+};
+
+// Per-block reduction record of the consistent tangent (C_volAvg, C_minMaxAvg).
+struct TangentPartial {
+  double sum[81];
+  double nmax, nmin;
+  long long imax, imin;
+  double dmax[81], dmin[81];
+};
+
+// Counters of constitutive work (for the FP64 roofline), accumulated per launch.
+struct ConsCounters {
+  unsigned long long state_iters, lp_iters, points;
+};
+
+}  // namespace dgx

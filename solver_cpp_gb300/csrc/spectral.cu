@@ -1,0 +1,493 @@
+// spectral.cu -- 3-D real FFTs of the 9-component tensor field on sm_103a, fused
+// with the Fourier-space Gamma convolution and the divergence-RMS reduction.
+//
+// Reference behaviour (reference paths):
+//   src/grid/fft.h:37-60, fft.cpp:9-78   unnormalised r2c / c2r of (3,3,N0,N1,N2) fields
+//   src/grid/spectral.cpp:53-130         xi1st (continuous / central difference), Nyquist zeroing
+//   src/grid/mech_base.cpp:302-398       divergence RMS with half-spectrum weights
+//   src/grid/mech_base.cpp:156-205, 400-477  Gamma_hat(xi; C_ref) : P_hat, zero frequency <- aim
+// Pipeline of one convolution (all FP64 in the plain form, FP32 spectrum in the
+// mixed form), spectrum stored component-planar, x-frequency fastest:
+//   x-pass  r2c of each x line               (real planes -> half spectrum)
+//   y-pass  complex FFT along y              (tile of x-frequencies, coalesced)
+//   z-pass  forward FFT along z, per-frequency div-RMS + Gamma, inverse FFT along z
+//           (all 9 components of a pencil tile resident in shared memory)
+//   y-pass  inverse
+//   x-pass  c2r (Hermitian extension), real planes out
+// Line FFTs are Stockham autosort (radix 4/2 butterflies with exact +-i, other
+// radices by a direct DFT) in shared memory with twiddles from a host table.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "dgx_internal.cuh"
+
+namespace dgx {
+
+template <typename T> struct cpx;
+template <> struct cpx<double> { typedef double2 t; };
+template <> struct cpx<float> { typedef float2 t; };
+
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+
+// FFT plan for one axis length (device constant data passed by value)
+struct AxisPlan {
+  int n, nstages;
+  int radix[16];
+  const double2* tw;      // exp(-2 pi i j / n), j < n  (FP64 table)
+  const float2* twf;      // same in FP32
+};
+
+template <typename R> __device__ __forceinline__ typename cpx<R>::t twid(const AxisPlan& p, long j, int sign) {
+  typename cpx<R>::t w;
+  int k = (int)(j % p.n);
+  if constexpr (sizeof(R) == 8) { double2 t = p.tw[k]; w.x = t.x; w.y = sign > 0 ? -t.y : t.y; }
+  else { float2 t = p.twf[k]; w.x = t.x; w.y = sign > 0 ? -t.y : t.y; }
+  return w;
+}
+
+// Stockham FFT of `nl` lines of length p.n, stored contiguously (line l at a + l*n).
+// Returns the buffer that holds the result (a or b).  sign -1 forward, +1 inverse.
+template <typename R>
+__device__ typename cpx<R>::t* block_fft(typename cpx<R>::t* a, typename cpx<R>::t* b, int nl, const AxisPlan& p, int sign) {
+  typedef typename cpx<R>::t C;
+  const int n = p.n;
+  int Ls = 1;
+  for (int s = 0; s < p.nstages; ++s) {
+    const int r = p.radix[s], m = n / r;
+    const int tot = nl * m;
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+      const int line = t / m, j = t - line * m;
+      const int k = j % Ls;
+      const C* in = a + (long)line * n;
+      C* out = b + (long)line * n;
+      const int od = (j / Ls) * Ls * r + k;
+      const long twstep = (long)(n / (Ls * r)) * k;
+      if (r == 2) {
+        C v0 = in[j], v1 = cmul(in[j + m], twid<R>(p, twstep, sign));
+        C y0, y1; y0.x = v0.x + v1.x; y0.y = v0.y + v1.y; y1.x = v0.x - v1.x; y1.y = v0.y - v1.y;
+        out[od] = y0; out[od + Ls] = y1;
+      } else if (r == 4) {
+        C v0 = in[j];
+        C v1 = cmul(in[j + m], twid<R>(p, twstep, sign));
+        C v2 = cmul(in[j + 2 * m], twid<R>(p, 2 * twstep, sign));
+        C v3 = cmul(in[j + 3 * m], twid<R>(p, 3 * twstep, sign));
+        C s02, d02, s13, d13;
+        s02.x = v0.x + v2.x; s02.y = v0.y + v2.y; d02.x = v0.x - v2.x; d02.y = v0.y - v2.y;
+        s13.x = v1.x + v3.x; s13.y = v1.y + v3.y; d13.x = v1.x - v3.x; d13.y = v1.y - v3.y;
+        // (v1 - v3) * (-i) forward, * (+i) inverse
+        C rot; if (sign < 0) { rot.x = d13.y; rot.y = -d13.x; } else { rot.x = -d13.y; rot.y = d13.x; }
+        C y0, y1, y2, y3;
+        y0.x = s02.x + s13.x; y0.y = s02.y + s13.y;
+        y2.x = s02.x - s13.x; y2.y = s02.y - s13.y;
+        y1.x = d02.x + rot.x; y1.y = d02.y + rot.y;
+        y3.x = d02.x - rot.x; y3.y = d02.y - rot.y;
+        out[od] = y0; out[od + Ls] = y1; out[od + 2 * Ls] = y2; out[od + 3 * Ls] = y3;
+      } else {
+        C v[16];
+        for (int q = 0; q < r; ++q) v[q] = cmul(in[j + q * m], twid<R>(p, (long)q * twstep, sign));
+        for (int s2 = 0; s2 < r; ++s2) {
+          C acc; acc.x = v[0].x; acc.y = v[0].y;
+          for (int q = 1; q < r; ++q) {
+            C w = twid<R>(p, (long)q * s2 * m, sign);
+            C t2 = cmul(v[q], w);
+            acc.x += t2.x; acc.y += t2.y;
+          }
+          out[od + s2 * Ls] = acc;
+        }
+      }
+    }
+    __syncthreads();
+    C* tmp = a; a = b; b = tmp;
+    Ls *= r;
+  }
+  return a;
+}
+
+struct SpecGeom {
+  int N0, N1, N2, N0r;
+  long long N, Nh;        // real points, half-spectrum points (per component)
+};
+
+// ---------------------------------------------------------------- x pass
+// forward: real planes (ld_in) -> spectrum planes (stride Nh); one block = LX lines
+template <typename R, typename Rin>
+__global__ void k_xfwd(SpecGeom g, AxisPlan px, const Rin* __restrict__ field, long long ld_in,
+                       typename cpx<R>::t* __restrict__ spec, int LX) {
+  typedef typename cpx<R>::t C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + (long)LX * g.N0;
+  const long long nlines = 9LL * g.N1 * g.N2;
+  const long long l0 = (long long)blockIdx.x * LX;
+  const int nl = (int)min((long long)LX, nlines - l0);
+  for (int t = threadIdx.x; t < nl * g.N0; t += blockDim.x) {
+    int l = t / g.N0, x = t - l * g.N0;
+    long long L = l0 + l;
+    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
+    C v; v.x = (R)field[c * ld_in + yz * g.N0 + x]; v.y = 0;
+    a[t] = v;
+  }
+  __syncthreads();
+  C* res = block_fft<R>(a, b, nl, px, -1);
+  for (int t = threadIdx.x; t < nl * g.N0r; t += blockDim.x) {
+    int l = t / g.N0r, i = t - l * g.N0r;
+    long long L = l0 + l;
+    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
+    spec[c * g.Nh + yz * g.N0r + i] = res[(long)l * g.N0 + i];
+  }
+}
+
+// inverse: spectrum -> real planes (ld_out), c2r by Hermitian extension.
+// If `accumulate`, out += scale * result (FP64 accumulation of an update).
+template <typename R, typename Rout>
+__global__ void k_xinv(SpecGeom g, AxisPlan px, const typename cpx<R>::t* __restrict__ spec, Rout* __restrict__ field,
+                       long long ld_out, int LX) {
+  typedef typename cpx<R>::t C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + (long)LX * g.N0;
+  const long long nlines = 9LL * g.N1 * g.N2;
+  const long long l0 = (long long)blockIdx.x * LX;
+  const int nl = (int)min((long long)LX, nlines - l0);
+  for (int t = threadIdx.x; t < nl * g.N0r; t += blockDim.x) {
+    int l = t / g.N0r, i = t - l * g.N0r;
+    long long L = l0 + l;
+    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
+    a[(long)l * g.N0 + i] = spec[c * g.Nh + yz * g.N0r + i];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nl * g.N0; t += blockDim.x) {
+    int l = t / g.N0, i = t - l * g.N0;
+    if (i >= g.N0r) { C v = a[(long)l * g.N0 + (g.N0 - i)]; v.y = -v.y; a[(long)l * g.N0 + i] = v; }
+  }
+  __syncthreads();
+  C* res = block_fft<R>(a, b, nl, px, +1);
+  for (int t = threadIdx.x; t < nl * g.N0; t += blockDim.x) {
+    int l = t / g.N0, x = t - l * g.N0;
+    long long L = l0 + l;
+    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
+    field[c * ld_out + yz * g.N0 + x] = (Rout)res[t].x;
+  }
+}
+
+// ---------------------------------------------------------------- y pass
+// block = (tile of TI x-frequencies) x (component, z); lines along y, stride N0r
+template <typename R>
+__global__ void k_ypass(SpecGeom g, AxisPlan py, typename cpx<R>::t* __restrict__ spec, int TI, int sign) {
+  typedef typename cpx<R>::t C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + (long)TI * g.N1;
+  const int ntile = (g.N0r + TI - 1) / TI;
+  const int tile = blockIdx.x % ntile;
+  const long long cz = blockIdx.x / ntile;           // c * N2 + z
+  const long long c = cz / g.N2, z = cz - c * g.N2;
+  const int i0 = tile * TI;
+  const int ti = min(TI, g.N0r - i0);
+  C* base = spec + c * g.Nh + z * (long long)g.N1 * g.N0r;
+  for (int t = threadIdx.x; t < ti * g.N1; t += blockDim.x) {
+    int y = t / ti, i = t - y * ti;
+    a[(long)i * g.N1 + y] = base[(long long)y * g.N0r + i0 + i];
+  }
+  __syncthreads();
+  C* res = block_fft<R>(a, b, ti, py, sign);
+  for (int t = threadIdx.x; t < ti * g.N1; t += blockDim.x) {
+    int y = t / ti, i = t - y * ti;
+    base[(long long)y * g.N0r + i0 + i] = res[(long)i * g.N1 + y];
+  }
+}
+
+// ---------------------------------------------------------------- z pass + Gamma + div
+struct GammaArgs {
+  const double* xi_x;     // N0r  (imaginary part of xi1st along x; continuous/central)
+  const double* xi_y;     // N1
+  const double* xi_z;     // N2
+  double resc[3];         // geom / scaled_geom
+  const double* C_ref;    // 81, device
+  const double* aim;      // 9, device (zero-frequency value), may be null when !gamma
+  int do_gamma, do_div;
+  int store_fwd;          // without gamma: write the forward z transform back
+  double* div_part;       // per block partial of the divergence sum (FP64)
+};
+
+template <typename R>
+__global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict__ spec, int TI, GammaArgs ga) {
+  typedef typename cpx<R>::t C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int per = TI * g.N2;                       // lines x length per component
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + 9L * per;
+  __shared__ double s_C[81];
+  __shared__ double s_red[256];
+  const int ntile = (g.N0r + TI - 1) / TI;
+  const int tile = blockIdx.x % ntile;
+  const int y = blockIdx.x / ntile;
+  const int i0 = tile * TI;
+  const int ti = min(TI, g.N0r - i0);
+  const long long zs = (long long)g.N1 * g.N0r;
+  for (int k = threadIdx.x; k < 81; k += blockDim.x) s_C[k] = ga.do_gamma ? ga.C_ref[k] : 0.0;
+  // load: line (c, i) at a + (c*ti + i) * N2
+  for (int t = threadIdx.x; t < 9 * ti * g.N2; t += blockDim.x) {
+    int c = t / (ti * g.N2), rem = t - c * ti * g.N2;
+    int z = rem / ti, i = rem - z * ti;
+    a[((long)c * ti + i) * g.N2 + z] = spec[c * g.Nh + z * zs + (long long)y * g.N0r + i0 + i];
+  }
+  __syncthreads();
+  C* res = block_fft<R>(a, b, 9 * ti, pz, -1);
+  C* other = (res == a) ? b : a;
+  double dsum = 0.0;
+  for (int t = threadIdx.x; t < ti * g.N2; t += blockDim.x) {
+    int i = t / g.N2, z = t - i * g.N2;
+    int ix = i0 + i;
+    double ax = ga.xi_x[ix], ay = ga.xi_y[y], az = ga.xi_z[z];
+    C Ph[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) Ph[c] = res[((long)c * ti + i) * g.N2 + z];
+    if (ga.do_div) {
+      double wgt = (ix == 0 ? 1.0 : 0.0) + (ix == g.N0r - 1 ? 1.0 : 0.0) + ((ix > 0 && ix < g.N0r - 1) ? 2.0 : 0.0);
+      double bx = ax * ga.resc[0], by = ay * ga.resc[1], bz = az * ga.resc[2];
+      double s = 0.0;
+#pragma unroll
+      for (int l = 0; l < 3; ++l) {
+        double ur = (double)Ph[l].x * bx + (double)Ph[l + 3].x * by + (double)Ph[l + 6].x * bz;
+        double ui = (double)Ph[l].y * bx + (double)Ph[l + 3].y * by + (double)Ph[l + 6].y * bz;
+        s += ur * ur + ui * ui;
+      }
+      dsum += wgt * s;
+    }
+    if (ga.do_gamma) {
+      C out[9];
+      if (ix == 0 && y == 0 && z == 0) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) { out[c].x = (R)ga.aim[c]; out[c].y = 0; }
+      } else {
+        double av[3] = {ax, ay, az};
+        double K[9];
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            double s = 0.0;
+#pragma unroll
+            for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+              for (int o = 0; o < 3; ++o) s = fma(s_C[l + 3 * nn + 9 * m + 27 * o], av[nn] * av[o], s);
+            K[l + 3 * m] = -s;
+          }
+        double c0 = K[4] * K[8] - K[7] * K[5], c1 = -K[1] * K[8] + K[7] * K[2], c2 = K[1] * K[5] - K[4] * K[2];
+        double det = K[0] * c0 + K[3] * c1 + K[6] * c2;
+        if (fabs(det) > 1e-16) {
+          double r = 1.0 / det;
+          double Ki[9] = {c0 * r, c1 * r, c2 * r,
+                          (-K[3] * K[8] + K[6] * K[5]) * r, (K[0] * K[8] - K[6] * K[2]) * r, (-K[0] * K[5] + K[3] * K[2]) * r,
+                          (K[3] * K[7] - K[6] * K[4]) * r, (-K[0] * K[7] + K[6] * K[1]) * r, (K[0] * K[4] - K[3] * K[1]) * r};
+          // v(n) = sum_o a_o P(n,o); w(l) = sum_n Kinv(l,n) v(n); out(l,m) = -a_m w(l)
+          double vr[3], vi[3];
+#pragma unroll
+          for (int nn = 0; nn < 3; ++nn) {
+            vr[nn] = ax * (double)Ph[nn].x + ay * (double)Ph[nn + 3].x + az * (double)Ph[nn + 6].x;
+            vi[nn] = ax * (double)Ph[nn].y + ay * (double)Ph[nn + 3].y + az * (double)Ph[nn + 6].y;
+          }
+#pragma unroll
+          for (int l = 0; l < 3; ++l) {
+            double wr = Ki[l] * vr[0] + Ki[l + 3] * vr[1] + Ki[l + 6] * vr[2];
+            double wi = Ki[l] * vi[0] + Ki[l + 3] * vi[1] + Ki[l + 6] * vi[2];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) { out[l + 3 * m].x = (R)(-av[m] * wr); out[l + 3 * m].y = (R)(-av[m] * wi); }
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 9; ++c) { out[c].x = 0; out[c].y = 0; }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 9; ++c) other[((long)c * ti + i) * g.N2 + z] = out[c];
+    }
+  }
+  if (ga.do_div) {
+    s_red[threadIdx.x] = dsum;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) s_red[threadIdx.x] += s_red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) ga.div_part[blockIdx.x] = s_red[0];
+  }
+  if (!ga.do_gamma) {
+    if (ga.store_fwd)
+      for (int t = threadIdx.x; t < 9 * ti * g.N2; t += blockDim.x) {
+        int c = t / (ti * g.N2), rem = t - c * ti * g.N2;
+        int z = rem / ti, i = rem - z * ti;
+        spec[c * g.Nh + z * zs + (long long)y * g.N0r + i0 + i] = res[((long)c * ti + i) * g.N2 + z];
+      }
+    return;
+  }
+  __syncthreads();
+  C* res2 = block_fft<R>(other, res, 9 * ti, pz, +1);
+  for (int t = threadIdx.x; t < 9 * ti * g.N2; t += blockDim.x) {
+    int c = t / (ti * g.N2), rem = t - c * ti * g.N2;
+    int z = rem / ti, i = rem - z * ti;
+    spec[c * g.Nh + z * zs + (long long)y * g.N0r + i0 + i] = res2[((long)c * ti + i) * g.N2 + z];
+  }
+}
+
+__global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt, int N0, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += part[b];
+    double r = sqrt(s) * wgt;
+    if (N0 == 1) r = r / 2.0;
+    *out = r;
+  }
+}
+
+}  // namespace dgx
+
+// ------------------------------------------------------------------ host side
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace dgx {
+
+static void twiddle(long j, long n, double* c, double* s) {
+  // cos/sin of 2 pi j / n, argument reduced to the first octant (quarter turns exact)
+  const double TAU = 6.283185307179586476925286766559;
+  j %= n; if (j < 0) j += n;
+  long q = (4 * j) / n, r = 4 * j - q * n;
+  double c0, s0;
+  if (r == 0) { c0 = 1.0; s0 = 0.0; }
+  else if (2 * r <= n) { double a = (TAU / 4.0) * ((double)r / (double)n); c0 = std::cos(a); s0 = std::sin(a); }
+  else { double a = (TAU / 4.0) * ((double)(n - r) / (double)n); c0 = std::sin(a); s0 = std::cos(a); }
+  switch (q) {
+    case 0: *c = c0; *s = s0; break;
+    case 1: *c = -s0; *s = c0; break;
+    case 2: *c = -c0; *s = -s0; break;
+    default: *c = s0; *s = -c0; break;
+  }
+}
+
+struct AxisHost {
+  AxisPlan plan;
+  double2* d_tw = nullptr;
+  float2* d_twf = nullptr;
+};
+
+static int factorize(int n, int* rad) {
+  int ns = 0, m = n;
+  while (m % 4 == 0) { rad[ns++] = 4; m /= 4; }
+  while (m % 2 == 0) { rad[ns++] = 2; m /= 2; }
+  for (int r = 3; m > 1 && ns < 16; r += 2)
+    while (m % r == 0) { rad[ns++] = r; m /= r; }
+  return m == 1 ? ns : -1;
+}
+
+bool axis_create(AxisHost* ax, int n) {
+  ax->plan.n = n;
+  int ns = factorize(n, ax->plan.radix);
+  if (ns < 0) return false;
+  for (int s = 0; s < ns; ++s) if (ax->plan.radix[s] > 16) return false;
+  ax->plan.nstages = ns;
+  std::vector<double2> tw(n);
+  std::vector<float2> twf(n);
+  for (int j = 0; j < n; ++j) {
+    double c, s;
+    twiddle(j, n, &c, &s);
+    tw[j] = make_double2(c, -s);
+    twf[j] = make_float2((float)c, (float)-s);
+  }
+  if (cudaMalloc(&ax->d_tw, sizeof(double2) * n) != cudaSuccess) return false;
+  if (cudaMalloc(&ax->d_twf, sizeof(float2) * n) != cudaSuccess) return false;
+  cudaMemcpy(ax->d_tw, tw.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(ax->d_twf, twf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+  ax->plan.tw = ax->d_tw;
+  ax->plan.twf = ax->d_twf;
+  return true;
+}
+
+void axis_destroy(AxisHost* ax) {
+  if (ax->d_tw) cudaFree(ax->d_tw);
+  if (ax->d_twf) cudaFree(ax->d_twf);
+  ax->d_tw = nullptr; ax->d_twf = nullptr;
+}
+
+// launch configuration shared by the spectral kernels
+struct SpecLaunch {
+  SpecGeom g;
+  int LX, TIy, TIz;
+  size_t smx, smy, smz;
+  int nbx, nby, nbz;
+};
+
+SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize) {
+  SpecLaunch L;
+  L.g.N0 = N0; L.g.N1 = N1; L.g.N2 = N2; L.g.N0r = N0 / 2 + 1;
+  L.g.N = (long long)N0 * N1 * N2;
+  L.g.Nh = (long long)L.g.N0r * N1 * N2;
+  L.LX = N0 >= 256 ? 1 : 256 / N0;
+  L.TIy = N1 >= 256 ? 1 : 256 / N1;
+  if (L.TIy > L.g.N0r) L.TIy = L.g.N0r;
+  L.TIz = N2 >= 256 ? 1 : 256 / N2;
+  if (L.TIz > L.g.N0r) L.TIz = L.g.N0r;
+  // keep the z-pass tile within 200 KB of shared memory (9 components x 2 buffers)
+  while (L.TIz > 1 && 2 * 9 * (size_t)L.TIz * N2 * csize > 200 * 1024) L.TIz /= 2;
+  L.smx = 2 * (size_t)L.LX * N0 * csize;
+  L.smy = 2 * (size_t)L.TIy * N1 * csize;
+  L.smz = 2 * 9 * (size_t)L.TIz * N2 * csize;
+  long long nlines = 9LL * N1 * N2;
+  L.nbx = (int)((nlines + L.LX - 1) / L.LX);
+  L.nby = ((L.g.N0r + L.TIy - 1) / L.TIy) * 9 * N2;
+  L.nbz = ((L.g.N0r + L.TIz - 1) / L.TIz) * N1;
+  return L;
+}
+
+template <typename R>
+static void set_smem_limits(const SpecLaunch& L) {
+  cudaFuncSetAttribute(k_zpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smz);
+  cudaFuncSetAttribute(k_ypass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smy);
+  cudaFuncSetAttribute(k_xfwd<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smx);
+  cudaFuncSetAttribute(k_xinv<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smx);
+}
+
+void spec_prepare(const SpecLaunch& L, bool fp32) {
+  if (fp32) set_smem_limits<float>(L);
+  else set_smem_limits<double>(L);
+}
+
+// forward transform (x, y passes) of 9 real planes into the spectrum buffer
+template <typename R>
+static void fwd_xy(const SpecLaunch& L, const AxisPlan& px, const AxisPlan& py, const double* field, long long ld,
+                   void* spec, cudaStream_t st) {
+  typedef typename cpx<R>::t C;
+  k_xfwd<R, double><<<L.nbx, 256, L.smx, st>>>(L.g, px, field, ld, (C*)spec, L.LX);
+  k_ypass<R><<<L.nby, 256, L.smy, st>>>(L.g, py, (C*)spec, L.TIy, -1);
+}
+
+// full convolution: in (9 planes, ld) -> Gamma * in written to field; div RMS
+// partials into ga.div_part (nbz blocks)
+void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                   const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st) {
+  if (fp32) {
+    fwd_xy<float>(L, px, py, in, ld, spec, st);
+    k_zpass<float><<<L.nbz, 256, L.smz, st>>>(L.g, pz, (float2*)spec, L.TIz, ga);
+    if (ga.do_gamma) {
+      k_ypass<float><<<L.nby, 256, L.smy, st>>>(L.g, py, (float2*)spec, L.TIy, +1);
+      k_xinv<float, double><<<L.nbx, 256, L.smx, st>>>(L.g, px, (const float2*)spec, field, ld, L.LX);
+    }
+  } else {
+    fwd_xy<double>(L, px, py, in, ld, spec, st);
+    k_zpass<double><<<L.nbz, 256, L.smz, st>>>(L.g, pz, (double2*)spec, L.TIz, ga);
+    if (ga.do_gamma) {
+      k_ypass<double><<<L.nby, 256, L.smy, st>>>(L.g, py, (double2*)spec, L.TIy, +1);
+      k_xinv<double, double><<<L.nbx, 256, L.smx, st>>>(L.g, px, (const double2*)spec, field, ld, L.LX);
+    }
+  }
+}
+
+void spec_div_finish(const double* part, int nb, double wgt, int N0, double* out, cudaStream_t st) {
+  k_div_finish<<<1, 32, 0, st>>>(part, nb, wgt, N0, out);
+}
+
+}  // namespace dgx

@@ -1,0 +1,155 @@
+"""GPU parity: the sm_103a path through the C ABI against the CPU oracle.
+
+Tolerance (FP64 plain form): 1e-8 relative, normalised by the largest magnitude
+of the compared quantity (the bound required of the GPU drop-in).  Observed
+agreement is ~1e-12; the kernels reorder FP64 sums and use exact algebraic
+rewrites (rank-12 Jacobian, Fi = I), so bitwise equality is not expected.
+"""
+import numpy as np
+import pytest
+
+from oracle import dgo
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-8
+
+
+def rel(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import solver_cpp_gb300 as g
+    from solver_cpp_gb300 import build
+    build.build()
+    return g
+
+
+def test_constitutive_sequence_vs_oracle(gpu):
+    cells = (4, 4, 4)
+    n = 64
+    from solver_cpp_gb300.synthetic import microstructure
+    mat_at, q = microstructure(cells, 5, seed=11)
+    rve = gpu.RVE(cells, (1, 1, 1), mat_at, q)
+    ops = dgo.PointSet(dgo.material(), q[mat_at])
+    rng = np.random.default_rng(3)
+    for k in range(1, 5):
+        F = np.eye(3)[None] * 1.0 + 1e-4 * rng.standard_normal((n, 3, 3))
+        F[:, 0, 0] += 1.5e-3 * k
+        F[:, 1, 1] -= 0.5e-3 * k
+        F[:, 2, 2] -= 0.5e-3 * k
+        dt = 0.5
+        P, dPdF = rve.constitutive_response(F, dt, want_dPdF=True)
+        ill = ops.response(dgo.fortran9(F), dt, True)
+        assert not ill and not rve.terminally_ill
+        assert rel(P, dgo.from_fortran9(ops.field("P"))) < TOL
+        for name in ("Fp", "Lp", "S"):
+            assert rel(rve.get(name), dgo.from_fortran9(ops.field(name))) < TOL, name
+        assert rel(rve.get("xi"), ops.field("xi", 12)) < TOL
+        d_or = ops.field("dPdF", 81).reshape(n, 3, 3, 3, 3, order="C").transpose(0, 4, 3, 2, 1)
+        assert rel(dPdF, d_or) < 1e-7
+        Pav, Cv, Cm = rve.averages()
+        P_av, Cv_o, Cm_o = dgo.averages(ops.field("P"), ops.field("dPdF", 81))
+        assert rel(Pav, dgo.from_fortran9(P_av)) < TOL
+        assert rel(Cv.ravel(order="F"), Cv_o) < 1e-7
+        assert rel(Cm.ravel(order="F"), Cm_o) < 1e-7
+        rve.commit()
+        ops.commit()
+
+
+def test_fft_forward_vs_numpy(gpu):
+    rng = np.random.default_rng(5)
+    for cells in [(6, 7, 8), (16, 8, 4), (2, 1, 1), (5, 3, 9), (32, 32, 32)]:
+        N0, N1, N2 = cells
+        rve = gpu.RVE(cells, (1, 1, 1), np.zeros(N0 * N1 * N2, int), [[1, 0, 0, 0]])
+        f = rng.standard_normal((N2, N1, N0, 3, 3))
+        spec = rve.fft_forward(f.reshape(-1, 3, 3))                  # (N1, N2, N0r, 3, 3)
+        ref = np.fft.rfftn(f, axes=(0, 1, 2))                          # (N2, N1, N0r, 3, 3)
+        assert rel(spec, np.transpose(ref, (1, 0, 2, 3, 4))) < 1e-13
+
+
+def test_divergence_rms_golden_and_oracle(gpu, knowns):
+    # MechBaseTestDivergenceRMS: 4x1x1, mock scaled geometry (4,1,1) == size+grid here
+    k = knowns["divergence_rms_4x1x1"]
+    field = np.asarray(k["field"])[:, :, :, 0, 0]                      # (3, 3, 4)
+    P = np.transpose(field, (2, 0, 1))
+    rve = gpu.RVE((4, 1, 1), (4e-5, 1e-5, 1e-5), np.zeros(4, int), [[1, 0, 0, 0]])
+    assert rve.calculate_divergence_rms(P) == pytest.approx(k["rms"], rel=1e-14, abs=0)
+    rng = np.random.default_rng(9)
+    for cells in [(6, 7, 8), (16, 16, 16), (9, 4, 5)]:
+        n = int(np.prod(cells))
+        P = rng.standard_normal((n, 3, 3)) * 1e7
+        size = (0.75, 0.875, 1.0)
+        rve = gpu.RVE(cells, size, np.zeros(n, int), [[1, 0, 0, 0]])
+        x1, _ = dgo.xi(cells, size, 0)
+        sg = dgo.scaled_geom(cells, size, "size+grid")
+        r_or = dgo.divergence_rms(cells, size, sg, x1, dgo.fortran9(P))
+        assert rve.calculate_divergence_rms(P) == pytest.approx(r_or, rel=1e-12)
+
+
+def test_gamma_convolution_vs_oracle(gpu):
+    cells = (8, 6, 5)
+    n = int(np.prod(cells))
+    from solver_cpp_gb300.synthetic import microstructure
+    mat_at, q = microstructure(cells, 4, seed=2)
+    rve = gpu.RVE(cells, (1.0, 0.75, 0.625), mat_at, q)
+    rve.init()
+    C_ref = rve.get("C_ref").ravel(order="F")
+    rng = np.random.default_rng(4)
+    P = 1e7 * rng.standard_normal((n, 3, 3))
+    aim = 1e-4 * rng.standard_normal((3, 3))
+    out = rve.gamma_convolution(P, aim)
+    x1, _ = dgo.xi(cells, (1.0, 0.75, 0.625), 0)
+    ref = dgo.gamma_convolution(cells, x1, C_ref, dgo.fortran9(aim[None])[0], dgo.fortran9(P))
+    assert rel(out, dgo.from_fortran9(ref.reshape(n, 9))) < 1e-11
+
+
+def _compare_runs(recs_g, recs_o, tol):
+    assert len(recs_g) == len(recs_o)
+    for rg, ro in zip(recs_g, recs_o):
+        assert rel(rg["P_av"], dgo.from_fortran9(ro["P_av"])) < tol
+        assert rel(rg["F_av"], dgo.from_fortran9(ro["F_av"])) < tol
+        assert rg["iterations"] == ro["iterations"]
+
+
+def test_solver_6grains_vs_oracle_and_damask(gpu):
+    fx = cases.damask_6grains()
+    rve = gpu.RVE(fx["cells"], fx["size"], fx["material_at"], fx["orientations"])
+    recs = rve.loop_over_loadcase([gpu.load_step("tensionY", t=20.0, N=40, f_out=4)])
+    s = dgo.Solver(fx["cells"], fx["size"], fx["material_at"], fx["orientations"])
+    ro = s.run([dgo.loadstep("tensionY", t=20.0, N=40, f_out=4)])
+    _compare_runs(recs, ro, TOL)
+    for name, key in (("F", "F"), ("P", "P"), ("F_p", "Fp"), ("L_p", "Lp")):
+        assert rel(rve.get(key), dgo.from_fortran9(s.get(key))) < TOL, name
+        assert rel(rve.get(key), fx[f"{name}_40"]) < 1e-9, name
+    for k, inc in enumerate(fx["increments"]):
+        if inc:
+            assert rel(recs[inc - 1]["P_av"], fx["P_av"][k]) < 1e-9
+
+
+def test_solver_16cube_20grains_vs_oracle(gpu):
+    cells, size, mat_at = cases.grains16()
+    q = __import__("solver_cpp_gb300.synthetic", fromlist=["x"]).random_quaternions(20, 2024)
+    rve = gpu.RVE(cells, size, mat_at, q)
+    recs = rve.loop_over_loadcase([gpu.load_step("tensionX", t=10.0, N=10)])
+    s = dgo.Solver(cells, size, mat_at, q)
+    ro = s.run([dgo.loadstep("tensionX", t=10.0, N=10)])
+    _compare_runs(recs, ro, TOL)
+    for key in ("F", "P", "Fp"):
+        assert rel(rve.get(key), dgo.from_fortran9(s.get(key))) < TOL, key
+
+
+def test_mixed_precision_error_bound(gpu):
+    cells, size, mat_at = cases.grains16()
+    q = __import__("solver_cpp_gb300.synthetic", fromlist=["x"]).random_quaternions(20, 2024)
+    ref = gpu.RVE(cells, size, mat_at, q)
+    mixed = gpu.RVE(cells, size, mat_at, q, num=gpu.numerics(precision="mixed"))
+    steps = [gpu.load_step("tensionX", t=6.0, N=6)]
+    a = ref.loop_over_loadcase(steps)
+    b = mixed.loop_over_loadcase(steps)
+    for ra, rb in zip(a, b):
+        assert rel(rb["P_av"], ra["P_av"]) < 1e-5
