@@ -16,6 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdgx.so")
 SOURCES = ["constitutive.cu", "spectral.cu", "solver.cu"]
+HOST_SOURCES = ["ref_stiffness.cpp"]
 HEADERS = ["dgx_internal.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -28,7 +29,9 @@ def nvcc():
 
 
 def _flags(verbose_ptxas=False):
-    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")] + ARCH
+    # host code keeps the reference's FP64 rounding (no FMA contraction); device code is unaffected
+    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "-I", os.path.join(ROOT, "include")] + ARCH
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]
     return f
@@ -36,7 +39,10 @@ def _flags(verbose_ptxas=False):
 
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + _flags(verbose_ptxas)
+    if src.endswith(".cpp"):
+        cmd = ["g++", "-c", os.path.join(CSRC, src), "-o", obj, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
+    else:
+        cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + _flags(verbose_ptxas)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -45,14 +51,14 @@ def _compile(src, verbose_ptxas=False):
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS] + [os.path.join(ROOT, "include", "dgx.h"),
+    deps = [os.path.join(CSRC, s) for s in SOURCES + HOST_SOURCES + HEADERS] + [os.path.join(ROOT, "include", "dgx.h"),
                                                                    os.path.abspath(__file__)]
     if not force and not verbose_ptxas and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES))
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + len(HOST_SOURCES)) as ex:
+        results = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES + HOST_SOURCES))
     if verbose_ptxas:
         for _, log in results:
             sys.stderr.write(log)

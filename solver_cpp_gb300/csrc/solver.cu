@@ -54,6 +54,10 @@ void spec_div_finish(const double* part, int nb, double wgt, int N0, double* out
 
 using namespace dgx;
 
+// ref_stiffness.cpp
+extern "C" int dgx_reference_stiffness(double C11, double C12, double C44, int n_mat, const double* q,
+                                       const int32_t* material_at, int64_t N, double* C_minMaxAvg);
+
 // ------------------------------------------------------------------ errors
 static thread_local std::string g_err;
 static void set_err(const char* fmt, ...) {
@@ -434,6 +438,9 @@ struct dgx_rve {
   double* d_dPdF = nullptr;        // optional (81 planes) for the boundary call
   int32_t* d_mat = nullptr;
   double* d_Rm = nullptr;
+  int n_materials = 0;
+  std::vector<int32_t> h_mat;
+  std::vector<double> h_orient;
   AxisHost ax[3];
   SpecLaunch sl{};
   int nb_cons = 0, nb_tan = 0, nb_red = 0;
@@ -855,6 +862,9 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
     }
   }
   // orientations -> initial Fp per material
+  r->n_materials = n_materials;
+  r->h_mat.assign(material_at, material_at + N);
+  r->h_orient.assign(orientations, orientations + 4 * (size_t)n_materials);
   {
     std::vector<double> Rm(9 * (size_t)n_materials);
     for (int m2 = 0; m2 < n_materials; ++m2) qu2om(orientations + 4 * m2, Rm.data() + 9 * m2);
@@ -980,11 +990,23 @@ extern "C" dgx_status dgx_fft_forward(dgx_rve* r, const double* field, double* s
 
 extern "C" dgx_status dgx_solver_init(dgx_rve* r) {
   if (!r) return DGX_ERR_ARG;
+  // fresh material-point state (init of the reference runs on a fresh state)
+  k_init_points<<<nblk(r->N), 256, 0, r->st>>>(r->ps, r->d_mat, r->d_Rm, r->n_materials, r->mat.xi_0);
   k_fill_identity<<<nblk(9 * r->N), 256, 0, r->st>>>(r->X, r->N);
   k_fill_identity<<<nblk(9 * r->N), 256, 0, r->st>>>(r->F_last_inc, r->N);
-  r->n_launch += 2;
+  r->n_launch += 3;
+  for (int k = 0; k < 9; ++k) {
+    r->F_aim[k] = r->F_aim_last_inc[k] = (k % 4) == 0 ? 1.0 : 0.0;
+    r->F_aim_dot[k] = 0.0; r->P_aim[k] = 0.0;
+  }
   r->terminally_ill = 0;
   TRY(constitutive_response(r, r->X, 0.0, true));
+  // the argmax/argmin of |dPdF| at F = I is a tie broken by FP64 rounding: take it
+  // with the reference's operation order (see ref_stiffness.cpp)
+  if (dgx_reference_stiffness(r->mat.C11, r->mat.C12, r->mat.C44, r->n_materials, r->h_orient.data(),
+                              r->h_mat.data(), r->N, r->C_minMaxAvg) != 0) {
+    set_err("reference stiffness selection failed"); return DGX_ERR_STATE;
+  }
   for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
   CK(cudaMemcpy(r->d_Cref, r->C_ref, 81 * sizeof(double), cudaMemcpyHostToDevice));
   memcpy(r->C_minMaxAvgLastInc, r->C_minMaxAvg, sizeof(r->C_minMaxAvg));
