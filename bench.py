@@ -1,0 +1,320 @@
+#!/usr/bin/env python
+"""Point-updates/s of the DAMASK_grid spectral-basic solver (phenopowerlaw cF) on GB300.
+
+Workload (the plain-FP64 GPU configuration of the benchmark definition): 64^3 cells,
+200 grains from a seeded periodic Voronoi tessellation with uniformly random
+orientations, single-phase cF phenopowerlaw (C11 106.75 GPa, C12 60.41 GPa,
+C44 28.34 GPa, xi_0 31 MPa, xi_inf 63 MPa, h_0 75 MPa, n 20, dot_gamma_0 1e-3/s,
+a 2.25, h_sl-sl [1,1,1.4,1.4,1.4,1.4,1.4]), uniaxial tension in x (dot_F_xx =
+1e-3/s, P_yy = P_zz = 0), 40 increments over 40 s, FP64 end to end.
+
+One "step" is one load increment (a full NGMRES solve of the increment).
+The point-update is one material point's constitutive evaluation plus its share
+of one residual evaluation (FFT -> div-RMS/Gamma -> iFFT, reductions, NGMRES
+vector work): value = N_cells x (residual evaluations) / time.
+
+  value  : K increments, state resident in HBM, timed with CUDA events on the
+           solver's stream (state + NGMRES history ~1.3 GB >> 129 MB L2).
+  e2e    : the same through the public C ABI with every increment's result
+           fields (P and F, 2 x 9N doubles) copied to host memory inside the
+           timed region; byte counts are the library's own copy counters.
+  --impl reference : the CPU oracle (plain-C restatement of the reference path,
+           all host threads) on the same workload; the reference itself cannot
+           be built on this image (Fortran/PETSc/FFTW toolchain absent).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "point-updates/s, mixed vs FP64 GPU at ≤1e-5 rel. P error; p50/p99 RVE latency"
+UNIT = "point-updates/s"
+SEED = 42
+
+# algorithmic FP64 flops of the constitutive kernel's restatement (FMA = 2), per unit:
+#   every Lp iteration (B, Fe, Hooke S, 12-system kinetics, Lp, residual norms)   724
+#   every Lp Jacobian + 9x9 LU solve (rank-12 J: 12 x (WQ_a + 6x9 FMA), LU)       2535
+#   every state iteration (dotState, damper, state update, stress-call overhead)   1400
+FLOPS_LP, FLOPS_JAC, FLOPS_STATE = 724.0, 2535.0, 1400.0
+# DRAM traffic of one constitutive launch per cell, from the ncu capture summarised in
+# profiles/constitutive_64cube.md (dram__bytes_read.sum + dram__bytes_write.sum / cells)
+TRAFFIC_BYTES_PER_CELL = None
+
+
+def args_():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--cells", type=int, default=64)
+    p.add_argument("--grains", type=int, default=200)
+    p.add_argument("--increments", type=int, default=40)
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--no-extras", action="store_true", help="skip e2e / mixed / CPU-baseline legs")
+    p.add_argument("--cpu-sample-increments", type=int, default=1)
+    return p.parse_args()
+
+
+def workload(a):
+    from solver_cpp_gb300.synthetic import microstructure
+    cells = (a.cells, a.cells, a.cells)
+    mat_at, q = microstructure(cells, a.grains, SEED)
+    return cells, (1.0, 1.0, 1.0), mat_at, q
+
+
+def config(a):
+    return {"workload": f"{a.cells}^3 cells, {a.grains} Voronoi grains (seed {SEED}), phenopowerlaw cF, "
+                        f"tension x 1e-3/s, {a.increments} increments over {float(a.increments):g} s",
+            "cells": a.cells, "grains": a.grains, "increments": a.increments, "step": "one load increment",
+            "precision": a.precision, "solver": "NGMRES (PETSc SNESNGMRES defaults)",
+            "l2": "inputs larger than L2 (resident state + NGMRES history > 1 GB)"}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+
+
+# ---------------------------------------------------------------- CPU oracle timing
+def oracle_increments(a, count, threads):
+    """Run `count` increments of the workload on the CPU oracle (load case restarted
+    from a fresh solve every `a.increments` increments); per-increment records."""
+    from oracle import dgo
+    cells, size, mat_at, q = workload(a)
+    recs = []
+    while len(recs) < count:
+        take = min(a.increments, count - len(recs))
+        s = dgo.Solver(cells, size, mat_at, q, nthreads=threads)
+        recs += s.run([dgo.loadstep("tensionX", t=float(take), N=take)])
+    return recs
+
+
+def cpu_oracle_sample(a, increments, threads):
+    cells, _, _, _ = workload(a)
+    n = cells[0] * cells[1] * cells[2]
+    recs = oracle_increments(a, increments, threads)
+    dt = sum(r["seconds"] for r in recs)
+    ev = sum(r["evaluations"] for r in recs)
+    return n * ev / dt, dt, ev, recs
+
+
+def reference_arm(a):
+    rank, world = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    cells, _, _, _ = workload(a)
+    n = cells[0] * cells[1] * cells[2]
+    recs = oracle_increments(a, a.warmup + a.steps, threads)
+    timed = recs[a.warmup:]
+    total_t = sum(r["seconds"] for r in timed)
+    total_ev = sum(r["evaluations"] for r in timed)
+    value = n * total_ev / total_t if total_t > 0 else 0.0
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * total_t / max(1, a.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Voronoi + uniform SO(3) orientations)", "config": config(a),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{a.steps} increments of the {a.cells}^3 workload after {a.warmup} warm-up "
+                                       "increments (CPU oracle, OpenMP over cells; reference not buildable here)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- clocks sampling
+class Clocks:
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, nm in enumerate(names):
+                if len(s) > 4 + k and s[4 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_increments(rve, step, start, count, n_inc, read_back=False):
+    """Run `count` increments starting at global index `start` (load case cycled)."""
+    lat = []
+    for i in range(start, start + count):
+        inc = i % n_inc
+        if inc == 0:
+            rve.init()
+        t0 = time.perf_counter()
+        rec = rve.run_increment(step, 0, inc)
+        if read_back:
+            rve.get("P"); rve.get("F")
+        lat.append(time.perf_counter() - t0)
+    return lat
+
+
+def gpu_arm(a):
+    import torch
+    rank, world = dist_env()
+    if world > 1:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import ctypes as C
+    import solver_cpp_gb300 as g
+    from solver_cpp_gb300 import build, dgx
+    build.build()
+    cells, size, mat_at, q = workload(a)
+    n = cells[0] * cells[1] * cells[2]
+    num = g.numerics(precision=a.precision)
+    step = g.load_step("tensionX", t=float(a.increments), N=a.increments)
+
+    peak = C.c_double(0.0)
+    dgx.check(dgx.lib().dgx_measure_fp64_peak(C.byref(peak), None), "fp64 peak")
+
+    rve = g.RVE(cells, size, mat_at, q, num=num)
+    stream = torch.cuda.ExternalStream(rve.stream)
+    run_increments(rve, step, 0, a.warmup, a.increments)
+    c0, t0 = rve.counters(), rve.timers()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(); clocks.start()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0.record(stream)
+    lat = run_increments(rve, step, a.warmup, a.steps, a.increments)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    c1, t1 = rve.counters(), rve.timers()
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    evals = c1["evaluations"] - c0["evaluations"]
+    value = n * evals * world / (ms * 1e-3)
+    # roofline of the dominant kernel (constitutive, FP64-bound)
+    d_lp = c1["lp_iterations"] - c0["lp_iterations"]
+    d_jac = c1["jacobians"] - c0["jacobians"]
+    d_st = c1["state_iterations"] - c0["state_iterations"]
+    launches = t1["constitutive_launches"] - t0["constitutive_launches"]
+    kms = t1["constitutive_ms"] - t0["constitutive_ms"]
+    flops = FLOPS_LP * d_lp + FLOPS_JAC * d_jac + FLOPS_STATE * d_st
+    achieved = flops / (kms * 1e-3) / 1e12 if kms > 0 else 0.0
+    traffic = TRAFFIC_BYTES_PER_CELL * n if TRAFFIC_BYTES_PER_CELL else None
+    spec_ms = t1["spectral_ms"] - t0["spectral_ms"]
+    spec_n = t1["spectral_launches"] - t0["spectral_launches"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if a.precision == "fp64" else "f64+f32", "data": "synthetic (seeded Voronoi + uniform "
+            "SO(3) orientations; inputs generated in-process)", "config": config(a),
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
+                         "kernel": "k_constitutive", "flops_per_launch": flops / max(1, launches),
+                         "ms_per_launch": kms / max(1, launches),
+                         "peak_source": "measured: dgx_measure_fp64_peak DFMA probe (MEASURED_PEAKS.json has no FP64)"},
+            "kernel_time_share": {"constitutive": kms / ms, "spectral": spec_ms / ms,
+                                  "spectral_ms_per_residual": spec_ms / max(1, spec_n)},
+            "evaluations_per_increment": evals / a.steps,
+            "latency": {"p50_increment_ms": 1e3 * statistics.median(lat),
+                        "p99_increment_ms": 1e3 * sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))]},
+            "gpu_launches": c1["launches"] - c0["launches"], "clocks": ck}
+    rve.close()
+    if not a.no_extras and rank == 0:
+        # e2e through the public API with results read back to host each increment
+        rve2 = g.RVE(cells, size, mat_at, q, num=num)
+        run_increments(rve2, step, 0, a.warmup, a.increments, read_back=True)
+        c0 = rve2.counters()
+        t_e = time.perf_counter()
+        run_increments(rve2, step, a.warmup, a.steps, a.increments, read_back=True)
+        t_e = time.perf_counter() - t_e
+        c1 = rve2.counters()
+        rve2.close()
+        line["e2e"] = {"value": n * (c1["evaluations"] - c0["evaluations"]) / t_e, "unit": UNIT,
+                       "h2d_bytes_per_step": (c1["h2d_bytes"] - c0["h2d_bytes"]) / a.steps,
+                       "d2h_bytes_per_step": (c1["d2h_bytes"] - c0["d2h_bytes"]) / a.steps,
+                       "note": "public C-ABI increments, P and F fields copied to host every step"}
+        # mixed precision form on the same workload: throughput and P_av error vs FP64
+        if a.precision == "fp64":
+            ref = g.RVE(cells, size, mat_at, q, num=g.numerics(precision="fp64"))
+            mix = g.RVE(cells, size, mat_at, q, num=g.numerics(precision="mixed"))
+            m_inc = min(a.increments, 10)
+            ref.init(); mix.init()
+            errs, tm, evm = [], 0.0, 0
+            for inc in range(m_inc):
+                ra = ref.run_increment(step, 0, inc)
+                c0 = mix.counters()
+                torch.cuda.synchronize(); ts = time.perf_counter()
+                rb = mix.run_increment(step, 0, inc)
+                torch.cuda.synchronize(); tm += time.perf_counter() - ts
+                evm += mix.counters()["evaluations"] - c0["evaluations"]
+                errs.append(float(abs(rb["P_av"] - ra["P_av"]).max() / abs(ra["P_av"]).max()))
+            line["mixed"] = {"value": n * evm / tm, "unit": UNIT, "increments": m_inc,
+                             "max_rel_P_av_error_vs_fp64": max(errs), "per_increment_error": errs}
+            ref.close(); mix.close()
+        if rank == 0:
+            threads = os.cpu_count() or 1
+            try:
+                v, dt, ev, _ = cpu_oracle_sample(a, a.cpu_sample_increments, threads)
+                line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                        "sample": f"solver init + first {a.cpu_sample_increments} increment(s) of the "
+                                                  f"{a.cells}^3 workload ({ev} residual evaluations, {dt:.1f} s), "
+                                                  "CPU oracle with OpenMP over cells"}
+            except Exception as ex:  # the baseline is reported, never required
+                line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": threads, "kind": "port",
+                                        "sample": f"failed: {ex}"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = args_()
+    if a.impl == "reference":
+        from oracle import build as ob
+        ob.build()
+        reference_arm(a)
+        return
+    gpu_arm(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -142,8 +142,18 @@ dgx_status dgx_get(dgx_rve* rve, const char* name, double* out);
 
 /* Work counters since creation: [0] residual evaluations, [1] constitutive
  * state (FPI) iterations, [2] Lp Newton iterations, [3] tangent evaluations,
- * [4] kernel launches issued by the library. */
-dgx_status dgx_counters(const dgx_rve* rve, int64_t out[5]);
+ * [4] kernel launches issued by the library, [5] Lp Jacobian factorisations,
+ * [6] host-to-device bytes, [7] device-to-host bytes copied by the library. */
+dgx_status dgx_counters(const dgx_rve* rve, int64_t out[8]);
+/* CUDA-event time (ms, accumulated) and launch counts of [0] the constitutive
+ * kernel, [1] the spectral chain (FFT + Gamma + div-RMS), [2] the tangent kernel,
+ * measured on the RVE's stream. */
+dgx_status dgx_timers(const dgx_rve* rve, double ms[3], int64_t launches[3]);
+/* The CUDA stream (cudaStream_t) all work of the RVE is queued on. */
+void* dgx_rve_stream(const dgx_rve* rve);
+/* FP64 FMA throughput of the current device (TFLOP/s, best of 5), the
+ * denominator of the constitutive kernel's roofline.  No reference counterpart. */
+dgx_status dgx_measure_fp64_peak(double* tflops, double* ms);
 
 #ifdef __cplusplus
 }

@@ -148,6 +148,7 @@ typedef struct dgo_inc_record {
   double P_av[9], F_aim[9], F_av[9];
   int    iterations, evaluations, converged, cutbacks;
   double err_div, err_BC;
+  double seconds;               /* wall time of the increment */
 } dgo_inc_record;
 
 /* runs all load steps; returns number of increments recorded (<0 on error) */

@@ -56,7 +56,8 @@ class LoadStep(C.Structure):
 class IncRecord(C.Structure):
     _fields_ = [("t", C.c_double), ("dt", C.c_double), ("P_av", C.c_double * 9), ("F_aim", C.c_double * 9),
                 ("F_av", C.c_double * 9), ("iterations", C.c_int), ("evaluations", C.c_int),
-                ("converged", C.c_int), ("cutbacks", C.c_int), ("err_div", C.c_double), ("err_BC", C.c_double)]
+                ("converged", C.c_int), ("cutbacks", C.c_int), ("err_div", C.c_double), ("err_BC", C.c_double),
+                ("seconds", C.c_double)]
 
 
 def _p(a):
@@ -351,7 +352,7 @@ class Solver:
         for r in recs[:n]:
             out.append(dict(t=r.t, dt=r.dt, P_av=np.array(r.P_av[:]), F_aim=np.array(r.F_aim[:]),
                             F_av=np.array(r.F_av[:]), iterations=r.iterations, evaluations=r.evaluations,
-                            cutbacks=r.cutbacks, err_div=r.err_div, err_BC=r.err_BC))
+                            cutbacks=r.cutbacks, err_div=r.err_div, err_BC=r.err_BC, seconds=r.seconds))
         return out
 
     def get(self, name):

@@ -21,6 +21,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -425,6 +426,8 @@ int dgo_solver_run(dgo_solver* s, int nsteps, const dgo_loadstep* steps, dgo_inc
       dt = forward_time(dt, ls, inc, sub_step_factor, cut_back_level);
       int step_fraction = 0, iters = 0, cutbacks = 0;
       int64_t ev0 = s->evaluations;
+      struct timespec ts0, ts1;
+      clock_gettime(CLOCK_MONOTONIC, &ts0);
       while (step_fraction < (int)pow(sub_step_factor, cut_back_level)) {
         t_remaining = ls->t + t_0 - t;
         t += dt;
@@ -444,7 +447,9 @@ int dgo_solver_run(dgo_solver* s, int nsteps, const dgo_loadstep* steps, dgo_inc
         }
       }
       cut_back_level = cut_back - 1 > 0 ? cut_back - 1 : 0;
+      clock_gettime(CLOCK_MONOTONIC, &ts1);
       if (rec && nrec < max_rec) {
+        rec[nrec].seconds = (double)(ts1.tv_sec - ts0.tv_sec) + 1e-9 * (double)(ts1.tv_nsec - ts0.tv_nsec);
         dgo_inc_record* r = &rec[nrec];
         r->t = t; r->dt = dt;
         memcpy(r->P_av, s->P_av, sizeof(r->P_av));

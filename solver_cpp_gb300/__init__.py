@@ -181,9 +181,21 @@ class RVE:
         return _unf9(out, self.N) if width == 9 else out.reshape(self.N, width)
 
     def counters(self):
-        a = (C.c_int64 * 5)()
+        a = (C.c_int64 * 8)()
         _d.check(_d.lib().dgx_counters(self.h, a), "dgx_counters")
-        return dict(evaluations=a[0], state_iterations=a[1], lp_iterations=a[2], tangents=a[3], launches=a[4])
+        return dict(evaluations=a[0], state_iterations=a[1], lp_iterations=a[2], tangents=a[3], launches=a[4],
+                    jacobians=a[5], h2d_bytes=a[6], d2h_bytes=a[7])
+
+    def timers(self):
+        ms = (C.c_double * 3)(); n = (C.c_int64 * 3)()
+        _d.check(_d.lib().dgx_timers(self.h, ms, n), "dgx_timers")
+        return dict(constitutive_ms=ms[0], spectral_ms=ms[1], tangent_ms=ms[2], constitutive_launches=n[0],
+                    spectral_launches=n[1], tangent_launches=n[2])
+
+    @property
+    def stream(self):
+        """cudaStream_t of this RVE (as an int), e.g. for torch.cuda.ExternalStream."""
+        return int(_d.lib().dgx_rve_stream(self.h) or 0)
 
 
 def _record(r):

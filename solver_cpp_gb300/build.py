@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdgx.so")
-SOURCES = ["constitutive.cu", "spectral.cu", "solver.cu"]
+SOURCES = ["constitutive.cu", "spectral.cu", "solver.cu", "peak.cu"]
 HOST_SOURCES = ["ref_stiffness.cpp"]
 HEADERS = ["dgx_internal.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

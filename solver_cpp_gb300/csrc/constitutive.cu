@@ -192,7 +192,7 @@ __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) 
 // P, S, Lp, Fp (regularised), Fe.
 __device__ bool integrate_stress(const MatParams& mp, const double* F, const double* Fp0, double dt,
                                  const double* xi, double* Lp, double* S, double* P, double* Fp, double* Fe,
-                                 unsigned* lp_iters) {
+                                 unsigned* lp_iters, unsigned* jac_iters) {
   double invFp0[9], A[9];
   if (!inv33(Fp0, invFp0)) return true;
   mm(F, invFp0, A);
@@ -242,6 +242,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* F, const dou
     }
     if (jaco % mp.f_update_jacobi_Lp == 0) {
       ++jaco;
+      (*jac_iters)++;
       // J[3k+l][3p+q] = delta + dt |dg_a| P_a(k,l) (W Q_a)(p,q), W = A^T Fe
       double W[9];
       mtm(A, Fe_, W);
@@ -309,7 +310,7 @@ __device__ __forceinline__ double damper(const double* o0, const double* o1, con
 // first dot state (restored committed stress); state in/out.
 __device__ bool integrate_state(const MatParams& mp, const double* F, const double* Fp0, const double* state0,
                                 double dt, double* state, double* Lp, double* S, double* P, double* Fp,
-                                double* Fe, unsigned* lp_iters, unsigned* st_iters) {
+                                double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters) {
   double dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
   (*st_iters)++;
   dot_state(mp, S, state, dot);
@@ -323,7 +324,7 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) { last2[i] = it > 1 ? last1[i] : 0.0; last1[i] = dot[i]; }
-    broken = integrate_stress(mp, F, Fp0, dt, state, Lp, S, P, Fp, Fe, lp_iters);
+    broken = integrate_stress(mp, F, Fp0, dt, state, Lp, S, P, Fp, Fe, lp_iters, jac_iters);
     if (broken) break;
     dot_state(mp, S, state, dot);
     bool nan = false;
@@ -355,7 +356,7 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
                double* __restrict__ Ppart, int* __restrict__ ill, ConsCounters* cnt) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   double P[9];
-  unsigned lp_iters = 0, st_iters = 0;
+  unsigned lp_iters = 0, st_iters = 0, jac_iters = 0;
   bool ok = true;
   if (e < ps.n) {
     double F[9], F0c[9], Fphase0[9], Fp0[9], Lp[9], Lp0[9], S[9], S0[9], state0[2 * NSLIP], state[2 * NSLIP];
@@ -402,7 +403,8 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
       if (todo) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
-        converged = !integrate_state(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &st_iters);
+        converged = !integrate_state(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &jac_iters,
+                                     &st_iters);
       }
     }
     ok = converged;
@@ -437,11 +439,16 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
   if (threadIdx.x < 9) Ppart[blockIdx.x * 9 + threadIdx.x] = red[threadIdx.x][0];
   if (cnt) {
     // per-warp aggregation of the work counters
-    unsigned lp = lp_iters, st = st_iters;
-    for (int o = 16; o > 0; o >>= 1) { lp += __shfl_down_sync(0xffffffffu, lp, o); st += __shfl_down_sync(0xffffffffu, st, o); }
+    unsigned lp = lp_iters, st = st_iters, jc = jac_iters;
+    for (int o = 16; o > 0; o >>= 1) {
+      lp += __shfl_down_sync(0xffffffffu, lp, o);
+      st += __shfl_down_sync(0xffffffffu, st, o);
+      jc += __shfl_down_sync(0xffffffffu, jc, o);
+    }
     if ((threadIdx.x & 31) == 0) {
       atomicAdd(&cnt->lp_iters, (unsigned long long)lp);
       atomicAdd(&cnt->state_iters, (unsigned long long)st);
+      atomicAdd(&cnt->jac_iters, (unsigned long long)jc);
     }
   }
 }

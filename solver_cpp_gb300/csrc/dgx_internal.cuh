@@ -60,7 +60,7 @@ struct TangentPartial {
 
 // Counters of constitutive work (for the FP64 roofline), accumulated per launch.
 struct ConsCounters {
-  unsigned long long state_iters, lp_iters, points;
+  unsigned long long state_iters, lp_iters, jac_iters, points;
 };
 
 }  // namespace dgx

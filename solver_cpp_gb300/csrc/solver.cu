@@ -460,9 +460,25 @@ struct dgx_rve {
   int guess = 0, cur_step = -1;
   // counters
   int64_t n_eval = 0, n_tangent = 0, n_launch = 0;
+  // CUDA-event timers on the RVE stream: [0] constitutive kernel, [1] spectral chain, [2] tangent
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double t_ms[3] = {0, 0, 0};
+  int64_t t_n[3] = {0, 0, 0};
+  bool timing = true;
+  int64_t bytes_h2d = 0, bytes_d2h = 0;
 };
 
 namespace {
+
+// counted host<->device copies on the RVE stream (bytes per direction)
+inline cudaError_t h2d(dgx_rve* r, void* dst, const void* src, size_t bytes) {
+  r->bytes_h2d += (int64_t)bytes;
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, r->st);
+}
+inline cudaError_t d2h(dgx_rve* r, void* dst, const void* src, size_t bytes) {
+  r->bytes_d2h += (int64_t)bytes;
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, r->st);
+}
 
 template <typename T>
 dgx_status dalloc(dgx_rve* r, T** p, size_t count) {
@@ -488,7 +504,7 @@ dgx_status multi(dgx_rve* r, int mode, const double* a, const double* b, const s
   k_multi<<<r->nb_red, RB, 0, r->st>>>(mode, a, b, vl, K, K2, n, r->d_redpart);
   k_multi_finish<<<1, 64, 0, r->st>>>(r->d_redpart, r->nb_red, K + K2, r->d_redout);
   r->n_launch += 2;
-  CK(cudaMemcpyAsync(out, r->d_redout, sizeof(double) * (K + K2), cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, out, r->d_redout, sizeof(double) * (K + K2)));
   CK(cudaStreamSynchronize(r->st));
   return DGX_OK;
 }
@@ -503,27 +519,36 @@ dgx_status norm2(dgx_rve* r, const double* v, double* out) {
 dgx_status constitutive_response(dgx_rve* r, const double* X, double dt, bool want_tangent) {
   r->n_eval++;
   CK(cudaMemsetAsync(r->d_ill, 0, sizeof(int), r->st));
+  if (r->timing) cudaEventRecord(r->ev[0], r->st);
   launch_constitutive(r->mp, r->ps, X, r->N, dt, r->d_Ppart, r->d_ill, r->d_cnt, r->st);
+  if (r->timing) cudaEventRecord(r->ev[1], r->st);
   launch_pav_finish(r->d_Ppart, r->nb_cons, r->wgt, r->d_Pav, r->st);
   r->n_launch += 2;
   r->tangent_fresh = false;
   r->tangent_dt = dt;
   if (want_tangent) {
+    if (r->timing) cudaEventRecord(r->ev[4], r->st);
     launch_tangent(r->mp, r->ps, dt, r->d_dPdF, r->N, r->d_tpart, r->st);
+    if (r->timing) cudaEventRecord(r->ev[5], r->st);
     launch_tangent_finish(r->d_tpart, r->nb_tan, r->wgt, r->d_Cvol, r->d_Cmm, r->st);
     r->n_launch += 2;
     r->n_tangent++;
     r->tangent_fresh = true;
   }
   int ill = 0;
-  CK(cudaMemcpyAsync(r->P_av, r->d_Pav, 9 * sizeof(double), cudaMemcpyDeviceToHost, r->st));
-  CK(cudaMemcpyAsync(&ill, r->d_ill, sizeof(int), cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, r->P_av, r->d_Pav, 9 * sizeof(double)));
+  CK(d2h(r, &ill, r->d_ill, sizeof(int)));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
+  if (r->timing) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]); r->t_ms[0] += ms; r->t_n[0]++;
+    if (want_tangent) { cudaEventElapsedTime(&ms, r->ev[4], r->ev[5]); r->t_ms[2] += ms; r->t_n[2]++; }
+  }
   if (ill) r->terminally_ill = 1;
   if (want_tangent) {
-    CK(cudaMemcpy(r->C_volAvg, r->d_Cvol, 81 * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(r->C_minMaxAvg, r->d_Cmm, 81 * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(d2h(r, r->C_volAvg, r->d_Cvol, 81 * sizeof(double))); CK(cudaStreamSynchronize(r->st));
+    CK(d2h(r, r->C_minMaxAvg, r->d_Cmm, 81 * sizeof(double))); CK(cudaStreamSynchronize(r->st));
   }
   if (!(r->rot_q[0] == 1.0 && r->rot_q[1] == 0.0 && r->rot_q[2] == 0.0 && r->rot_q[3] == 0.0)) {
     double t[9];
@@ -540,8 +565,8 @@ dgx_status ensure_tangent(dgx_rve* r) {
   launch_tangent_finish(r->d_tpart, r->nb_tan, r->wgt, r->d_Cvol, r->d_Cmm, r->st);
   r->n_launch += 2;
   r->n_tangent++;
-  CK(cudaMemcpyAsync(r->C_volAvg, r->d_Cvol, 81 * sizeof(double), cudaMemcpyDeviceToHost, r->st));
-  CK(cudaMemcpyAsync(r->C_minMaxAvg, r->d_Cmm, 81 * sizeof(double), cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, r->C_volAvg, r->d_Cvol, 81 * sizeof(double)));
+  CK(d2h(r, r->C_minMaxAvg, r->d_Cmm, 81 * sizeof(double)));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
   r->tangent_fresh = true;
@@ -574,15 +599,21 @@ dgx_status form_residual(dgx_rve* r, const double* X, double* Rv) {
   r->err_BC = err;
   double rot[9];
   rotate2(r->rot_q, dF, rot, true);
-  CK(cudaMemcpyAsync(r->d_aim, rot, 9 * sizeof(double), cudaMemcpyHostToDevice, r->st));
+  CK(h2d(r, r->d_aim, rot, 9 * sizeof(double)));
   GammaArgs ga = gamma_args(r, true, true);
+  if (r->timing) cudaEventRecord(r->ev[2], r->st);
   spec_convolve(r->sl, r->num.precision == 1, r->ax[0].plan, r->ax[1].plan, r->ax[2].plan, r->ps.P, Rv, r->N, r->spec,
                 ga, r->st);
   spec_div_finish(r->d_divpart, r->sl.nbz, r->wgt, r->cells[0], r->d_rms, r->st);
+  if (r->timing) cudaEventRecord(r->ev[3], r->st);
   r->n_launch += 6;
-  CK(cudaMemcpyAsync(&r->err_div, r->d_rms, sizeof(double), cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, &r->err_div, r->d_rms, sizeof(double)));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
+  if (r->timing) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r->ev[2], r->ev[3]); r->t_ms[1] += ms; r->t_n[1]++;
+  }
   return DGX_OK;
 }
 
@@ -659,7 +690,7 @@ dgx_status snes_solve(dgx_rve* r, int* reason_out) {
     for (int i = 0; i < l; ++i) alph += beta[i];
     VecList xl{};
     for (int i = 0; i < l; ++i) xl.v[i] = r->Xdot[i];
-    CK(cudaMemcpyAsync(r->d_beta, beta.data(), sizeof(double) * l, cudaMemcpyHostToDevice, r->st));
+    CK(h2d(r, r->d_beta, beta.data(), sizeof(double) * l));
     k_combine<<<r->nb_red, 256, 0, r->st>>>(r->XA, r->XM, xl, l, 1.0 - alph, r->d_beta, n9);
     r->n_launch++;
     TRY(form_residual(r, r->XA, r->FA));
@@ -725,14 +756,14 @@ dgx_status commit(dgx_rve* r) {
 
 dgx_status upload_aos(dgx_rve* r, const double* host, int w, double* planar) {
   double* tmp = r->XM;                        // scratch: 9N doubles (w <= 9)
-  CK(cudaMemcpyAsync(tmp, host, sizeof(double) * w * r->N, cudaMemcpyHostToDevice, r->st));
+  CK(h2d(r, tmp, host, sizeof(double) * w * r->N));
   k_aos2planar<<<nblk(w * r->N), 256, 0, r->st>>>(tmp, w, r->N, planar, r->N);
   r->n_launch++;
   return DGX_OK;
 }
 dgx_status download_aos(dgx_rve* r, const double* planar, int w, double* host) {
   std::vector<double> tmp((size_t)w * r->N);
-  CK(cudaMemcpyAsync(tmp.data(), planar, sizeof(double) * w * r->N, cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, tmp.data(), planar, sizeof(double) * w * r->N));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
   for (int64_t e = 0; e < r->N; ++e)
@@ -771,6 +802,7 @@ extern "C" void dgx_rve_destroy(dgx_rve* r) {
   if (!r) return;
   for (auto p : r->allocs) cudaFree(p);
   for (int i = 0; i < 3; ++i) axis_destroy(&r->ax[i]);
+  for (int i = 0; i < 6; ++i) if (r->ev[i]) cudaEventDestroy(r->ev[i]);
   if (r->owns_stream && r->st) cudaStreamDestroy(r->st);
   delete r;
 }
@@ -808,6 +840,7 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
   cudaError_t ce = cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking);
   if (ce != cudaSuccess) { set_err("cudaStreamCreate: %s", cudaGetErrorString(ce)); delete r; return DGX_ERR_CUDA; }
   r->owns_stream = true;
+  for (int i = 0; i < 6; ++i) cudaEventCreate(&r->ev[i]);
   const int64_t N = r->N;
   dgx_status s = DGX_OK;
 #define AL(p, c) do { s = dalloc(r, p, c); if (s != DGX_OK) { dgx_rve_destroy(r); return s; } } while (0)
@@ -933,7 +966,7 @@ extern "C" dgx_status dgx_commit_increment(dgx_rve* r) {
 extern "C" dgx_status dgx_update_gamma(dgx_rve* r, const double C[81]) {
   if (!r || !C) return DGX_ERR_ARG;
   for (int k = 0; k < 81; ++k) r->C_ref[k] = C[k] / r->wgt;
-  CK(cudaMemcpy(r->d_Cref, r->C_ref, 81 * sizeof(double), cudaMemcpyHostToDevice));
+  CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
   return DGX_OK;
 }
 
@@ -945,7 +978,7 @@ extern "C" dgx_status dgx_divergence_rms(dgx_rve* r, const double* P, double* rm
                 ga, r->st);
   spec_div_finish(r->d_divpart, r->sl.nbz, r->wgt, r->cells[0], r->d_rms, r->st);
   r->n_launch += 4;
-  CK(cudaMemcpyAsync(rms, r->d_rms, sizeof(double), cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, rms, r->d_rms, sizeof(double)));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
   return DGX_OK;
@@ -954,7 +987,7 @@ extern "C" dgx_status dgx_divergence_rms(dgx_rve* r, const double* P, double* rm
 extern "C" dgx_status dgx_gamma_convolution(dgx_rve* r, double* field, const double aim[9]) {
   if (!r || !field || !aim) return DGX_ERR_ARG;
   TRY(upload_aos(r, field, 9, r->XA));
-  CK(cudaMemcpyAsync(r->d_aim, aim, 9 * sizeof(double), cudaMemcpyHostToDevice, r->st));
+  CK(h2d(r, r->d_aim, aim, 9 * sizeof(double)));
   GammaArgs ga = gamma_args(r, true, false);
   spec_convolve(r->sl, r->num.precision == 1, r->ax[0].plan, r->ax[1].plan, r->ax[2].plan, r->XA, r->XA, r->N, r->spec,
                 ga, r->st);
@@ -974,7 +1007,7 @@ extern "C" dgx_status dgx_fft_forward(dgx_rve* r, const double* field, double* s
   r->n_launch += 3;
   const SpecGeom& g = r->sl.g;
   std::vector<double2> h(9 * g.Nh);
-  CK(cudaMemcpyAsync(h.data(), r->spec, sizeof(double2) * 9 * g.Nh, cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, h.data(), r->spec, sizeof(double2) * 9 * g.Nh));
   CK(cudaStreamSynchronize(r->st));
   // device: spec[c*Nh + i + N0r*(y + N1*z)] -> reference (l,m,i,k=z,j=y) interleaved
   for (int c = 0; c < 9; ++c)
@@ -1008,7 +1041,7 @@ extern "C" dgx_status dgx_solver_init(dgx_rve* r) {
     set_err("reference stiffness selection failed"); return DGX_ERR_STATE;
   }
   for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
-  CK(cudaMemcpy(r->d_Cref, r->C_ref, 81 * sizeof(double), cudaMemcpyHostToDevice));
+  CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
   memcpy(r->C_minMaxAvgLastInc, r->C_minMaxAvg, sizeof(r->C_minMaxAvg));
   memcpy(r->C_volAvgLastInc, r->C_volAvg, sizeof(r->C_volAvg));
   r->initialized = true;
@@ -1061,11 +1094,11 @@ extern "C" dgx_status dgx_solver_forward(dgx_rve* r, int32_t cutback, int32_t gu
   k_plane_sums<<<r->nb_red, RB, 0, r->st>>>(r->X, N, r->d_redpart);
   k_multi_finish<<<1, 64, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
   double sums[9];
-  CK(cudaMemcpyAsync(sums, r->d_redout, 9 * sizeof(double), cudaMemcpyDeviceToHost, r->st));
+  CK(d2h(r, sums, r->d_redout, 9 * sizeof(double)));
   CK(cudaStreamSynchronize(r->st));
   double diff[9];
   for (int k = 0; k < 9; ++k) diff[k] = sums[k] * r->wgt - rot[k];
-  CK(cudaMemcpyAsync(r->d_redout, diff, 9 * sizeof(double), cudaMemcpyHostToDevice, r->st));
+  CK(h2d(r, r->d_redout, diff, 9 * sizeof(double)));
   k_shift_planes<<<nblk(9 * N), 256, 0, r->st>>>(r->X, r->d_redout, N);
   r->n_launch += 4;
   memcpy(r->stress_mask, ls->stress_mask, sizeof(r->stress_mask));
@@ -1082,7 +1115,7 @@ extern "C" dgx_status dgx_solver_solve(dgx_rve* r, int32_t* conv, int32_t* itera
   masked_compliance(r->C_volAvg, r->rot_q, r->stress_mask, r->S);
   if (r->num.update_gamma) {
     for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
-    CK(cudaMemcpy(r->d_Cref, r->C_ref, 81 * sizeof(double), cudaMemcpyHostToDevice));
+    CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
   }
   int reason = 0;
   TRY(snes_solve(r, &reason));
@@ -1131,7 +1164,7 @@ static dgx_status run_one_increment(dgx_rve* r, const dgx_loadstep* ls, int l, i
     k_multi_finish<<<1, 64, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
     r->n_launch += 2;
     double sums[9];
-    CK(cudaMemcpyAsync(sums, r->d_redout, 9 * sizeof(double), cudaMemcpyDeviceToHost, r->st));
+    CK(d2h(r, sums, r->d_redout, 9 * sizeof(double)));
     CK(cudaStreamSynchronize(r->st));
     for (int k = 0; k < 9; ++k) rec->F_av[k] = sums[k] * r->wgt;
     rec->iterations = iters; rec->evaluations = (int32_t)(r->n_eval - ev0);
@@ -1189,11 +1222,19 @@ extern "C" dgx_status dgx_get(dgx_rve* r, const char* name, double* out) {
   return download_aos(r, planar, w, out);
 }
 
-extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[5]) {
+extern "C" void* dgx_rve_stream(const dgx_rve* r) { return r ? (void*)r->st : nullptr; }
+
+extern "C" dgx_status dgx_timers(const dgx_rve* r, double ms[3], int64_t launches[3]) {
+  if (!r || !ms) return DGX_ERR_ARG;
+  for (int i = 0; i < 3; ++i) { ms[i] = r->t_ms[i]; if (launches) launches[i] = r->t_n[i]; }
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[8]) {
   if (!r || !out) return DGX_ERR_ARG;
   ConsCounters c{};
   CK(cudaMemcpy(&c, r->d_cnt, sizeof(c), cudaMemcpyDeviceToHost));
   out[0] = r->n_eval; out[1] = (int64_t)c.state_iters; out[2] = (int64_t)c.lp_iters; out[3] = r->n_tangent;
-  out[4] = r->n_launch;
+  out[4] = r->n_launch; out[5] = (int64_t)c.jac_iters; out[6] = r->bytes_h2d; out[7] = r->bytes_d2h;
   return DGX_OK;
 }

@@ -51,7 +51,8 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_rve_points", "dgx_rve_device_bytes", "dgx_constitutive_response", "dgx_averages",
            "dgx_commit_increment", "dgx_divergence_rms", "dgx_gamma_convolution", "dgx_update_gamma",
            "dgx_fft_forward", "dgx_solver_init", "dgx_solver_forward", "dgx_solver_solve", "dgx_run_loadcase",
-           "dgx_run_increment", "dgx_get", "dgx_counters"]
+           "dgx_run_increment", "dgx_get", "dgx_counters", "dgx_timers", "dgx_rve_stream",
+           "dgx_measure_fp64_peak"]
 
 
 class DgxError(RuntimeError):
@@ -94,10 +95,14 @@ def lib():
     L.dgx_run_increment.argtypes = [vp, C.POINTER(LoadStep), C.c_int32, C.c_int32, C.POINTER(IncRecord)]
     L.dgx_get.argtypes = [vp, C.c_char_p, dp]
     L.dgx_counters.argtypes = [vp, i64p]
+    L.dgx_timers.argtypes = [vp, dp, i64p]
+    L.dgx_rve_stream.argtypes = [vp]
+    L.dgx_rve_stream.restype = vp
+    L.dgx_measure_fp64_peak.argtypes = [dp, dp]
     for name in SYMBOLS:
         f = getattr(L, name)
         if name not in ("dgx_material_default", "dgx_numerics_default", "dgx_rve_destroy", "dgx_last_error",
-                        "dgx_rve_points", "dgx_rve_device_bytes"):
+                        "dgx_rve_points", "dgx_rve_device_bytes", "dgx_rve_stream"):
             f.restype = C.c_int32
     _lib = L
     return L
