@@ -70,15 +70,15 @@ __device__ __forceinline__ double nrm9(const double* a) {
   return sqrt(s);
 }
 
-// x^n for small integer n by binary powering, x^(q/4) via square roots
-__device__ __forceinline__ double pow_n(double x, const MatParams& mp) {
+// x^(n-1) for small integer n by binary powering, x^(q/4) via square roots
+__device__ __forceinline__ double pow_nm1(double x, const MatParams& mp) {
   if (mp.n_int > 0) {
-    int e = mp.n_int;
+    int e = mp.n_int - 1;
     double r = 1.0, b = x;
     while (e) { if (e & 1) r *= b; b *= b; e >>= 1; }
     return r;
   }
-  return pow(x, mp.n);
+  return pow(x, mp.n - 1.0);
 }
 __device__ __forceinline__ double pow_a(double y, const MatParams& mp) {
   if (mp.a_quarters > 0) {
@@ -97,39 +97,43 @@ __device__ __forceinline__ double pow_a(double y, const MatParams& mp) {
   return pow(y, mp.a);
 }
 
-// Hooke: S = C : E(Fe), E = (Fe^T Fe - I)/2, S symmetric (Voigt)
+// cF <110>{111} slip systems of the reference's table (crystal.f90:41-63) as
+// compile-time signs: P_a(k,l) = pval * d_a[k] * n_a[l], d, n in {-1,0,1}^3.
+// Encoded as digits (value + 1) so that unrolled loops fold them into constants.
+__host__ __device__ constexpr int fcc_d(int a, int k) { return "120012201100212021102010221122210001"[3 * a + k] - '1'; }
+__host__ __device__ constexpr int fcc_n(int a, int l) { return "222222222002002002200200200020020020"[3 * a + l] - '1'; }
+__host__ __device__ constexpr int fcc_s(int a, int k, int l) { return fcc_d(a, k) * fcc_n(a, l); }
+
+// Hooke for the cubic stiffness: S = C : E(Fe), E = (Fe^T Fe - I)/2 (symmetric)
 __device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, double* S) {
-  double e6[6];
   double E00 = 0.5 * (Fe[0] * Fe[0] + Fe[1] * Fe[1] + Fe[2] * Fe[2] - 1.0);
   double E11 = 0.5 * (Fe[3] * Fe[3] + Fe[4] * Fe[4] + Fe[5] * Fe[5] - 1.0);
   double E22 = 0.5 * (Fe[6] * Fe[6] + Fe[7] * Fe[7] + Fe[8] * Fe[8] - 1.0);
   double E12 = 0.5 * (Fe[3] * Fe[6] + Fe[4] * Fe[7] + Fe[5] * Fe[8]);
   double E02 = 0.5 * (Fe[0] * Fe[6] + Fe[1] * Fe[7] + Fe[2] * Fe[8]);
   double E01 = 0.5 * (Fe[0] * Fe[3] + Fe[1] * Fe[4] + Fe[2] * Fe[5]);
-  e6[0] = E00; e6[1] = E11; e6[2] = E22; e6[3] = 2.0 * E12; e6[4] = 2.0 * E02; e6[5] = 2.0 * E01;
-  double s6[6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    double s = 0.0;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) s = fma(mp.C66[i + 6 * j], e6[j], s);
-    s6[i] = s;
-  }
-  S[0] = s6[0]; S[4] = s6[1]; S[8] = s6[2];
-  S[5] = S[7] = s6[3]; S[2] = S[6] = s6[4]; S[1] = S[3] = s6[5];
+  double tr = E00 + E11 + E22;
+  S[0] = fma(mp.C11mC12, E00, mp.C12 * tr);
+  S[4] = fma(mp.C11mC12, E11, mp.C12 * tr);
+  S[8] = fma(mp.C11mC12, E22, mp.C12 * tr);
+  S[5] = S[7] = mp.C44x2 * E12;
+  S[2] = S[6] = mp.C44x2 * E02;
+  S[1] = S[3] = mp.C44x2 * E01;
 }
 
-// resolved shear, slip rates and |d gdot / d tau| on the 12 systems (Mp = S)
+// resolved shear, slip rates and |d gdot / d tau| on the 12 systems (Mp = S).
+// Division free: with r = |tau|/xi, gdot = gdot0 r^n and |dgdot/dtau| = n gdot0 r^(n-1) / xi.
 __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, const double* rxi,
                                          double* gdot, double* dg) {
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
     double tau = mp.Psym[a][0] * S[0] + mp.Psym[a][1] * S[4] + mp.Psym[a][2] * S[8]
                + mp.Psym[a][3] * S[5] + mp.Psym[a][4] * S[2] + mp.Psym[a][5] * S[1];
-    double t = fabs(tau);
-    double g = mp.gdot0 * pow_n(t * rxi[a], mp);
+    double r = fabs(tau) * rxi[a];
+    double p = pow_nm1(r, mp);               // r^(n-1)
+    double g = mp.gdot0 * (r * p);
     gdot[a] = tau > 0.0 ? g : -g;
-    if (dg) dg[a] = (g > 2.2250738585072014e-307) ? g * mp.n / t : 0.0;   // |dgdot/dtau|
+    if (dg) dg[a] = (g > 2.2250738585072014e-307) ? mp.ngdot0 * (rxi[a] * p) : 0.0;
   }
 }
 
@@ -143,7 +147,7 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
   for (int a = 0; a < NSLIP; ++a) g[a] = fabs(g[a]);
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
-    double x = 1.0 - xi[a] / mp.xi_inf;
+    double x = 1.0 - xi[a] * mp.rxi_inf;
     double left = copysign(pow_a(fabs(x), mp), x);
     double hs = 0.0;
 #pragma unroll
@@ -157,6 +161,7 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
 // for nrhs right-hand sides stored column by column in B (B[c * 9 + r]).
 __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) {
   int piv[9];
+  double rp[9];                                  // reciprocal pivots: one division per pivot
   for (int k = 0; k < 9; ++k) {
     int p = k;
     double mx = fabs(M[9 * k + k]);
@@ -169,6 +174,7 @@ __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) 
     if (p != k)
       for (int j = 0; j < 9; ++j) { double t = M[9 * k + j]; M[9 * k + j] = M[9 * p + j]; M[9 * p + j] = t; }
     double r = 1.0 / M[9 * k + k];
+    rp[k] = r;
     for (int i = k + 1; i < 9; ++i) {
       double l = M[9 * i + k] * r;
       M[9 * i + k] = l;
@@ -182,7 +188,7 @@ __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) 
     for (int i = 8; i >= 0; --i) {
       double s = x[i];
       for (int j = i + 1; j < 9; ++j) s = fma(-M[9 * i + j], x[j], s);
-      x[i] = s / M[9 * i + i];
+      x[i] = s * rp[i];
     }
   }
   return true;
@@ -214,23 +220,32 @@ __device__ bool integrate_stress(const MatParams& mp, const double* F, const dou
     hooke_S(mp, Fe_, S);
     double gdot[NSLIP], dg[NSLIP];
     kinetics(mp, S, rxi, gdot, dg);
+    // Lp = sum_a gdot_a P_a with the cF sparsity folded at compile time
     double Lpc[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      double s = 0.0;
+    for (int k = 0; k < 3; ++k)
 #pragma unroll
-      for (int a = 0; a < NSLIP; ++a) s = fma(gdot[a], mp.P[a][k], s);
-      Lpc[k] = s;
-    }
+      for (int l = 0; l < 3; ++l) {
+        double s = 0.0;
+#pragma unroll
+        for (int a = 0; a < NSLIP; ++a) {
+          if (fcc_s(a, k, l) > 0) s += gdot[a];
+          else if (fcc_s(a, k, l) < 0) s -= gdot[a];
+        }
+        Lpc[k + 3 * l] = mp.pval * s;
+      }
     double res[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) res[k] = Lpg[k] - Lpc[k];
-    double nLg = nrm9(Lpg), nLc = nrm9(Lpc), nr = nrm9(res);
-    double atol = fmax(mp.eps_rel_Lp * fmax(nLg, nLc), mp.eps_abs_Lp);
-    if (isnan(nr)) return true;
-    if (nr < atol) break;
-    if (it == 1 || nr < res_old_n) {
-      res_old_n = nr;
+    // convergence tests on squared norms (no square roots)
+    double nLg2 = 0.0, nLc2 = 0.0, nr2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nLc2 = fma(Lpc[k], Lpc[k], nLc2); nr2 = fma(res[k], res[k], nr2); }
+    double atol2 = fmax(mp.eps_rel_Lp2 * fmax(nLg2, nLc2), mp.eps_abs_Lp2);
+    if (isnan(nr2)) return true;
+    if (nr2 < atol2) break;
+    if (it == 1 || nr2 < res_old_n) {
+      res_old_n = nr2;
 #pragma unroll
       for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
       step = 1.0;
@@ -243,23 +258,24 @@ __device__ bool integrate_stress(const MatParams& mp, const double* F, const dou
     if (jaco % mp.f_update_jacobi_Lp == 0) {
       ++jaco;
       (*jac_iters)++;
-      // J[3k+l][3p+q] = delta + dt |dg_a| P_a(k,l) (W Q_a)(p,q), W = A^T Fe
+      // J[3k+l][3p+q] = delta + dt |dg_a| P_a(k,l) (W Q_a)(p,q), W = A^T Fe;
+      // P_a(k,l) = pval * s_a(k,l) with compile-time signs s in {-1,0,1}
       double W[9];
       mtm(A, Fe_, W);
       double J[81];
 #pragma unroll
       for (int k = 0; k < 81; ++k) J[k] = (k % 10) == 0 ? 1.0 : 0.0;
+#pragma unroll
       for (int a = 0; a < NSLIP; ++a) {
-        double c = dt * dg[a];
-        if (c == 0.0) continue;
+        double c = (dt * mp.pval) * dg[a];
         double V[9];
         mm(W, mp.Q[a], V);
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
           for (int l = 0; l < 3; ++l) {
-            double pc = c * mp.P[a][k + 3 * l];
-            if (pc == 0.0) continue;
+            if (fcc_s(a, k, l) == 0) continue;
+            double pc = fcc_s(a, k, l) > 0 ? c : -c;
 #pragma unroll
             for (int p = 0; p < 3; ++p)
 #pragma unroll
@@ -289,9 +305,9 @@ __device__ bool integrate_stress(const MatParams& mp, const double* F, const dou
   double dFp = Fp_new[0] * (Fp_new[4] * Fp_new[8] - Fp_new[7] * Fp_new[5])
              - Fp_new[3] * (Fp_new[1] * Fp_new[8] - Fp_new[7] * Fp_new[2])
              + Fp_new[6] * (Fp_new[1] * Fp_new[5] - Fp_new[4] * Fp_new[2]);
-  double s = pow(dFp, 1.0 / 3.0);
+  double rs = 1.0 / pow(dFp, 1.0 / 3.0);
 #pragma unroll
-  for (int k = 0; k < 9; ++k) { Fp[k] = Fp_new[k] / s; Lp[k] = Lpg[k]; Fe[k] = t1[k]; }
+  for (int k = 0; k < 9; ++k) { Fp[k] = Fp_new[k] * rs; Lp[k] = Lpg[k]; Fe[k] = t1[k]; }
   return false;
 }
 

@@ -23,9 +23,13 @@ struct MatParams {
   double Q[NSLIP][9];        // C : P_alpha  (column-major 3x3)
   double h[NSLIP][NSLIP];    // slip-slip interaction, h[reacting][acting]
   double xi_inf, h0, n, gdot0, a, c1, c2;
+  double C11mC12, C12, C44x2;  // cubic stiffness: C11 - C12, C12, 2 C44
+  double ngdot0, rxi_inf;      // n * gdot0, 1 / xi_inf
+  double pval;                 // magnitude of the non-zero Schmid entries (1/sqrt2 * 1/sqrt3)
   double atol_xi, atol_gamma;
   double r_cutback_min, r_cutback, r_increase, eps_rel_state;
   double r_linesearch_Lp, eps_rel_Lp, eps_abs_Lp;
+  double eps_rel_Lp2, eps_abs_Lp2;   // squared tolerances (norm tests without square roots)
   int N_iter_state_max, N_iter_Lp_max, f_update_jacobi_Lp;
   int n_int;                 // n if it is an integer in [1, 64], else -1
   int a_quarters;            // 4a if it is an integer in [1, 256], else -1

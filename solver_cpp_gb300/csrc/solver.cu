@@ -404,6 +404,10 @@ MatParams make_params(const dgx_material& m) {
   p.N_iter_state_max = m.N_iter_state_max; p.N_iter_Lp_max = m.N_iter_Lp_max;
   p.f_update_jacobi_Lp = m.f_update_jacobi_Lp < 1 ? 1 : m.f_update_jacobi_Lp;
   p.n_int = (m.n == std::floor(m.n) && m.n >= 1 && m.n <= 64) ? (int)m.n : -1;
+  p.C11mC12 = m.C11 - m.C12; p.C12 = m.C12; p.C44x2 = 2.0 * m.C44;
+  p.ngdot0 = m.n * m.dot_gamma_0; p.rxi_inf = 1.0 / m.xi_inf;
+  p.pval = std::fabs(p.P[0][1]);                       // (1/sqrt2)(1/sqrt3), as the host computed P
+  p.eps_rel_Lp2 = m.eps_rel_Lp * m.eps_rel_Lp; p.eps_abs_Lp2 = m.eps_abs_Lp * m.eps_abs_Lp;
   double aq = 4.0 * m.a;
   p.a_quarters = (aq == std::floor(aq) && aq >= 1 && aq <= 256) ? (int)aq : -1;
   return p;
@@ -824,6 +828,13 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
   r->wgt = std::pow((double)r->N, -1.0);
   r->mat = *mat; r->num = *num;
   r->mp = make_params(*mat);
+  // the kernels fold the cF Schmid sparsity at compile time: the host table must agree
+  for (int a = 0; a < 12; ++a)
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) {
+        int sg = CF_SLIP[a][k] * CF_SLIP[a][3 + l];
+        if (r->mp.P[a][k + 3 * l] != sg * r->mp.pval) { set_err("Schmid table mismatch"); delete r; return DGX_ERR_STATE; }
+      }
   // divergence correction (MechBase::base_init, mech_base.cpp:11-43)
   {
     int idx[3] = {0, 1, 2};
