@@ -367,7 +367,8 @@ __device__ __forceinline__ double ldp(const double* p, int64_t ld, int c, int64_
 
 // Per-point constitutive response (restore, cut-back driver, FPI, P) plus the
 // block partial sums of P for P_av.  One thread per point.
-__global__ void __launch_bounds__(128)
+template <int BS>
+__global__ void __launch_bounds__(BS)
 k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int64_t ldF, double dt,
                double* __restrict__ Ppart, int* __restrict__ ill, ConsCounters* cnt) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -441,18 +442,23 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
 #pragma unroll
     for (int k = 0; k < 9; ++k) P[k] = 0.0;
   }
-  // deterministic block reduction of P (fixed tree)
-  __shared__ double red[9][128];
+  // deterministic reduction of P per group of 64 cells (fixed tree, independent of BS)
+  __shared__ double red[9][BS];
 #pragma unroll
   for (int k = 0; k < 9; ++k) red[k][threadIdx.x] = P[k];
   __syncthreads();
-  for (int s = 64; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
+  for (int s = 32; s > 0; s >>= 1) {
+    if ((threadIdx.x & 63) < s)
 #pragma unroll
       for (int k = 0; k < 9; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x < 9) Ppart[blockIdx.x * 9 + threadIdx.x] = red[threadIdx.x][0];
+  if ((threadIdx.x & 63) == 0) {
+    const int64_t g = (blockIdx.x * (int64_t)BS + threadIdx.x) >> 6;
+    if (g * 64 < ps.n)
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Ppart[g * 9 + k] = red[k][threadIdx.x];
+  }
   if (cnt) {
     // per-warp aggregation of the work counters
     unsigned lp = lp_iters, st = st_iters, jc = jac_iters;
@@ -646,48 +652,86 @@ k_tangent(MatParams mp, PointState ps, double dt, double* __restrict__ dPdF_out,
   }
 }
 
-// Final reduction of tangent partials (single block, fixed order).
+// deterministic warp sum: lane j adds x[j], x[j+32], ... then a fixed shuffle tree
+__device__ __forceinline__ double warp_sum_strided(const double* x, int n, int stride) {
+  double s = 0.0;
+  for (int b = threadIdx.x & 31; b < n; b += 32) s += x[(long)b * stride];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  return s;
+}
+
+__device__ __forceinline__ bool better_max(double n1, long long i1, double n0, long long i0) {
+  return n1 > n0 || (n1 == n0 && i1 < i0);
+}
+__device__ __forceinline__ bool better_min(double n1, long long i1, double n0, long long i0) {
+  return n1 < n0 || (n1 == n0 && i1 < i0);
+}
+
+// Final reduction of tangent partials: block 0..80 sum one component each; block 81
+// finds the argmax/argmin block (first index on ties) and writes C_minMaxAvg.
 __global__ void k_tangent_finish(const TangentPartial* __restrict__ part, int nblocks, double wgt,
                                  double* __restrict__ Cvol, double* __restrict__ Cminmax) {
+  const int stride = sizeof(TangentPartial) / sizeof(double);
+  if (blockIdx.x < 81) {
+    double s = warp_sum_strided(&part[0].sum[blockIdx.x], nblocks, stride);
+    if (threadIdx.x == 0) Cvol[blockIdx.x] = s * wgt;
+    return;
+  }
   __shared__ int bmax, bmin;
-  if (threadIdx.x == 0) {
-    int im = 0, in = 0;
-    for (int b = 1; b < nblocks; ++b) {
-      if (part[b].nmax > part[im].nmax || (part[b].nmax == part[im].nmax && part[b].imax < part[im].imax)) im = b;
-      if (part[b].nmin < part[in].nmin || (part[b].nmin == part[in].nmin && part[b].imin < part[in].imin)) in = b;
+  if (threadIdx.x < 32) {
+    double nx = -1.0, nn = 1.7976931348623157e308;
+    long long ix = (long long)1 << 62, in = (long long)1 << 62;
+    int bx = 0, bn = 0;
+    for (int b = threadIdx.x; b < nblocks; b += 32) {
+      if (better_max(part[b].nmax, part[b].imax, nx, ix)) { nx = part[b].nmax; ix = part[b].imax; bx = b; }
+      if (better_min(part[b].nmin, part[b].imin, nn, in)) { nn = part[b].nmin; in = part[b].imin; bn = b; }
     }
-    bmax = im; bmin = in;
+    for (int o = 16; o > 0; o >>= 1) {
+      double nx2 = __shfl_down_sync(0xffffffffu, nx, o); long long ix2 = __shfl_down_sync(0xffffffffu, ix, o);
+      int bx2 = __shfl_down_sync(0xffffffffu, bx, o);
+      double nn2 = __shfl_down_sync(0xffffffffu, nn, o); long long in2 = __shfl_down_sync(0xffffffffu, in, o);
+      int bn2 = __shfl_down_sync(0xffffffffu, bn, o);
+      if (better_max(nx2, ix2, nx, ix)) { nx = nx2; ix = ix2; bx = bx2; }
+      if (better_min(nn2, in2, nn, in)) { nn = nn2; in = in2; bn = bn2; }
+    }
+    if (threadIdx.x == 0) { bmax = bx; bmin = bn; }
   }
   __syncthreads();
   for (int k = threadIdx.x; k < 81; k += blockDim.x) {
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += part[b].sum[k];
-    Cvol[k] = s * wgt;
     double mx = part[bmax].nmax > 0.0 ? part[bmax].dmax[k] : 0.0;
     Cminmax[k] = 0.5 * (mx + part[bmin].dmin[k]);
   }
 }
 
-// P_av from block partials (single block, fixed order).
+// P_av from block partials: warp c sums component c (fixed order)
 __global__ void k_pav_finish(const double* __restrict__ part, int nblocks, double wgt, double* __restrict__ Pav) {
-  if (threadIdx.x < 9) {
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += part[b * 9 + threadIdx.x];
-    Pav[threadIdx.x] = s * wgt;
-  }
+  int c = threadIdx.x >> 5;
+  if (c >= 9) return;
+  const double* base = part + c;
+  double s = 0.0;
+  for (int b = threadIdx.x & 31; b < nblocks; b += 32) s += base[(long)b * 9];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) Pav[c] = s * wgt;
 }
 
 }  // namespace dgx
 
 // ------------------------------------------------------------------ host launchers
 namespace dgx {
+// block size of the constitutive launch (64, 128 or 256 threads); P_av partials are
+// per 64 cells whatever the block size: ceil(n / 64) x 9 doubles
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
-                         double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st) {
-  int nb = (int)((ps.n + 127) / 128);
-  k_constitutive<<<nb, 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+                         double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block) {
+  if (block == 64) {
+    k_constitutive<64><<<(int)((ps.n + 63) / 64), 64, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+  } else if (block == 256) {
+    k_constitutive<256><<<(int)((ps.n + 255) / 256), 256, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+  } else {
+    k_constitutive<128><<<(int)((ps.n + 127) / 128), 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+  }
 }
 void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st) {
-  k_pav_finish<<<1, 32, 0, st>>>(Ppart, nblocks, wgt, Pav);
+  k_pav_finish<<<1, 9 * 32, 0, st>>>(Ppart, nblocks, wgt, Pav);
 }
 void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,
                     TangentPartial* part, cudaStream_t st) {
@@ -696,6 +740,6 @@ void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double
 }
 void launch_tangent_finish(const TangentPartial* part, int nblocks, double wgt, double* Cvol, double* Cmm,
                            cudaStream_t st) {
-  k_tangent_finish<<<1, 96, 0, st>>>(part, nblocks, wgt, Cvol, Cmm);
+  k_tangent_finish<<<82, 32, 0, st>>>(part, nblocks, wgt, Cvol, Cmm);
 }
 }  // namespace dgx

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -28,7 +29,7 @@
 namespace dgx {
 // constitutive.cu
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
-                         double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st);
+                         double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block);
 void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st);
 void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,
                     TangentPartial* part, cudaStream_t st);
@@ -172,12 +173,14 @@ __global__ void k_multi(int mode, const double* __restrict__ a, const double* __
   }
 }
 
+// one block (warp) per component, fixed summation order
 __global__ void k_multi_finish(const double* __restrict__ part, int nb, int K, double* __restrict__ out) {
-  int k = threadIdx.x;
+  int k = blockIdx.x;
   if (k >= K) return;
   double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += part[b * K + k];
-  out[k] = s;
+  for (int b = threadIdx.x; b < nb; b += 32) s += part[b * K + k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) out[k] = s;
 }
 
 // forward_field: F = last + rate*dt - (avg - aim)   (two launches: sum, then shift)
@@ -448,6 +451,7 @@ struct dgx_rve {
   AxisHost ax[3];
   SpecLaunch sl{};
   int nb_cons = 0, nb_tan = 0, nb_red = 0;
+  int cons_block = 128;
   // host solver state (MechBase / MechSolverBasic members)
   double F_aim[9], F_aim_last_inc[9], F_aim_dot[9], P_aim[9], P_av[9];
   double C_volAvg[81], C_minMaxAvg[81], C_volAvgLastInc[81], C_minMaxAvgLastInc[81], C_ref[81], S[81];
@@ -506,7 +510,7 @@ dgx_status multi(dgx_rve* r, int mode, const double* a, const double* b, const s
   for (int k = 0; k < K; ++k) vl.v[k] = vs[k];
   int64_t n = 9 * r->N;
   k_multi<<<r->nb_red, RB, 0, r->st>>>(mode, a, b, vl, K, K2, n, r->d_redpart);
-  k_multi_finish<<<1, 64, 0, r->st>>>(r->d_redpart, r->nb_red, K + K2, r->d_redout);
+  k_multi_finish<<<K + K2, 32, 0, r->st>>>(r->d_redpart, r->nb_red, K + K2, r->d_redout);
   r->n_launch += 2;
   CK(d2h(r, out, r->d_redout, sizeof(double) * (K + K2)));
   CK(cudaStreamSynchronize(r->st));
@@ -524,7 +528,7 @@ dgx_status constitutive_response(dgx_rve* r, const double* X, double dt, bool wa
   r->n_eval++;
   CK(cudaMemsetAsync(r->d_ill, 0, sizeof(int), r->st));
   if (r->timing) cudaEventRecord(r->ev[0], r->st);
-  launch_constitutive(r->mp, r->ps, X, r->N, dt, r->d_Ppart, r->d_ill, r->d_cnt, r->st);
+  launch_constitutive(r->mp, r->ps, X, r->N, dt, r->d_Ppart, r->d_ill, r->d_cnt, r->st, r->cons_block);
   if (r->timing) cudaEventRecord(r->ev[1], r->st);
   launch_pav_finish(r->d_Ppart, r->nb_cons, r->wgt, r->d_Pav, r->st);
   r->n_launch += 2;
@@ -871,7 +875,12 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
     AL(&sp, (fp32 ? 1 : 2) * 9 * r->sl.g.Nh);
     r->spec = sp;
   }
-  r->nb_cons = (int)((N + 127) / 128);
+  r->nb_cons = (int)((N + 63) / 64);            // P_av partials: one per 64 cells
+  {
+    const char* env = std::getenv("DGX_CONS_BLOCK");
+    int b = env ? std::atoi(env) : 128;
+    r->cons_block = (b == 64 || b == 256) ? b : 128;
+  }
   r->nb_tan = (int)((N + 63) / 64);
   r->nb_red = (int)std::min<int64_t>(608, std::max<int64_t>(1, (9 * N + 1023) / 1024));
   AL(&r->d_Ppart, 9 * (int64_t)r->nb_cons);
@@ -1103,7 +1112,7 @@ extern "C" dgx_status dgx_solver_forward(dgx_rve* r, int32_t cutback, int32_t gu
   // forward_field: F = F_last_inc + F_dot dt, shifted so that its average is the aim
   k_forward_field<<<nblk(9 * N), 256, 0, r->st>>>(r->X, r->F_last_inc, r->F_dot, dt, 9 * N);
   k_plane_sums<<<r->nb_red, RB, 0, r->st>>>(r->X, N, r->d_redpart);
-  k_multi_finish<<<1, 64, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
+  k_multi_finish<<<9, 32, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
   double sums[9];
   CK(d2h(r, sums, r->d_redout, 9 * sizeof(double)));
   CK(cudaStreamSynchronize(r->st));
@@ -1172,7 +1181,7 @@ static dgx_status run_one_increment(dgx_rve* r, const dgx_loadstep* ls, int l, i
     memcpy(rec->P_av, r->P_av, sizeof(rec->P_av));
     memcpy(rec->F_aim, r->F_aim, sizeof(rec->F_aim));
     k_plane_sums<<<r->nb_red, RB, 0, r->st>>>(r->X, r->N, r->d_redpart);
-    k_multi_finish<<<1, 64, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
+    k_multi_finish<<<9, 32, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
     r->n_launch += 2;
     double sums[9];
     CK(d2h(r, sums, r->d_redout, 9 * sizeof(double)));

@@ -334,9 +334,10 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
 }
 
 __global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt, int N0, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += part[b];
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += 32) s += part[b];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) {
     double r = sqrt(s) * wgt;
     if (N0 == 1) r = r / 2.0;
     *out = r;
