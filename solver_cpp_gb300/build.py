@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdgx.so")
 SOURCES = ["constitutive.cu", "spectral.cu", "solver.cu", "peak.cu"]
 HOST_SOURCES = ["ref_stiffness.cpp"]
-HEADERS = ["dgx_internal.cuh"]
+HEADERS = ["dgx_internal.cuh", "spectral.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

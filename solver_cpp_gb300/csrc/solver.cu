@@ -25,6 +25,7 @@
 
 #include "../../include/dgx.h"
 #include "dgx_internal.cuh"
+#include "spectral.cuh"
 
 namespace dgx {
 // constitutive.cu
@@ -35,22 +36,6 @@ void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double
                     TangentPartial* part, cudaStream_t st);
 void launch_tangent_finish(const TangentPartial* part, int nblocks, double wgt, double* Cvol, double* Cmm,
                            cudaStream_t st);
-// spectral.cu
-struct AxisPlan { int n, nstages; int radix[16]; const double2* tw; const float2* twf; };
-struct AxisHost { AxisPlan plan; double2* d_tw = nullptr; float2* d_twf = nullptr; };
-struct SpecGeom { int N0, N1, N2, N0r; long long N, Nh; };
-struct SpecLaunch { SpecGeom g; int LX, TIy, TIz; size_t smx, smy, smz; int nbx, nby, nbz; };
-struct GammaArgs {
-  const double* xi_x; const double* xi_y; const double* xi_z; double resc[3];
-  const double* C_ref; const double* aim; int do_gamma, do_div; int store_fwd; double* div_part;
-};
-bool axis_create(AxisHost* ax, int n);
-void axis_destroy(AxisHost* ax);
-SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize);
-void spec_prepare(const SpecLaunch& L, bool fp32);
-void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
-                   const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st);
-void spec_div_finish(const double* part, int nb, double wgt, int N0, double* out, cudaStream_t st);
 }  // namespace dgx
 
 using namespace dgx;

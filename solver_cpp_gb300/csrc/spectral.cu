@@ -20,6 +20,7 @@
 #include <cstdint>
 
 #include "dgx_internal.cuh"
+#include "spectral.cuh"
 
 namespace dgx {
 
@@ -31,13 +32,6 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
   C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }
 
-// FFT plan for one axis length (device constant data passed by value)
-struct AxisPlan {
-  int n, nstages;
-  int radix[16];
-  const double2* tw;      // exp(-2 pi i j / n), j < n  (FP64 table)
-  const float2* twf;      // same in FP32
-};
 
 template <typename R> __device__ __forceinline__ typename cpx<R>::t twid(const AxisPlan& p, long j, int sign) {
   typename cpx<R>::t w;
@@ -105,10 +99,6 @@ __device__ typename cpx<R>::t* block_fft(typename cpx<R>::t* a, typename cpx<R>:
   return a;
 }
 
-struct SpecGeom {
-  int N0, N1, N2, N0r;
-  long long N, Nh;        // real points, half-spectrum points (per component)
-};
 
 // ---------------------------------------------------------------- x pass
 // forward: real planes (ld_in) -> spectrum planes (stride Nh); one block = LX lines
@@ -200,17 +190,6 @@ __global__ void k_ypass(SpecGeom g, AxisPlan py, typename cpx<R>::t* __restrict_
 }
 
 // ---------------------------------------------------------------- z pass + Gamma + div
-struct GammaArgs {
-  const double* xi_x;     // N0r  (imaginary part of xi1st along x; continuous/central)
-  const double* xi_y;     // N1
-  const double* xi_z;     // N2
-  double resc[3];         // geom / scaled_geom
-  const double* C_ref;    // 81, device
-  const double* aim;      // 9, device (zero-frequency value), may be null when !gamma
-  int do_gamma, do_div;
-  int store_fwd;          // without gamma: write the forward z transform back
-  double* div_part;       // per block partial of the divergence sum (FP64)
-};
 
 template <typename R>
 __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict__ spec, int TI, GammaArgs ga) {
@@ -353,7 +332,7 @@ __global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt
 
 namespace dgx {
 
-static void twiddle(long j, long n, double* c, double* s) {
+void twiddle(long j, long n, double* c, double* s) {
   // cos/sin of 2 pi j / n, argument reduced to the first octant (quarter turns exact)
   const double TAU = 6.283185307179586476925286766559;
   j %= n; if (j < 0) j += n;
@@ -370,13 +349,8 @@ static void twiddle(long j, long n, double* c, double* s) {
   }
 }
 
-struct AxisHost {
-  AxisPlan plan;
-  double2* d_tw = nullptr;
-  float2* d_twf = nullptr;
-};
 
-static int factorize(int n, int* rad) {
+int factorize(int n, int* rad) {
   int ns = 0, m = n;
   while (m % 4 == 0) { rad[ns++] = 4; m /= 4; }
   while (m % 2 == 0) { rad[ns++] = 2; m /= 2; }
@@ -414,13 +388,6 @@ void axis_destroy(AxisHost* ax) {
   ax->d_tw = nullptr; ax->d_twf = nullptr;
 }
 
-// launch configuration shared by the spectral kernels
-struct SpecLaunch {
-  SpecGeom g;
-  int LX, TIy, TIz;
-  size_t smx, smy, smz;
-  int nbx, nby, nbz;
-};
 
 SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize) {
   SpecLaunch L;

@@ -1,0 +1,60 @@
+// spectral.cuh -- host interface of the spectral kernels (spectral.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace dgx {
+
+// FFT plan for one axis length (device constant data passed by value)
+struct AxisPlan {
+  int n, nstages;
+  int radix[16];
+  const double2* tw;      // exp(-2 pi i j / n), j < n  (FP64 table)
+  const float2* twf;      // same in FP32
+};
+
+struct AxisHost {
+  AxisPlan plan;
+  double2* d_tw = nullptr;
+  float2* d_twf = nullptr;
+};
+
+struct SpecGeom {
+  int N0, N1, N2, N0r;
+  long long N, Nh;        // real points, half-spectrum points (per component)
+};
+
+// launch configuration shared by the spectral kernels
+struct SpecLaunch {
+  SpecGeom g;
+  int LX, TIy, TIz;
+  size_t smx, smy, smz;
+  int nbx, nby, nbz;
+};
+
+struct GammaArgs {
+  const double* xi_x;     // N0r  (imaginary part of xi1st along x; continuous/central)
+  const double* xi_y;     // N1
+  const double* xi_z;     // N2
+  double resc[3];         // geom / scaled_geom
+  const double* C_ref;    // 81, device
+  const double* aim;      // 9, device (zero-frequency value), may be null when !gamma
+  int do_gamma, do_div;
+  int store_fwd;          // without gamma: write the forward z transform back
+  double* div_part;       // per block partial of the divergence sum (FP64)
+};
+
+// cos/sin of 2 pi j / n with the argument reduced to the first octant
+void twiddle(long j, long n, double* c, double* s);
+// radix factorisation (4, 2, then odd primes <= 16); number of stages or -1
+int factorize(int n, int* rad);
+bool axis_create(AxisHost* ax, int n);
+void axis_destroy(AxisHost* ax);
+SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize);
+void spec_prepare(const SpecLaunch& L, bool fp32);
+void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                   const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st);
+void spec_div_finish(const double* part, int nb, double wgt, int N0, double* out, cudaStream_t st);
+
+}  // namespace dgx
