@@ -119,6 +119,20 @@ dgx_status dgx_update_gamma(dgx_rve* rve, const double C[81]);
  * (3,3,N0/2+1,N2,N1) as interleaved (re,im) (FFT<5>::forward, src/grid/fft.h:37-47). */
 dgx_status dgx_fft_forward(dgx_rve* rve, const double* field, double* spectrum);
 
+/* Divergence RMS of a device-resident stress field (3,3,N) without any device
+ * allocation.  No counterpart in the reference: it is for callers that cannot call
+ * cudaMalloc (all device memory owned by their own pool or budget, or no
+ * allocation allowed inside their time-critical loop); they pass input and output
+ * buffers they already own.  Scratch is one file-scope device array of 10 MiB,
+ * held by every GPU that loads the library until exit; at most 32768 cells
+ * (larger grids return DGX_ERR_ARG).  All calls share that array and leave their
+ * contents in it, so calls that overlap on the GPU race and must be serialised.
+ * The first call on a device looks up the array's address (make it before any
+ * stream capture).  P_device: device (3,3,N) reference layout; rms_device: one
+ * device double; stream: cudaStream_t (0 = default stream); asynchronous. */
+dgx_status dgx_divergence_rms_static(const int32_t cells[3], const double size[3], int32_t divergence_correction,
+                                     int32_t derivative, const double* P_device, double* rms_device, void* stream);
+
 /* Solver (MechSolverBasic + DamaskGrid, src/grid/mech_solver_basic.cpp, damask_grid.cpp) */
 dgx_status dgx_solver_init(dgx_rve* rve);                                   /* MechSolverBasic::init :19-108 */
 dgx_status dgx_solver_forward(dgx_rve* rve, int32_t cutback, int32_t guess, double dt, double dt_old,

@@ -52,7 +52,7 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_commit_increment", "dgx_divergence_rms", "dgx_gamma_convolution", "dgx_update_gamma",
            "dgx_fft_forward", "dgx_solver_init", "dgx_solver_forward", "dgx_solver_solve", "dgx_run_loadcase",
            "dgx_run_increment", "dgx_get", "dgx_counters", "dgx_timers", "dgx_rve_stream",
-           "dgx_measure_fp64_peak"]
+           "dgx_measure_fp64_peak", "dgx_divergence_rms_static"]
 
 
 class DgxError(RuntimeError):
@@ -99,6 +99,7 @@ def lib():
     L.dgx_rve_stream.argtypes = [vp]
     L.dgx_rve_stream.restype = vp
     L.dgx_measure_fp64_peak.argtypes = [dp, dp]
+    L.dgx_divergence_rms_static.argtypes = [ip, dp, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
     for name in SYMBOLS:
         f = getattr(L, name)
         if name not in ("dgx_material_default", "dgx_numerics_default", "dgx_rve_destroy", "dgx_last_error",
