@@ -165,6 +165,41 @@ dgx_status dgx_counters(const dgx_rve* rve, int64_t out[8]);
 dgx_status dgx_timers(const dgx_rve* rve, double ms[3], int64_t launches[3]);
 /* The CUDA stream (cudaStream_t) all work of the RVE is queued on. */
 void* dgx_rve_stream(const dgx_rve* rve);
+/* ---- Batched execution (no counterpart in the reference, which solves one RVE per
+ * process).  A batch advances many RVEs of uneven size together on one stream: each
+ * round serves the pending residual evaluations of all members with one persistent
+ * constitutive launch over all their points and one launch per FFT pass for every
+ * group of equal grids, and the pending fused reductions with one launch.  A member
+ * computes exactly what dgx_run_loadcase computes for it alone (same kernels, same
+ * reduction order), whatever else is in the batch.  Members may be added between
+ * rounds (continuous batching); an RVE in a batch may not be driven by the
+ * single-RVE calls until it is removed. */
+typedef struct dgx_batch dgx_batch;
+/* capacity: most members at once; cons_block: points per constitutive block (64,
+ * 128 or 256; other values mean 128) */
+dgx_status dgx_batch_create(int32_t capacity, int32_t cons_block, dgx_batch** out);
+void dgx_batch_destroy(dgx_batch* batch);
+/* Add an RVE that runs the load case steps[0..nsteps) from solver init (as
+ * dgx_run_loadcase); records[k] is filled per increment (up to max_records).  steps
+ * and records must stay valid until the member is done.  *slot identifies it. */
+dgx_status dgx_batch_add(dgx_batch* batch, dgx_rve* rve, int32_t nsteps, const dgx_loadstep* steps,
+                         dgx_inc_record* records, int32_t max_records, int32_t* slot);
+/* One round; *n_active = members not yet done. */
+dgx_status dgx_batch_step(dgx_batch* batch, int32_t* n_active);
+/* Rounds until every member is done. */
+dgx_status dgx_batch_run(dgx_batch* batch);
+/* done: 1 when the member finished (status: its dgx_status), n_records written. */
+dgx_status dgx_batch_member(const dgx_batch* batch, int32_t slot, int32_t* done, int32_t* n_records,
+                            int32_t* status);
+/* Detach a finished member: the RVE returns to its own stream and the single-RVE calls. */
+dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
+/* ms: CUDA-event time of [0] constitutive launches, [1] spectral chains, [2] unused;
+ * out: [0] point evaluations, [1] state iterations, [2] Lp iterations, [3] rounds,
+ * [4] launches of the batched kernels, [5] Jacobian factorisations, [6] h2d bytes,
+ * [7] d2h bytes of the executor. */
+dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[8]);
+void* dgx_batch_stream(const dgx_batch* batch);
+
 /* FP64 FMA throughput of the current device (TFLOP/s, best of 5), the
  * denominator of the constitutive kernel's roofline.  No reference counterpart. */
 dgx_status dgx_measure_fp64_peak(double* tflops, double* ms);

@@ -16,7 +16,7 @@ from . import dgx as _d
 from .dgx import DgxError  # noqa: F401
 from .loadcase import load_step, parse_load_yaml, parse_numerics_yaml  # noqa: F401
 
-__all__ = ["RVE", "material", "numerics", "load_step", "DgxError"]
+__all__ = ["RVE", "Batch", "material", "numerics", "load_step", "DgxError"]
 
 
 def material(**kw):
@@ -202,3 +202,75 @@ def _record(r):
     return dict(t=r.t, dt=r.dt, P_av=_unf9(np.array(r.P_av[:]), 1)[0], F_aim=_unf9(np.array(r.F_aim[:]), 1)[0],
                 F_av=_unf9(np.array(r.F_av[:]), 1)[0], iterations=r.iterations, evaluations=r.evaluations,
                 cutbacks=r.cutbacks, err_div=r.err_div, err_BC=r.err_BC, seconds=r.seconds)
+
+
+class Batch:
+    """Many RVEs advanced together on one stream (dgx_batch_*).
+
+    ``add(rve, steps)`` makes the RVE run the load case from solver init, like
+    ``RVE.loop_over_loadcase``; ``step()`` runs one round (every member's pending
+    residual evaluation or reduction in batched launches); ``run()`` rounds until
+    all members are done.  Members can be added between rounds.
+    """
+
+    def __init__(self, capacity, cons_block=128):
+        h = C.c_void_p()
+        _d.check(_d.lib().dgx_batch_create(int(capacity), int(cons_block), C.byref(h)), "dgx_batch_create")
+        self.h = h
+        self._keep = {}          # slot -> (rve, steps array, records array)
+
+    def close(self):
+        if getattr(self, "h", None):
+            _d.lib().dgx_batch_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, rve, steps, max_records=None):
+        arr = (_d.LoadStep * len(steps))(*steps)
+        nrec = sum(int(s.N) for s in steps)
+        recs = (_d.IncRecord * max(1, nrec if max_records is None else min(nrec, max_records)))()
+        slot = C.c_int32(0)
+        _d.check(_d.lib().dgx_batch_add(self.h, rve.h, len(steps), arr, recs, len(recs), C.byref(slot)),
+                 "dgx_batch_add")
+        self._keep[slot.value] = (rve, arr, recs)
+        return slot.value
+
+    def step(self):
+        n = C.c_int32(0)
+        _d.check(_d.lib().dgx_batch_step(self.h, C.byref(n)), "dgx_batch_step")
+        return n.value
+
+    def run(self):
+        _d.check(_d.lib().dgx_batch_run(self.h), "dgx_batch_run")
+
+    def member(self, slot):
+        done = C.c_int32(0); n = C.c_int32(0); st = C.c_int32(0)
+        _d.check(_d.lib().dgx_batch_member(self.h, int(slot), C.byref(done), C.byref(n), C.byref(st)),
+                 "dgx_batch_member")
+        return dict(done=bool(done.value), n_records=n.value, status=st.value)
+
+    def records(self, slot):
+        m = self.member(slot)
+        recs = self._keep[slot][2]
+        return [_record(r) for r in recs[:m["n_records"]]]
+
+    def remove(self, slot):
+        _d.check(_d.lib().dgx_batch_remove(self.h, int(slot)), "dgx_batch_remove")
+        self._keep.pop(slot, None)
+
+    def stats(self):
+        ms = (C.c_double * 3)(); a = (C.c_int64 * 8)()
+        _d.check(_d.lib().dgx_batch_stats(self.h, ms, a), "dgx_batch_stats")
+        return dict(constitutive_ms=ms[0], spectral_ms=ms[1], point_evaluations=a[0], state_iterations=a[1],
+                    lp_iterations=a[2], rounds=a[3], launches=a[4], jacobians=a[5], h2d_bytes=a[6],
+                    d2h_bytes=a[7])
+
+    @property
+    def stream(self):
+        return int(_d.lib().dgx_batch_stream(self.h) or 0)

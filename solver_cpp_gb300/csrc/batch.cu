@@ -1,0 +1,762 @@
+// batch.cu -- batched execution of the spectral solver: many RVEs of uneven size
+// advanced together on one stream.
+//
+// The solve of one RVE (MechSolverBasic::calculate_solution with PETSc NGMRES,
+// mech_solver_basic.cpp:110-339, inside DamaskGrid::loop_over_loadcase,
+// damask_grid.cpp:82-196) is written here as a resumable state machine (Task).  A
+// task runs its host logic until it needs the device -- a residual evaluation or a
+// fused reduction -- and parks the request.  The executor then serves the requests
+// of every task in one batched launch sequence:
+//   residual   one persistent constitutive launch over the points of all RVEs
+//              (offset-indexed tiles), one P_av reduction launch, host BC step,
+//              then per group of equal grids one launch per FFT pass with one
+//              blockIdx.y per RVE (FFT, divergence RMS, Gamma), one RMS launch
+//   reduction  one fused multi-dot launch for all RVEs plus one finishing launch
+// and hands the results back.  Per-RVE arithmetic is identical to a batch of one
+// (the same tiles, reduction partitions and summation orders), so an RVE's result
+// does not depend on which other RVEs share the batch.  A single-RVE solve is a
+// batch of one.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "rve.cuh"
+
+namespace dgx {
+
+// ------------------------------------------------------------------ fused reductions
+struct MultiItem {
+  const double* a;          // anchor vector
+  const double* b;          // second anchor (first K2 sums), may be null
+  const double* v[32];
+  int mode, K, K2, nb;      // mode 0: sum a*v_k ; mode 1: sum (v_k - a)^2 ; nb blocks
+  long long n;
+  double* part;             // nb x (K + K2)
+  double* out;              // K + K2 results
+};
+
+// the reduction of k_multi (solver.cu) per item; blockIdx.y = item, same partition
+__global__ void __launch_bounds__(RB) k_multi_batch(const MultiItem* __restrict__ items) {
+  __shared__ MultiItem s;
+  {
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(items + blockIdx.y);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&s);
+    for (int w = threadIdx.x; w < (int)(sizeof(MultiItem) / 8); w += blockDim.x) dst[w] = src[w];
+  }
+  __syncthreads();
+  if ((int)blockIdx.x >= s.nb) return;
+  const int K = s.K, K2 = s.K2;
+  double acc[32], acc2[32];
+  for (int k = 0; k < K; ++k) { acc[k] = 0.0; acc2[k] = 0.0; }
+  const int64_t stride = (int64_t)s.nb * blockDim.x;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < s.n; t += stride) {
+    double av = s.a[t];
+    double bv = s.b ? s.b[t] : 0.0;
+    for (int k = 0; k < K; ++k) {
+      double x = s.v[k][t];
+      if (s.mode == 0) acc[k] = fma(av, x, acc[k]);
+      else { double d = x - av; acc[k] = fma(d, d, acc[k]); }
+      if (k < K2) acc2[k] = fma(bv, x, acc2[k]);
+    }
+  }
+  __shared__ double red[RB];
+  const int KT = K + K2;
+  for (int k = 0; k < KT; ++k) {
+    red[threadIdx.x] = k < K ? acc[k] : acc2[k - K];
+    __syncthreads();
+    for (int q = RB / 2; q > 0; q >>= 1) {
+      if (threadIdx.x < q) red[threadIdx.x] += red[threadIdx.x + q];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) s.part[blockIdx.x * KT + k] = red[0];
+    __syncthreads();
+  }
+}
+
+// one warp per (sum, item), fixed summation order (as k_multi_finish)
+__global__ void k_multi_finish_batch(const MultiItem* __restrict__ items) {
+  const MultiItem& it = items[blockIdx.y];
+  const int KT = it.K + it.K2;
+  const int k = blockIdx.x;
+  if (k >= KT) return;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < it.nb; b += 32) s += it.part[b * KT + k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) it.out[k] = s;
+}
+
+// ------------------------------------------------------------------ executor
+struct ResReq { dgx_rve* r; const double* in; double* out; };
+struct MultiReq {
+  dgx_rve* r;
+  int mode, K, K2, slot;     // slot: which of the RVE's two partial buffers
+  const double* a;
+  const double* b;
+  const double* v[32];
+  double* out;               // host, K + K2 values
+};
+
+struct Executor {
+  cudaStream_t st = nullptr;
+  int cap = 0;                               // residual items per round; 2 cap reductions
+  ConsItem* d_cons = nullptr; SpecItem* d_spec = nullptr; MultiItem* d_multi = nullptr;
+  int* d_ill = nullptr; double* d_Pav = nullptr; double* d_aim = nullptr; double* d_rms = nullptr;
+  double* d_mout = nullptr; unsigned long long* d_queue = nullptr;
+  ConsItem* h_cons = nullptr; SpecItem* h_spec = nullptr; MultiItem* h_multi = nullptr;
+  int* h_ill = nullptr; double* h_Pav = nullptr; double* h_aim = nullptr; double* h_rms = nullptr;
+  double* h_mout = nullptr;
+  ConsCounters* cnt = nullptr;
+  bool own_cnt = false;
+  int cons_block = 128, resident = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_ms[3] = {0, 0, 0};
+  int64_t t_n[3] = {0, 0, 0};
+  int64_t launches = 0, bytes_h2d = 0, bytes_d2h = 0, point_evals = 0, rounds = 0;
+  std::vector<void*> dev, host;
+};
+
+void executor_destroy(Executor* e) {
+  if (!e) return;
+  for (void* p : e->dev) cudaFree(p);
+  for (void* p : e->host) cudaFreeHost(p);
+  for (auto& v : e->ev) if (v) cudaEventDestroy(v);
+  delete e;
+}
+
+template <typename T>
+static dgx_status ex_alloc(Executor* e, T** d, T** h, size_t n) {
+  void* p = nullptr;
+  if (d) {
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) { set_err("executor: cudaMalloc failed"); return DGX_ERR_NOMEM; }
+    e->dev.push_back(p); *d = (T*)p;
+  }
+  if (h) {
+    if (cudaMallocHost(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) { set_err("executor: cudaMallocHost failed"); return DGX_ERR_NOMEM; }
+    e->host.push_back(p); *h = (T*)p;
+  }
+  return DGX_OK;
+}
+
+dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons_block, Executor** out) {
+  Executor* e = new Executor();
+  e->st = st; e->cap = cap;
+  e->cons_block = (cons_block == 64 || cons_block == 256) ? cons_block : 128;
+  dgx_status s = DGX_OK;
+#define EA(d, h, n) do { s = ex_alloc(e, d, h, n); if (s != DGX_OK) { executor_destroy(e); return s; } } while (0)
+  EA(&e->d_cons, &e->h_cons, cap);
+  EA(&e->d_spec, &e->h_spec, cap);
+  EA(&e->d_multi, &e->h_multi, 2 * cap);
+  EA(&e->d_ill, &e->h_ill, cap);
+  EA(&e->d_Pav, &e->h_Pav, 9 * cap);
+  EA(&e->d_aim, &e->h_aim, 9 * cap);
+  EA(&e->d_rms, &e->h_rms, cap);
+  EA(&e->d_mout, &e->h_mout, 64 * 2 * cap);
+  EA(&e->d_queue, (unsigned long long**)nullptr, 16);
+  if (cnt) e->cnt = cnt;
+  else { EA(&e->cnt, (ConsCounters**)nullptr, 1); e->own_cnt = true; cudaMemset(e->cnt, 0, sizeof(ConsCounters)); }
+#undef EA
+  for (auto& v : e->ev) cudaEventCreate(&v);
+  e->resident = constitutive_batch_resident(e->cons_block);
+  *out = e;
+  return DGX_OK;
+}
+
+void executor_stats(const Executor* e, double ms[3], int64_t n[3], int64_t* launches, int64_t* h2d_b, int64_t* d2h_b) {
+  for (int i = 0; i < 3; ++i) { ms[i] += e->t_ms[i]; n[i] += e->t_n[i]; }
+  *launches += e->launches; *h2d_b += e->bytes_h2d; *d2h_b += e->bytes_d2h;
+}
+
+static dgx_status ex_h2d(Executor* e, void* d, const void* h, size_t b) {
+  e->bytes_h2d += (int64_t)b;
+  CK(cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, e->st));
+  return DGX_OK;
+}
+static dgx_status ex_d2h(Executor* e, void* h, const void* d, size_t b) {
+  e->bytes_d2h += (int64_t)b;
+  CK(cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, e->st));
+  return DGX_OK;
+}
+
+// equal grids (and spectral precision, derivative, geometry) share a launch
+typedef std::tuple<int, int, int, double, double, double, int, int, int> GridKey;
+static GridKey grid_key(const dgx_rve* r) {
+  return GridKey(r->cells[0], r->cells[1], r->cells[2], r->geom[0], r->geom[1], r->geom[2], r->num.precision,
+                 r->num.derivative, r->num.divergence_correction);
+}
+
+// residual evaluations R = Gamma * P(X) of every request (form_residual)
+static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
+  const int n = (int)q.size();
+  if (n == 0) return DGX_OK;
+  if (n > e->cap) { set_err("executor: %d residual requests exceed capacity %d", n, e->cap); return DGX_ERR_STATE; }
+  // constitutive pass: items grouped by material, largest RVEs first in the tile queue
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    int c = memcmp(&q[a].r->mp, &q[b].r->mp, sizeof(MatParams));
+    if (c != 0) return c < 0;
+    return q[a].r->N > q[b].r->N;
+  });
+  const int BS = e->cons_block;
+  std::vector<int> slot_of(n);
+  for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
+  CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, e->st));
+  CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * 16, e->st));
+  std::vector<std::pair<int, long long>> groups;    // (first slot, tiles)
+  {
+    long long tiles = 0;
+    int gstart = 0;
+    for (int j = 0; j < n; ++j) {
+      dgx_rve* r = q[order[j]].r;
+      if (j > 0 && memcmp(&r->mp, &q[order[j - 1]].r->mp, sizeof(MatParams)) != 0) {
+        groups.push_back({gstart, tiles}); gstart = j; tiles = 0;
+      }
+      ConsItem& it = e->h_cons[j];
+      it.ps = r->ps; it.F = q[order[j]].in; it.ldF = r->N; it.dt = r->delta_t; it.wgt = r->wgt;
+      it.Ppart = r->d_Ppart; it.ill = e->d_ill + j; it.tile0 = tiles;
+      tiles += (r->N + BS - 1) / BS;
+      r->n_eval++;
+      r->tangent_dt = r->delta_t;
+      e->point_evals += r->N;
+    }
+    groups.push_back({gstart, tiles});
+    if (groups.size() > 16) { set_err("executor: more than 16 materials in one round"); return DGX_ERR_UNSUPPORTED; }
+  }
+  TRY(ex_h2d(e, e->d_cons, e->h_cons, sizeof(ConsItem) * n));
+  CK(cudaEventRecord(e->ev[0], e->st));
+  for (size_t g = 0; g < groups.size(); ++g) {
+    int j0 = groups[g].first;
+    int j1 = g + 1 < groups.size() ? groups[g + 1].first : n;
+    long long tiles = groups[g].second;
+    int grid = (int)std::min<long long>(tiles, e->resident);
+    launch_constitutive_batch(q[order[j0]].r->mp, e->d_cons + j0, j1 - j0, tiles, e->d_queue + g, e->cnt, e->st, BS,
+                              std::max(grid, 1));
+    e->launches++;
+  }
+  CK(cudaEventRecord(e->ev[1], e->st));
+  launch_pav_finish_batch(e->d_cons, n, e->d_Pav, e->st);
+  e->launches++;
+  TRY(ex_d2h(e, e->h_Pav, e->d_Pav, sizeof(double) * 9 * n));
+  TRY(ex_d2h(e, e->h_ill, e->d_ill, sizeof(int) * n));
+  CK(cudaStreamSynchronize(e->st));
+  CK(cudaGetLastError());
+  {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[0] += ms; e->t_n[0]++;
+  }
+  // host BC step of every RVE
+  for (int i = 0; i < n; ++i) {
+    dgx_rve* r = q[i].r;
+    const int j = slot_of[i];
+    memcpy(r->P_av, e->h_Pav + 9 * j, 9 * sizeof(double));
+    TRY(post_constitutive(r, e->h_ill[j], !r->num.lazy_tangent));
+    residual_bc(r, e->h_aim + 9 * i);
+  }
+  // spectral pass: one launch chain per grid group
+  std::map<GridKey, std::vector<int>> gg;
+  for (int i = 0; i < n; ++i) gg[grid_key(q[i].r)].push_back(i);
+  int off = 0;
+  std::vector<std::pair<int, int>> spans;
+  for (auto& kv : gg) {
+    spans.push_back({off, (int)kv.second.size()});
+    for (int i : kv.second) {
+      dgx_rve* r = q[i].r;
+      SpecItem& it = e->h_spec[off++];
+      it.in = r->ps.P; it.out = q[i].out; it.spec = r->spec; it.C_ref = r->d_Cref; it.aim = e->d_aim + 9 * i;
+      it.div_part = r->d_divpart; it.rms = e->d_rms + i;
+    }
+  }
+  TRY(ex_h2d(e, e->d_aim, e->h_aim, sizeof(double) * 9 * n));
+  TRY(ex_h2d(e, e->d_spec, e->h_spec, sizeof(SpecItem) * n));
+  CK(cudaEventRecord(e->ev[2], e->st));
+  {
+    size_t gi = 0;
+    for (auto& kv : gg) {
+      dgx_rve* r0 = q[kv.second[0]].r;
+      GammaArgs ga = gamma_args(r0, true, true);
+      const int o = spans[gi].first, cnt = spans[gi].second;
+      spec_convolve_batch(r0->sl, r0->num.precision == 1, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan, e->d_spec + o,
+                          cnt, ga, e->st);
+      spec_div_finish_batch(e->d_spec + o, cnt, r0->sl.nbz, r0->wgt, r0->cells[0], e->st);
+      e->launches += 6;
+      ++gi;
+    }
+  }
+  CK(cudaEventRecord(e->ev[3], e->st));
+  TRY(ex_d2h(e, e->h_rms, e->d_rms, sizeof(double) * n));
+  CK(cudaStreamSynchronize(e->st));
+  CK(cudaGetLastError());
+  {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[1] += ms; e->t_n[1]++;
+  }
+  for (int i = 0; i < n; ++i) q[i].r->err_div = e->h_rms[i];
+  return DGX_OK;
+}
+
+// fused reductions of every request
+static dgx_status ex_multi(Executor* e, std::vector<MultiReq>& q) {
+  const int n = (int)q.size();
+  if (n == 0) return DGX_OK;
+  if (n > 2 * e->cap) { set_err("executor: %d reductions exceed capacity", n); return DGX_ERR_STATE; }
+  int maxnb = 1;
+  for (int i = 0; i < n; ++i) {
+    dgx_rve* r = q[i].r;
+    MultiItem& it = e->h_multi[i];
+    it.a = q[i].a; it.b = q[i].b;
+    for (int k = 0; k < 32; ++k) it.v[k] = k < q[i].K ? q[i].v[k] : nullptr;
+    it.mode = q[i].mode; it.K = q[i].K; it.K2 = q[i].K2; it.nb = r->nb_red; it.n = 9 * r->N;
+    it.part = r->d_redpart + (int64_t)64 * r->nb_red * q[i].slot;
+    it.out = e->d_mout + 64 * i;
+    maxnb = std::max(maxnb, r->nb_red);
+  }
+  TRY(ex_h2d(e, e->d_multi, e->h_multi, sizeof(MultiItem) * n));
+  k_multi_batch<<<dim3(maxnb, n), RB, 0, e->st>>>(e->d_multi);
+  k_multi_finish_batch<<<dim3(64, n), 32, 0, e->st>>>(e->d_multi);
+  e->launches += 2;
+  TRY(ex_d2h(e, e->h_mout, e->d_mout, sizeof(double) * 64 * n));
+  CK(cudaStreamSynchronize(e->st));
+  CK(cudaGetLastError());
+  for (int i = 0; i < n; ++i) memcpy(q[i].out, e->h_mout + 64 * i, sizeof(double) * (q[i].K + q[i].K2));
+  return DGX_OK;
+}
+
+// ------------------------------------------------------------------ solver state machine
+enum TState {
+  T_LC_BEGIN, T_INC_BEGIN, T_SUB_CHECK, T_SOLVE_BEGIN, T_N_INIT1, T_N_INIT2, T_FP_ITER, T_FP_NORM, T_FP_CHECK,
+  T_N_ITER, T_N_M1, T_N_LSQ, T_N_A1, T_N_DECIDE, T_SOLVE_END, T_SUB_AFTER, T_INC_END, T_DONE
+};
+
+struct Task {
+  dgx_rve* r = nullptr;
+  int mode = 0;                       // 0 one solve, 1 one increment, 2 load case
+  const dgx_loadstep* steps = nullptr;
+  int nsteps = 0, l = 0, inc = 0;
+  dgx_inc_record* records = nullptr;
+  int max_records = 0, nrec = 0;
+  int32_t conv = 0, sit = 0, sill = 0;
+  TState pc = T_LC_BEGIN;
+  dgx_status err = DGX_OK;
+  // pending device request: 0 none, 1 residual, 2 reductions
+  int want = 0;
+  const double* rin = nullptr;
+  double* rout = nullptr;
+  int nmq = 0;
+  MultiReq mq[2];
+  // increment locals (run_one_increment)
+  int step_fraction = 0, iters = 0, cutbacks = 0;
+  int64_t ev0 = 0;
+  std::chrono::steady_clock::time_point t0;
+  // SNESSolve locals
+  int reason = 0, k = 0, k_restart = 1, lh = 1, ivec = 0, restart_count = 0;
+  double *X = nullptr, *F = nullptr;
+  double fnorm = 0.0, fminnorm = 0.0, fMnorm = 0.0;
+  std::vector<double> qm, beta, xi, tmp, tmpA;
+  bool done() const { return pc == T_DONE; }
+  const dgx_loadstep* cur_step() const { return mode == 2 ? &steps[l] : steps; }
+};
+
+static void req_residual(Task& t, const double* in, double* out) { t.want = 1; t.rin = in; t.rout = out; }
+static void req_multi(Task& t, int mode, const double* a, const double* b, const std::vector<const double*>& vs, int K2,
+                      double* out) {
+  MultiReq& m = t.mq[t.nmq];
+  m.r = t.r; m.mode = mode; m.a = a; m.b = b; m.K = (int)vs.size(); m.K2 = K2; m.slot = t.nmq; m.out = out;
+  for (int k = 0; k < m.K; ++k) m.v[k] = vs[k];
+  t.nmq++;
+  t.want = 2;
+}
+static dgx_status d2d9(dgx_rve* r, double* dst, const double* src) {
+  CK(cudaMemcpyAsync(dst, src, sizeof(double) * 9 * r->N, cudaMemcpyDeviceToDevice, r->st));
+  return DGX_OK;
+}
+
+// run the task's host logic until it parks a device request or finishes
+static dgx_status advance(Task& t) {
+  dgx_rve* r = t.r;
+  const int64_t n9 = 9 * r->N;
+  for (;;) {
+    switch (t.pc) {
+      case T_LC_BEGIN:
+        t.l = 0; t.inc = 0; t.nrec = 0;
+        t.pc = t.nsteps > 0 ? T_INC_BEGIN : T_DONE;
+        break;
+      case T_INC_BEGIN: {
+        const dgx_loadstep* ls = t.cur_step();
+        if (t.l != r->cur_step) { r->cur_step = t.l; r->t_0 = r->t; r->guess = ls->estimate_rate && t.l > 0; }
+        t.t0 = std::chrono::steady_clock::now();
+        r->dt_prev = r->dt;
+        r->dt = forward_time(ls, t.inc, 2, r->cut_back_level);
+        t.step_fraction = 0; t.iters = 0; t.cutbacks = 0; t.ev0 = r->n_eval;
+        t.pc = T_SUB_CHECK;
+        break;
+      }
+      case T_SUB_CHECK: {
+        const dgx_loadstep* ls = t.cur_step();
+        if (t.step_fraction < (int)std::pow(2, r->cut_back_level)) {
+          double t_remaining = ls->t + r->t_0 - r->t;
+          r->t += r->dt;
+          t.step_fraction++;
+          TRY(dgx_solver_forward(r, r->cut_back, r->guess, r->dt, r->dt_prev, t_remaining, ls));
+          if (!r->cut_back) TRY(commit(r));
+          t.pc = T_SOLVE_BEGIN;
+        } else {
+          t.pc = T_INC_END;
+        }
+        break;
+      }
+      case T_SOLVE_BEGIN:
+        TRY(solve_prologue(r));
+        t.X = r->X; t.F = r->R;
+        r->total_iter = 0;
+        t.tmp.assign(2 * 32 + 2, 0.0);
+        t.tmpA.assign(2, 0.0);
+        req_residual(t, t.X, t.F);
+        t.pc = T_N_INIT1;
+        return DGX_OK;
+      case T_N_INIT1:
+        req_multi(t, 0, t.F, nullptr, {t.F}, 0, t.tmp.data());
+        t.pc = T_N_INIT2;
+        return DGX_OK;
+      case T_N_INIT2: {
+        t.fnorm = std::sqrt(t.tmp[0]);
+        if (!std::isfinite(t.fnorm)) { t.reason = -2; t.pc = T_SOLVE_END; break; }
+        t.fminnorm = t.fnorm;
+        t.reason = converged(r);
+        if (t.reason) { t.pc = T_SOLVE_END; break; }
+        t.k = 1;
+        if (r->num.solver == 1) { t.pc = T_FP_ITER; break; }
+        const int m = r->num.ngmres_m;
+        t.qm.assign((size_t)m * m, 0.0); t.beta.assign(m, 0.0); t.xi.assign(m, 0.0);
+        TRY(d2d9(r, r->Fdot[0], t.F)); TRY(d2d9(r, r->Xdot[0], t.X));
+        t.k_restart = 1; t.lh = 1; t.ivec = 0; t.restart_count = 0;
+        t.pc = T_N_ITER;
+        break;
+      }
+      // ---- fixed point: X <- X - F
+      case T_FP_ITER:
+        if (t.k > r->num.snes_max_it) { t.reason = -1; t.pc = T_SOLVE_END; break; }
+        launch_axpy(t.X, t.X, -1.0, t.F, n9, r->st);
+        r->n_launch++;
+        r->total_iter = t.k;
+        req_residual(t, t.X, t.F);
+        t.pc = T_FP_NORM;
+        return DGX_OK;
+      case T_FP_NORM:
+        req_multi(t, 0, t.F, nullptr, {t.F}, 0, t.tmp.data());
+        t.pc = T_FP_CHECK;
+        return DGX_OK;
+      case T_FP_CHECK: {
+        double fn = std::sqrt(t.tmp[0]);
+        if (!std::isfinite(fn)) { t.reason = -2; t.pc = T_SOLVE_END; break; }
+        t.reason = converged(r);
+        if (t.reason) { t.pc = T_SOLVE_END; break; }
+        t.k++;
+        t.pc = T_FP_ITER;
+        break;
+      }
+      // ---- NGMRES iteration k
+      case T_N_ITER:
+        if (t.k > r->num.snes_max_it) { t.reason = 0; t.pc = T_SOLVE_END; break; }
+        launch_axpy(r->XM, t.X, -1.0, t.F, n9, r->st);       // x^M = x - F(x) (basic line search)
+        r->n_launch++;
+        r->total_iter = t.k;
+        req_residual(t, r->XM, r->FM);
+        t.pc = T_N_M1;
+        return DGX_OK;
+      case T_N_M1: {
+        // |FM|^2, <FM, Fdot_i>, <Fdot_ivec, Fdot_i> in one pass
+        std::vector<const double*> vs;
+        for (int i = 0; i < t.lh; ++i) vs.push_back(r->Fdot[i]);
+        vs.push_back(r->FM);
+        req_multi(t, 0, r->FM, r->Fdot[t.ivec], vs, t.lh, t.tmp.data());
+        t.pc = T_N_LSQ;
+        return DGX_OK;
+      }
+      case T_N_LSQ: {
+        const int m = r->num.ngmres_m, l = t.lh;
+        t.fMnorm = std::sqrt(t.tmp[l]);
+        if (!std::isfinite(t.fMnorm)) { t.reason = -2; t.pc = T_SOLVE_END; break; }
+        double nu = t.fMnorm * t.fMnorm;
+        for (int i = 0; i < l; ++i) { t.xi[i] = t.tmp[i]; t.beta[i] = t.tmp[l + 1 + i]; }
+        for (int i = 0; i < l; ++i) { t.qm[i + m * t.ivec] = t.beta[i]; t.qm[t.ivec + m * i] = t.beta[i]; }
+        for (int i = 0; i < l; ++i) t.beta[i] = nu - t.xi[i];
+        std::vector<double> H((size_t)l * l);
+        for (int j = 0; j < l; ++j)
+          for (int i = 0; i < l; ++i) H[i + l * j] = t.qm[i + m * j] - t.xi[i] - t.xi[j] + nu;
+        if (l == 1) t.beta[0] = H[0] != 0.0 ? t.beta[0] / H[0] : 0.0;
+        else lsq_svd(l, H.data(), t.beta.data());
+        for (int i = 0; i < l; ++i)
+          if (!std::isfinite(t.beta[i])) { set_err("NGMRES: non-finite coefficient"); return DGX_ERR_STATE; }
+        double alph = 0.0;
+        for (int i = 0; i < l; ++i) alph += t.beta[i];
+        VecList xl{};
+        for (int i = 0; i < l; ++i) xl.v[i] = r->Xdot[i];
+        CK(h2d(r, r->d_beta, t.beta.data(), sizeof(double) * l));
+        launch_combine(r->XA, r->XM, xl, l, 1.0 - alph, r->d_beta, n9, r->nb_red, r->st);
+        r->n_launch++;
+        req_residual(t, r->XA, r->FA);
+        t.pc = T_N_A1;
+        return DGX_OK;
+      }
+      case T_N_A1: {
+        if (t.fminnorm > t.fMnorm) t.fminnorm = t.fMnorm;
+        // |FA|^2 ; |XA - XM|^2, |XA - Xdot_i|^2
+        req_multi(t, 0, r->FA, nullptr, {r->FA}, 0, t.tmpA.data());
+        std::vector<const double*> ds;
+        ds.push_back(r->XM);
+        for (int i = 0; i < t.lh; ++i) ds.push_back(r->Xdot[i]);
+        req_multi(t, 1, r->XA, nullptr, ds, 0, t.tmp.data());
+        t.pc = T_N_DECIDE;
+        return DGX_OK;
+      }
+      case T_N_DECIDE: {
+        const int m = r->num.ngmres_m, l = t.lh;
+        double fAnorm = std::sqrt(t.tmpA[0]), dnorm = std::sqrt(t.tmp[0]), dminnorm = -1.0;
+        for (int i = 0; i < l; ++i) { double d = std::sqrt(t.tmp[1 + i]); if (d < dminnorm || dminnorm < 0.0) dminnorm = d; }
+        bool selectA = true;
+        if (fAnorm >= 2.0 * t.fminnorm) selectA = false;
+        if (!(0.1 * dnorm < dminnorm || std::sqrt(t.fnorm) < 0.9 * std::sqrt(t.fminnorm))) selectA = false;
+        if (selectA) { t.fnorm = fAnorm; std::swap(t.F, r->FA); std::swap(t.X, r->XA); }
+        else { t.fnorm = t.fMnorm; std::swap(t.F, r->FM); std::swap(t.X, r->XM); }
+        t.ivec = t.k_restart % m;
+        bool selectRestart = false;
+        if (0.1 * dnorm > dminnorm && std::sqrt(fAnorm) > 0.9 * std::sqrt(t.fminnorm) && l > 0) selectRestart = true;
+        if (std::sqrt(fAnorm) > 2.0 * std::sqrt(t.fminnorm)) selectRestart = true;
+        t.restart_count = selectRestart ? t.restart_count + 1 : 0;
+        if (t.restart_count >= 2) {
+          t.restart_count = 0; t.k_restart = 1; t.lh = 1; t.ivec = 0;
+          const double* srcF = selectA ? r->FM : t.F;    // the x^M pair, wherever it now lives
+          const double* srcX = selectA ? r->XM : t.X;
+          TRY(d2d9(r, r->Fdot[0], srcF)); TRY(d2d9(r, r->Xdot[0], srcX));
+        } else {
+          if (t.lh < m) t.lh++;
+          t.k_restart++;
+          if (t.fminnorm > t.fnorm) t.fminnorm = t.fnorm;
+          TRY(d2d9(r, r->Fdot[t.ivec], t.F)); TRY(d2d9(r, r->Xdot[t.ivec], t.X));
+        }
+        t.reason = converged(r);
+        if (t.reason) { t.pc = T_SOLVE_END; break; }
+        t.k++;
+        t.pc = T_N_ITER;
+        break;
+      }
+      case T_SOLVE_END: {
+        // buffers rotate between X/XM/XA and R/FM/FA; the three stay distinct
+        r->X = t.X; r->R = t.F;
+        solve_epilogue(r, t.reason ? t.reason : -1, &t.conv, &t.sit, &t.sill);
+        t.pc = t.mode == 0 ? T_DONE : T_SUB_AFTER;
+        break;
+      }
+      case T_SUB_AFTER:
+        t.iters += t.sit;
+        if (t.conv) {
+          r->dt_prev = r->dt; r->cut_back = 0; r->guess = 1;
+        } else if (r->cut_back_level < r->num.max_cut_back) {
+          r->cut_back = 1; t.step_fraction = (t.step_fraction - 1) * 2; r->cut_back_level++;
+          r->t -= r->dt; r->dt /= 2; t.cutbacks++;
+        } else {
+          set_err("no solution found for increment %d of load step %d", t.inc + 1, t.l + 1);
+          return DGX_ERR_NOT_CONVERGED;
+        }
+        t.pc = T_SUB_CHECK;
+        break;
+      case T_INC_END: {
+        r->cut_back_level = std::max(0, r->cut_back - 1);
+        if (t.records && (t.mode == 1 || t.nrec < t.max_records)) {
+          dgx_inc_record& rec = t.records[t.mode == 1 ? 0 : t.nrec];
+          rec = dgx_inc_record{};
+          rec.t = r->t; rec.dt = r->dt;
+          memcpy(rec.P_av, r->P_av, sizeof(rec.P_av));
+          memcpy(rec.F_aim, r->F_aim, sizeof(rec.F_aim));
+          TRY(field_average(r, r->X, rec.F_av));
+          rec.iterations = t.iters; rec.evaluations = (int32_t)(r->n_eval - t.ev0);
+          rec.converged = 1; rec.cutbacks = t.cutbacks; rec.err_div = r->err_div; rec.err_BC = r->err_BC;
+          rec.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t.t0).count();
+        }
+        t.nrec++;
+        if (t.mode == 1) { t.pc = T_DONE; break; }
+        if (++t.inc >= t.steps[t.l].N) { t.l++; t.inc = 0; }
+        t.pc = t.l < t.nsteps ? T_INC_BEGIN : T_DONE;
+        break;
+      }
+      case T_DONE:
+        return DGX_OK;
+    }
+  }
+}
+
+// one round: serve every parked request, then advance the tasks that were served.
+// A task that fails is finished with its error; the others go on.
+static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks) {
+  std::vector<ResReq> rq;
+  std::vector<MultiReq> mq;
+  for (Task* t : tasks) {
+    if (t->done() || t->want == 0) continue;
+    if (t->want == 1) rq.push_back({t->r, t->rin, t->rout});
+    else for (int i = 0; i < t->nmq; ++i) mq.push_back(t->mq[i]);
+  }
+  TRY(ex_residual(e, rq));
+  TRY(ex_multi(e, mq));
+  e->rounds++;
+  for (Task* t : tasks) {
+    if (t->done() || t->want == 0) continue;
+    t->want = 0; t->nmq = 0;
+    dgx_status s = advance(*t);
+    if (s != DGX_OK) { t->err = s; t->pc = T_DONE; }
+  }
+  return DGX_OK;
+}
+
+static dgx_status ensure_executor(dgx_rve* r) {
+  if (r->ex) return DGX_OK;
+  return executor_create(1, r->st, r->d_cnt, r->cons_block, &r->ex);
+}
+
+// a solve (mode 0), one increment (mode 1) or a load case (mode 2) of one RVE as a batch of one
+dgx_status run_single(dgx_rve* r, int mode, const dgx_loadstep* steps, int n_or_index, int inc,
+                      dgx_inc_record* records, int max_records, int32_t* n_records, int32_t* conv, int32_t* iterations,
+                      int32_t* ill) {
+  TRY(ensure_executor(r));
+  Task t;
+  t.r = r; t.mode = mode; t.steps = steps; t.records = records; t.max_records = max_records;
+  if (mode == 0) t.pc = T_SOLVE_BEGIN;
+  else if (mode == 1) { t.pc = T_INC_BEGIN; t.l = n_or_index; t.inc = inc; t.nsteps = 1; }
+  else { t.pc = T_LC_BEGIN; t.nsteps = n_or_index; }
+  std::vector<Task*> tasks{&t};
+  dgx_status s = advance(t);
+  while (s == DGX_OK && !t.done()) {
+    s = serve_round(r->ex, tasks);
+    if (s == DGX_OK && t.err != DGX_OK) s = t.err;
+  }
+  if (s == DGX_OK) s = t.err;
+  if (n_records) *n_records = std::min(t.nrec, max_records);
+  if (mode == 0) { if (conv) *conv = t.conv; if (iterations) *iterations = t.sit; if (ill) *ill = t.sill; }
+  return s;
+}
+
+}  // namespace dgx
+
+// ------------------------------------------------------------------ batch C ABI
+using namespace dgx;
+
+struct dgx_batch {
+  cudaStream_t st = nullptr;
+  Executor* ex = nullptr;
+  int cap = 0;
+  struct Member { dgx_rve* r; Task* t; int active; };
+  std::vector<Member> members;      // slot = index; removed members keep their slot (r = null)
+};
+
+extern "C" dgx_status dgx_batch_create(int32_t capacity, int32_t cons_block, dgx_batch** out) {
+  if (!out || capacity < 1 || capacity > 65535) { set_err("dgx_batch_create: capacity in [1, 65535]"); return DGX_ERR_ARG; }
+  dgx_batch* b = new dgx_batch();
+  b->cap = capacity;
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) {
+    set_err("dgx_batch_create: stream"); delete b; return DGX_ERR_CUDA;
+  }
+  dgx_status s = executor_create(capacity, b->st, nullptr, cons_block, &b->ex);
+  if (s != DGX_OK) { cudaStreamDestroy(b->st); delete b; return s; }
+  *out = b;
+  return DGX_OK;
+}
+
+static void batch_detach(dgx_batch::Member& m) {
+  if (!m.r) return;
+  cudaStreamSynchronize(m.r->st);
+  m.r->st = m.r->home_st;
+  m.r->in_batch = 0;
+  delete m.t;
+  m.t = nullptr; m.r = nullptr; m.active = 0;
+}
+
+extern "C" void dgx_batch_destroy(dgx_batch* b) {
+  if (!b) return;
+  for (auto& m : b->members) batch_detach(m);
+  executor_destroy(b->ex);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+extern "C" dgx_status dgx_batch_add(dgx_batch* b, dgx_rve* r, int32_t nsteps, const dgx_loadstep* steps,
+                                    dgx_inc_record* records, int32_t max_records, int32_t* slot) {
+  if (!b || !r || !steps || nsteps < 1) { set_err("dgx_batch_add: null argument"); return DGX_ERR_ARG; }
+  if (r->in_batch) { set_err("dgx_batch_add: RVE already in a batch"); return DGX_ERR_STATE; }
+  int active = 0;
+  for (auto& m : b->members) active += m.active;
+  if (active >= b->cap) { set_err("dgx_batch_add: batch full (%d members)", b->cap); return DGX_ERR_NOMEM; }
+  CK(cudaStreamSynchronize(r->st));
+  r->home_st = r->st;
+  r->st = b->st;
+  r->in_batch = 1;
+  dgx_status s = dgx_solver_init(r);
+  Task* t = new Task();
+  t->r = r; t->mode = 2; t->steps = steps; t->nsteps = nsteps; t->records = records; t->max_records = max_records;
+  t->pc = T_LC_BEGIN;
+  if (s == DGX_OK) s = advance(*t);
+  if (s != DGX_OK) { t->err = s; t->pc = T_DONE; }
+  b->members.push_back({r, t, 1});
+  if (slot) *slot = (int32_t)b->members.size() - 1;
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_batch_step(dgx_batch* b, int32_t* n_active) {
+  if (!b) return DGX_ERR_ARG;
+  std::vector<Task*> tasks;
+  for (auto& m : b->members) if (m.r && !m.t->done()) tasks.push_back(m.t);
+  if (!tasks.empty()) TRY(serve_round(b->ex, tasks));
+  int n = 0;
+  for (auto& m : b->members) {
+    if (m.r && m.active && m.t->done()) m.active = 0;
+    n += m.active;
+  }
+  if (n_active) *n_active = n;
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_batch_run(dgx_batch* b) {
+  if (!b) return DGX_ERR_ARG;
+  int32_t n = 1;
+  while (n > 0) TRY(dgx_batch_step(b, &n));
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_batch_member(const dgx_batch* b, int32_t slot, int32_t* done, int32_t* n_records,
+                                       int32_t* status) {
+  if (!b || slot < 0 || slot >= (int32_t)b->members.size()) return DGX_ERR_ARG;
+  const auto& m = b->members[slot];
+  if (!m.r) { set_err("dgx_batch_member: slot %d was removed", slot); return DGX_ERR_STATE; }
+  if (done) *done = m.t->done() ? 1 : 0;
+  if (n_records) *n_records = std::min(m.t->nrec, m.t->max_records);
+  if (status) *status = m.t->err;
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_batch_remove(dgx_batch* b, int32_t slot) {
+  if (!b || slot < 0 || slot >= (int32_t)b->members.size()) return DGX_ERR_ARG;
+  auto& m = b->members[slot];
+  if (!m.r) return DGX_OK;
+  if (!m.t->done()) { set_err("dgx_batch_remove: member %d still running", slot); return DGX_ERR_STATE; }
+  batch_detach(m);
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_batch_stats(const dgx_batch* b, double ms[3], int64_t out[8]) {
+  if (!b) return DGX_ERR_ARG;
+  const Executor* e = b->ex;
+  if (ms) for (int i = 0; i < 3; ++i) ms[i] = e->t_ms[i];
+  if (out) {
+    ConsCounters c{};
+    CK(cudaMemcpy(&c, e->cnt, sizeof(c), cudaMemcpyDeviceToHost));
+    out[0] = e->point_evals; out[1] = (int64_t)c.state_iters; out[2] = (int64_t)c.lp_iters; out[3] = e->rounds;
+    out[4] = e->launches; out[5] = (int64_t)c.jac_iters; out[6] = e->bytes_h2d; out[7] = e->bytes_d2h;
+  }
+  return DGX_OK;
+}
+
+extern "C" void* dgx_batch_stream(const dgx_batch* b) { return b ? (void*)b->st : nullptr; }

@@ -14,6 +14,8 @@
 //   Jacobian  J = I + dt sum_a |dg_a| vec(P_a) vec(W Q_a)^T,  W = A^T Fe,  Q_a = C : P_a
 //   tangent   lhs = dt sum_a |dg_a| vec(C : U_a) vec(P_a)^T,  U_a = Fe^T (F Fp0^-1) P_a
 // which are algebraically identical to the reference's contractions.
+#include <algorithm>
+
 #include "dgx_internal.cuh"
 
 namespace dgx {
@@ -365,13 +367,13 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 
 __device__ __forceinline__ double ldp(const double* p, int64_t ld, int c, int64_t e) { return p[c * ld + e]; }
 
-// Per-point constitutive response (restore, cut-back driver, FPI, P) plus the
-// block partial sums of P for P_av.  One thread per point.
+// Per-point constitutive response (restore, cut-back driver, FPI, P) of one tile of
+// BS points plus the partial sums of P (per 64 points) for P_av.  One thread per point.
 template <int BS>
-__global__ void __launch_bounds__(BS)
-k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int64_t ldF, double dt,
-               double* __restrict__ Ppart, int* __restrict__ ill, ConsCounters* cnt) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState& ps, const double* __restrict__ Fin,
+                                          int64_t ldF, double dt, double* __restrict__ Ppart, int* __restrict__ ill,
+                                          ConsCounters* cnt, int64_t tile) {
+  const int64_t e = tile * BS + threadIdx.x;
   double P[9];
   unsigned lp_iters = 0, st_iters = 0, jac_iters = 0;
   bool ok = true;
@@ -454,7 +456,7 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
     __syncthreads();
   }
   if ((threadIdx.x & 63) == 0) {
-    const int64_t g = (blockIdx.x * (int64_t)BS + threadIdx.x) >> 6;
+    const int64_t g = (tile * BS + threadIdx.x) >> 6;
     if (g * 64 < ps.n)
 #pragma unroll
       for (int k = 0; k < 9; ++k) Ppart[g * 9 + k] = red[k][threadIdx.x];
@@ -473,6 +475,56 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
       atomicAdd(&cnt->jac_iters, (unsigned long long)jc);
     }
   }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS)
+k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int64_t ldF, double dt,
+               double* __restrict__ Ppart, int* __restrict__ ill, ConsCounters* cnt) {
+  cons_tile<BS>(mp, ps, Fin, ldF, dt, Ppart, ill, cnt, blockIdx.x);
+}
+
+// Batched form: the points of many RVEs (uneven sizes) in one persistent launch.
+// Item i owns tiles [tile0_i, tile0_i + ceil(n_i / BS)); blocks take tiles from a
+// queue (one atomic per tile) so that a few slow tiles do not idle the rest.  Every
+// tile is the same computation as in k_constitutive, so results do not depend on
+// which RVEs share the launch.
+template <int BS>
+__global__ void __launch_bounds__(BS)
+k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitems, long long ntiles,
+                     unsigned long long* __restrict__ queue, ConsCounters* cnt) {
+  __shared__ ConsItem s_it;
+  __shared__ long long s_tile;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long t = (long long)atomicAdd(queue, 1ULL);
+      int lo = 0;
+      if (t < ntiles) {
+        int hi = nitems - 1;
+        while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (items[mid].tile0 <= t) lo = mid; else hi = mid - 1; }
+        s_it = items[lo];
+      }
+      s_tile = t;
+    }
+    __syncthreads();
+    const long long t = s_tile;
+    if (t >= ntiles) break;
+    cons_tile<BS>(mp, s_it.ps, s_it.F, s_it.ldF, s_it.dt, s_it.Ppart, s_it.ill, cnt, t - s_it.tile0);
+  }
+}
+
+// P_av of every item: block i, warp c sums component c (same order as k_pav_finish)
+__global__ void k_pav_finish_batch(const ConsItem* __restrict__ items, double* __restrict__ Pav) {
+  const ConsItem& it = items[blockIdx.x];
+  int c = threadIdx.x >> 5;
+  if (c >= 9) return;
+  const int nblocks = (int)((it.ps.n + 63) / 64);
+  const double* base = it.Ppart + c;
+  double s = 0.0;
+  for (int b = threadIdx.x & 31; b < nblocks; b += 32) s += base[(long)b * 9];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) Pav[9 * blockIdx.x + c] = s * it.wgt;
 }
 
 // Analytic consistent tangent (Fi = I) for one point; writes dPdF (col-major 3333).
@@ -729,6 +781,25 @@ void launch_constitutive(const MatParams& mp, const PointState& ps, const double
   } else {
     k_constitutive<128><<<(int)((ps.n + 127) / 128), 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
   }
+}
+// persistent batched launch: grid = min(tiles, resident blocks); queue must be zero
+void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
+                               unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int block, int grid) {
+  if (block == 64) k_constitutive_batch<64><<<grid, 64, 0, st>>>(mp, items, nitems, ntiles, queue, cnt);
+  else if (block == 256) k_constitutive_batch<256><<<grid, 256, 0, st>>>(mp, items, nitems, ntiles, queue, cnt);
+  else k_constitutive_batch<128><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt);
+}
+int constitutive_batch_resident(int block) {
+  int nb = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (block == 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<64>, 64, 0);
+  else if (block == 256) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<256>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128>, 128, 0);
+  return std::max(1, nb) * std::max(1, sms);
+}
+void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st) {
+  k_pav_finish_batch<<<nitems, 9 * 32, 0, st>>>(items, Pav);
 }
 void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st) {
   k_pav_finish<<<1, 9 * 32, 0, st>>>(Ppart, nblocks, wgt, Pav);

@@ -67,4 +67,29 @@ struct ConsCounters {
   unsigned long long state_iters, lp_iters, jac_iters, points;
 };
 
+// One RVE of a batched constitutive launch (device table, ordered by tile0).
+struct ConsItem {
+  PointState ps;
+  const double* F;           // deformation gradient planes (ld ldF)
+  int64_t ldF;
+  double dt;
+  double wgt;                // 1 / N
+  double* Ppart;             // ceil(n / 64) x 9 partial sums of P
+  int* ill;                  // terminally-ill flag of this RVE
+  long long tile0;           // first tile of this item in the launch
+};
+
+// constitutive.cu launchers
+void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
+                         double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block);
+void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
+                               unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int block, int grid);
+int constitutive_batch_resident(int block);
+void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st);
+void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st);
+void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,
+                    TangentPartial* part, cudaStream_t st);
+void launch_tangent_finish(const TangentPartial* part, int nblocks, double wgt, double* Cvol, double* Cmm,
+                           cudaStream_t st);
+
 }  // namespace dgx

@@ -25,18 +25,9 @@
 
 #include "../../include/dgx.h"
 #include "dgx_internal.cuh"
+#include "rve.cuh"
 #include "spectral.cuh"
 
-namespace dgx {
-// constitutive.cu
-void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
-                         double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block);
-void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st);
-void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,
-                    TangentPartial* part, cudaStream_t st);
-void launch_tangent_finish(const TangentPartial* part, int nblocks, double wgt, double* Cvol, double* Cmm,
-                           cudaStream_t st);
-}  // namespace dgx
 
 using namespace dgx;
 
@@ -46,23 +37,17 @@ extern "C" int dgx_reference_stiffness(double C11, double C12, double C44, int n
 
 // ------------------------------------------------------------------ errors
 static thread_local std::string g_err;
-static void set_err(const char* fmt, ...) {
+namespace dgx {
+void set_err(const char* fmt, ...) {
   char buf[512];
   va_list ap; va_start(ap, fmt); vsnprintf(buf, sizeof(buf), fmt, ap); va_end(ap);
   g_err = buf;
 }
+}  // namespace dgx
 extern "C" const char* dgx_last_error(void) { return g_err.c_str(); }
 
-#define CK(call)                                                                              \
-  do {                                                                                        \
-    cudaError_t e_ = (call);                                                                  \
-    if (e_ != cudaSuccess) { set_err("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); return DGX_ERR_CUDA; } \
-  } while (0)
-
 // ------------------------------------------------------------------ vector kernels
-namespace {
-
-constexpr int RB = 256;  // threads per reduction block
+namespace dgx {
 
 __global__ void k_init_points(PointState ps, const int32_t* __restrict__ mat, const double* __restrict__ R,
                               int nmat, double xi0) {
@@ -112,8 +97,6 @@ __global__ void k_axpy(double* __restrict__ z, const double* __restrict__ x, dou
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t < n) z[t] = x[t] + a * y[t];
 }
-
-struct VecList { const double* v[32]; };
 
 // XA = (1 - sum beta) XM + sum_i beta_i Xdot_i
 __global__ void k_combine(double* __restrict__ XA, const double* __restrict__ XM, VecList Xd, int l, double c0,
@@ -210,7 +193,6 @@ __global__ void k_rate(double* __restrict__ rate, const double* __restrict__ F0,
   }
 }
 
-inline int nblk(int64_t n, int b = 256) { return (int)((n + b - 1) / b); }
 
 // ------------------------------------------------------------------ small host math
 void mm3(const double* A, const double* B, double* C) {
@@ -403,75 +385,8 @@ MatParams make_params(const dgx_material& m) {
 
 }  // namespace
 
-// ------------------------------------------------------------------ RVE object
-struct dgx_rve {
-  int cells[3];
-  int64_t N;
-  double geom[3], scaled[3], wgt;
-  dgx_material mat;
-  dgx_numerics num;
-  MatParams mp;
-  cudaStream_t st = nullptr;
-  bool owns_stream = false;
-  // device memory
-  std::vector<void*> allocs;
-  int64_t bytes = 0;
-  PointState ps{};
-  double *X = nullptr, *R = nullptr, *XM = nullptr, *FM = nullptr, *XA = nullptr, *FA = nullptr;
-  double *F_last_inc = nullptr, *F_dot = nullptr;
-  std::vector<double*> Xdot, Fdot;
-  void* spec = nullptr;
-  double *d_Pav = nullptr, *d_Cvol = nullptr, *d_Cmm = nullptr, *d_Cref = nullptr, *d_aim = nullptr, *d_rms = nullptr;
-  double *d_Ppart = nullptr, *d_divpart = nullptr, *d_redpart = nullptr, *d_redout = nullptr, *d_beta = nullptr;
-  TangentPartial* d_tpart = nullptr;
-  int* d_ill = nullptr;
-  ConsCounters* d_cnt = nullptr;
-  double *d_xi_x = nullptr, *d_xi_y = nullptr, *d_xi_z = nullptr;
-  double* d_dPdF = nullptr;        // optional (81 planes) for the boundary call
-  int32_t* d_mat = nullptr;
-  double* d_Rm = nullptr;
-  int n_materials = 0;
-  std::vector<int32_t> h_mat;
-  std::vector<double> h_orient;
-  AxisHost ax[3];
-  SpecLaunch sl{};
-  int nb_cons = 0, nb_tan = 0, nb_red = 0;
-  int cons_block = 128;
-  // host solver state (MechBase / MechSolverBasic members)
-  double F_aim[9], F_aim_last_inc[9], F_aim_dot[9], P_aim[9], P_av[9];
-  double C_volAvg[81], C_minMaxAvg[81], C_volAvgLastInc[81], C_minMaxAvgLastInc[81], C_ref[81], S[81];
-  int stress_mask[9];
-  double rot_q[4];
-  double delta_t = 0.0;
-  double err_div = 0.0, err_BC = 0.0;
-  int terminally_ill = 0, total_iter = 0;
-  bool tangent_fresh = false, initialized = false;
-  double tangent_dt = 0.0;
-  // load-case loop state (DamaskGrid::loop_over_loadcase)
-  int cut_back = 0, cut_back_level = 0;
-  double t = 0.0, dt = 1.0, dt_prev = 0.0, t_0 = 0.0;
-  int guess = 0, cur_step = -1;
-  // counters
-  int64_t n_eval = 0, n_tangent = 0, n_launch = 0;
-  // CUDA-event timers on the RVE stream: [0] constitutive kernel, [1] spectral chain, [2] tangent
-  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  double t_ms[3] = {0, 0, 0};
-  int64_t t_n[3] = {0, 0, 0};
-  bool timing = true;
-  int64_t bytes_h2d = 0, bytes_d2h = 0;
-};
 
-namespace {
-
-// counted host<->device copies on the RVE stream (bytes per direction)
-inline cudaError_t h2d(dgx_rve* r, void* dst, const void* src, size_t bytes) {
-  r->bytes_h2d += (int64_t)bytes;
-  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, r->st);
-}
-inline cudaError_t d2h(dgx_rve* r, void* dst, const void* src, size_t bytes) {
-  r->bytes_d2h += (int64_t)bytes;
-  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, r->st);
-}
+namespace dgx {
 
 template <typename T>
 dgx_status dalloc(dgx_rve* r, T** p, size_t count) {
@@ -484,65 +399,13 @@ dgx_status dalloc(dgx_rve* r, T** p, size_t count) {
   return DGX_OK;
 }
 
-#define TRY(x) do { dgx_status s_ = (x); if (s_ != DGX_OK) return s_; } while (0)
 
-// fused reductions
-dgx_status multi(dgx_rve* r, int mode, const double* a, const double* b, const std::vector<const double*>& vs,
-                 int K2, double* out) {
-  int K = (int)vs.size();
-  if (K == 0) return DGX_OK;
-  VecList vl{};
-  for (int k = 0; k < K; ++k) vl.v[k] = vs[k];
-  int64_t n = 9 * r->N;
-  k_multi<<<r->nb_red, RB, 0, r->st>>>(mode, a, b, vl, K, K2, n, r->d_redpart);
-  k_multi_finish<<<K + K2, 32, 0, r->st>>>(r->d_redpart, r->nb_red, K + K2, r->d_redout);
-  r->n_launch += 2;
-  CK(d2h(r, out, r->d_redout, sizeof(double) * (K + K2)));
-  CK(cudaStreamSynchronize(r->st));
-  return DGX_OK;
-}
-dgx_status norm2(dgx_rve* r, const double* v, double* out) {
-  double s;
-  TRY(multi(r, 0, v, nullptr, {v}, 0, &s));
-  *out = std::sqrt(s);
-  return DGX_OK;
-}
-
-// Spectral::constitutive_response on the device: P (ps.P), P_av (host), optional tangent
-dgx_status constitutive_response(dgx_rve* r, const double* X, double dt, bool want_tangent) {
-  r->n_eval++;
-  CK(cudaMemsetAsync(r->d_ill, 0, sizeof(int), r->st));
-  if (r->timing) cudaEventRecord(r->ev[0], r->st);
-  launch_constitutive(r->mp, r->ps, X, r->N, dt, r->d_Ppart, r->d_ill, r->d_cnt, r->st, r->cons_block);
-  if (r->timing) cudaEventRecord(r->ev[1], r->st);
-  launch_pav_finish(r->d_Ppart, r->nb_cons, r->wgt, r->d_Pav, r->st);
-  r->n_launch += 2;
+// host tail of Spectral::constitutive_response (spectral.cpp:132-219) once P_av and
+// the terminally-ill flag are on the host
+dgx_status post_constitutive(dgx_rve* r, int ill, bool want_tangent) {
   r->tangent_fresh = false;
-  r->tangent_dt = dt;
-  if (want_tangent) {
-    if (r->timing) cudaEventRecord(r->ev[4], r->st);
-    launch_tangent(r->mp, r->ps, dt, r->d_dPdF, r->N, r->d_tpart, r->st);
-    if (r->timing) cudaEventRecord(r->ev[5], r->st);
-    launch_tangent_finish(r->d_tpart, r->nb_tan, r->wgt, r->d_Cvol, r->d_Cmm, r->st);
-    r->n_launch += 2;
-    r->n_tangent++;
-    r->tangent_fresh = true;
-  }
-  int ill = 0;
-  CK(d2h(r, r->P_av, r->d_Pav, 9 * sizeof(double)));
-  CK(d2h(r, &ill, r->d_ill, sizeof(int)));
-  CK(cudaStreamSynchronize(r->st));
-  CK(cudaGetLastError());
-  if (r->timing) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]); r->t_ms[0] += ms; r->t_n[0]++;
-    if (want_tangent) { cudaEventElapsedTime(&ms, r->ev[4], r->ev[5]); r->t_ms[2] += ms; r->t_n[2]++; }
-  }
   if (ill) r->terminally_ill = 1;
-  if (want_tangent) {
-    CK(d2h(r, r->C_volAvg, r->d_Cvol, 81 * sizeof(double))); CK(cudaStreamSynchronize(r->st));
-    CK(d2h(r, r->C_minMaxAvg, r->d_Cmm, 81 * sizeof(double))); CK(cudaStreamSynchronize(r->st));
-  }
+  if (want_tangent) TRY(ensure_tangent(r));
   if (!(r->rot_q[0] == 1.0 && r->rot_q[1] == 0.0 && r->rot_q[2] == 0.0 && r->rot_q[3] == 0.0)) {
     double t[9];
     rotate2(r->rot_q, r->P_av, t, false);
@@ -551,10 +414,36 @@ dgx_status constitutive_response(dgx_rve* r, const double* X, double dt, bool wa
   return DGX_OK;
 }
 
+// Spectral::constitutive_response on the device for one RVE: P (ps.P), P_av (host),
+// optional tangent.  Used by the initial reference-stiffness pass and the boundary
+// call; the solver's residual evaluations go through the batched executor.
+dgx_status constitutive_response(dgx_rve* r, const double* X, double dt, bool want_tangent) {
+  r->n_eval++;
+  CK(cudaMemsetAsync(r->d_ill, 0, sizeof(int), r->st));
+  if (r->timing) cudaEventRecord(r->ev[0], r->st);
+  launch_constitutive(r->mp, r->ps, X, r->N, dt, r->d_Ppart, r->d_ill, r->d_cnt, r->st, r->cons_block);
+  if (r->timing) cudaEventRecord(r->ev[1], r->st);
+  launch_pav_finish(r->d_Ppart, r->nb_cons, r->wgt, r->d_Pav, r->st);
+  r->n_launch += 2;
+  r->tangent_dt = dt;
+  int ill = 0;
+  CK(d2h(r, r->P_av, r->d_Pav, 9 * sizeof(double)));
+  CK(d2h(r, &ill, r->d_ill, sizeof(int)));
+  CK(cudaStreamSynchronize(r->st));
+  CK(cudaGetLastError());
+  if (r->timing) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r->ev[0], r->ev[1]); r->t_ms[0] += ms; r->t_n[0]++;
+  }
+  return post_constitutive(r, ill, want_tangent);
+}
+
 // make C_volAvg / C_minMaxAvg current (lazy tangent of the last evaluation)
 dgx_status ensure_tangent(dgx_rve* r) {
   if (r->tangent_fresh) return DGX_OK;
+  if (r->timing) cudaEventRecord(r->ev[4], r->st);
   launch_tangent(r->mp, r->ps, r->tangent_dt, r->d_dPdF, r->N, r->d_tpart, r->st);
+  if (r->timing) cudaEventRecord(r->ev[5], r->st);
   launch_tangent_finish(r->d_tpart, r->nb_tan, r->wgt, r->d_Cvol, r->d_Cmm, r->st);
   r->n_launch += 2;
   r->n_tangent++;
@@ -562,6 +451,10 @@ dgx_status ensure_tangent(dgx_rve* r) {
   CK(d2h(r, r->C_minMaxAvg, r->d_Cmm, 81 * sizeof(double)));
   CK(cudaStreamSynchronize(r->st));
   CK(cudaGetLastError());
+  if (r->timing) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r->ev[4], r->ev[5]); r->t_ms[2] += ms; r->t_n[2]++;
+  }
   r->tangent_fresh = true;
   return DGX_OK;
 }
@@ -576,10 +469,9 @@ GammaArgs gamma_args(dgx_rve* r, bool gamma, bool div) {
   return ga;
 }
 
-// form_residual (mech_solver_basic.cpp:286-339): R = Gamma * P(X), zero frequency <- rotated dF_aim
-dgx_status form_residual(dgx_rve* r, const double* X, double* Rv) {
-  bool want_t = !r->num.lazy_tangent;
-  TRY(constitutive_response(r, X, r->delta_t, want_t));
+// stress-BC part of form_residual (mech_solver_basic.cpp:321-334): dF_aim = S : P_av,
+// F_aim -= dF_aim, err_BC; the rotated dF_aim is the zero-frequency value of Gamma * P
+void residual_bc(dgx_rve* r, double aim[9]) {
   double dF[9];
   for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) {
     double s = 0.0;
@@ -590,24 +482,7 @@ dgx_status form_residual(dgx_rve* r, const double* X, double* Rv) {
   double err = 0.0;
   for (int k = 0; k < 9; ++k) if (!r->stress_mask[k]) err = std::max(err, std::fabs(r->P_av[k] - r->P_aim[k]));
   r->err_BC = err;
-  double rot[9];
-  rotate2(r->rot_q, dF, rot, true);
-  CK(h2d(r, r->d_aim, rot, 9 * sizeof(double)));
-  GammaArgs ga = gamma_args(r, true, true);
-  if (r->timing) cudaEventRecord(r->ev[2], r->st);
-  spec_convolve(r->sl, r->num.precision == 1, r->ax[0].plan, r->ax[1].plan, r->ax[2].plan, r->ps.P, Rv, r->N, r->spec,
-                ga, r->st);
-  spec_div_finish(r->d_divpart, r->sl.nbz, r->wgt, r->cells[0], r->d_rms, r->st);
-  if (r->timing) cudaEventRecord(r->ev[3], r->st);
-  r->n_launch += 6;
-  CK(d2h(r, &r->err_div, r->d_rms, sizeof(double)));
-  CK(cudaStreamSynchronize(r->st));
-  CK(cudaGetLastError());
-  if (r->timing) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, r->ev[2], r->ev[3]); r->t_ms[1] += ms; r->t_n[1]++;
-  }
-  return DGX_OK;
+  rotate2(r->rot_q, dF, aim, true);
 }
 
 int converged(dgx_rve* r) {
@@ -621,113 +496,44 @@ int converged(dgx_rve* r) {
   return 0;
 }
 
-dgx_status d2d(dgx_rve* r, double* dst, const double* src) {
-  CK(cudaMemcpyAsync(dst, src, sizeof(double) * 9 * r->N, cudaMemcpyDeviceToDevice, r->st));
+// MechSolverBasic::calculate_solution (mech_solver_basic.cpp:110-160) before SNESSolve
+dgx_status solve_prologue(dgx_rve* r) {
+  masked_compliance(r->C_volAvg, r->rot_q, r->stress_mask, r->S);
+  if (r->num.update_gamma) {
+    for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
+    CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
+  }
   return DGX_OK;
 }
 
-// SNESSolve with NGMRES (or fixed point): X in/out; returns reason (>0 conv, <0 div)
-dgx_status snes_solve(dgx_rve* r, int* reason_out) {
-  const int64_t n9 = 9 * r->N;
-  const int m = r->num.ngmres_m;
-  double* X = r->X;
-  double* F = r->R;
-  r->total_iter = 0;
-  TRY(form_residual(r, X, F));
-  double fnorm;
-  TRY(norm2(r, F, &fnorm));
-  if (!std::isfinite(fnorm)) { *reason_out = -2; return DGX_OK; }
-  double fminnorm = fnorm;
-  int reason = converged(r);
-  if (reason) { *reason_out = reason; return DGX_OK; }
-  if (r->num.solver == 1) {
-    for (int k = 1; k <= r->num.snes_max_it; ++k) {
-      k_axpy<<<nblk(n9), 256, 0, r->st>>>(X, X, -1.0, F, n9);
-      r->n_launch++;
-      r->total_iter = k;
-      TRY(form_residual(r, X, F));
-      double fn;
-      TRY(norm2(r, F, &fn));
-      if (!std::isfinite(fn)) { *reason_out = -2; return DGX_OK; }
-      reason = converged(r);
-      if (reason) { *reason_out = reason; return DGX_OK; }
-    }
-    *reason_out = -1;
-    return DGX_OK;
-  }
-  std::vector<double> q((size_t)m * m, 0.0), H, beta(m), xi(m), tmp(2 * m + 2);
-  TRY(d2d(r, r->Fdot[0], F)); TRY(d2d(r, r->Xdot[0], X));
-  int k_restart = 1, l = 1, ivec = 0, restart_count = 0;
-  for (int k = 1; k <= r->num.snes_max_it; ++k) {
-    k_axpy<<<nblk(n9), 256, 0, r->st>>>(r->XM, X, -1.0, F, n9);
-    r->n_launch++;
-    r->total_iter = k;
-    TRY(form_residual(r, r->XM, r->FM));
-    // |FM|^2, <FM, Fdot_i>, <Fdot_ivec, Fdot_i> in one pass
-    std::vector<const double*> vs;
-    for (int i = 0; i < l; ++i) vs.push_back(r->Fdot[i]);
-    vs.push_back(r->FM);
-    TRY(multi(r, 0, r->FM, r->Fdot[ivec], vs, l, tmp.data()));
-    double fMnorm = std::sqrt(tmp[l]);
-    if (!std::isfinite(fMnorm)) { *reason_out = -2; return DGX_OK; }
-    double nu = fMnorm * fMnorm;
-    for (int i = 0; i < l; ++i) { xi[i] = tmp[i]; beta[i] = tmp[l + 1 + i]; }
-    for (int i = 0; i < l; ++i) { q[i + m * ivec] = beta[i]; q[ivec + m * i] = beta[i]; }
-    for (int i = 0; i < l; ++i) beta[i] = nu - xi[i];
-    H.assign((size_t)l * l, 0.0);
-    for (int j = 0; j < l; ++j) for (int i = 0; i < l; ++i) H[i + l * j] = q[i + m * j] - xi[i] - xi[j] + nu;
-    if (l == 1) beta[0] = H[0] != 0.0 ? beta[0] / H[0] : 0.0;
-    else lsq_svd(l, H.data(), beta.data());
-    for (int i = 0; i < l; ++i) if (!std::isfinite(beta[i])) { set_err("NGMRES: non-finite coefficient"); return DGX_ERR_STATE; }
-    double alph = 0.0;
-    for (int i = 0; i < l; ++i) alph += beta[i];
-    VecList xl{};
-    for (int i = 0; i < l; ++i) xl.v[i] = r->Xdot[i];
-    CK(h2d(r, r->d_beta, beta.data(), sizeof(double) * l));
-    k_combine<<<r->nb_red, 256, 0, r->st>>>(r->XA, r->XM, xl, l, 1.0 - alph, r->d_beta, n9);
-    r->n_launch++;
-    TRY(form_residual(r, r->XA, r->FA));
-    if (fminnorm > fMnorm) fminnorm = fMnorm;
-    // |FA|, |XA - XM|, |Xdot_i - XA|
-    double fAn2, dn2;
-    TRY(multi(r, 0, r->FA, nullptr, {r->FA}, 0, &fAn2));
-    std::vector<const double*> ds;
-    ds.push_back(r->XM);
-    for (int i = 0; i < l; ++i) ds.push_back(r->Xdot[i]);
-    TRY(multi(r, 1, r->XA, nullptr, ds, 0, tmp.data()));
-    dn2 = tmp[0];
-    double fAnorm = std::sqrt(fAn2), dnorm = std::sqrt(dn2), dminnorm = -1.0;
-    for (int i = 0; i < l; ++i) { double d = std::sqrt(tmp[1 + i]); if (d < dminnorm || dminnorm < 0.0) dminnorm = d; }
-    bool selectA = true;
-    if (fAnorm >= 2.0 * fminnorm) selectA = false;
-    if (!(0.1 * dnorm < dminnorm || std::sqrt(fnorm) < 0.9 * std::sqrt(fminnorm))) selectA = false;
-    if (selectA) { fnorm = fAnorm; std::swap(F, r->FA); std::swap(X, r->XA); }
-    else { fnorm = fMnorm; std::swap(F, r->FM); std::swap(X, r->XM); }
-    ivec = k_restart % m;
-    bool selectRestart = false;
-    if (0.1 * dnorm > dminnorm && std::sqrt(fAnorm) > 0.9 * std::sqrt(fminnorm) && l > 0) selectRestart = true;
-    if (std::sqrt(fAnorm) > 2.0 * std::sqrt(fminnorm)) selectRestart = true;
-    restart_count = selectRestart ? restart_count + 1 : 0;
-    if (restart_count >= 2) {
-      restart_count = 0; k_restart = 1; l = 1; ivec = 0;
-      const double* srcF = selectA ? r->FM : F;   // FM buffer (unselected or aliased)
-      const double* srcX = selectA ? r->XM : X;
-      // FM/XM: if XM was selected it now lives in F/X
-      TRY(d2d(r, r->Fdot[0], srcF)); TRY(d2d(r, r->Xdot[0], srcX));
-    } else {
-      if (l < m) l++;
-      k_restart++;
-      if (fminnorm > fnorm) fminnorm = fnorm;
-      TRY(d2d(r, r->Fdot[ivec], F)); TRY(d2d(r, r->Xdot[ivec], X));
-    }
-    reason = converged(r);
-    if (reason) break;
-  }
-  // buffers rotate between X/XM/XA and R/FM/FA; the three stay distinct
-  r->X = X;
-  r->R = F;
-  *reason_out = reason ? reason : -1;
+// ... and after it: terminally-ill flag, stress aim of the mixed BC, solution status
+void solve_epilogue(dgx_rve* r, int reason, int32_t* conv, int32_t* iterations, int32_t* ill_out) {
+  int ill = r->terminally_ill;
+  r->terminally_ill = 0;
+  for (int k = 0; k < 9; ++k) if (r->stress_mask[k]) r->P_aim[k] = r->P_av[k];
+  if (conv) *conv = (reason > 0) && !ill;
+  if (iterations) *iterations = r->total_iter;
+  if (ill_out) *ill_out = ill;
+}
+
+// volume average of a 9-plane field (fixed-order reduction)
+dgx_status field_average(dgx_rve* r, const double* X, double out[9]) {
+  k_plane_sums<<<r->nb_red, RB, 0, r->st>>>(X, r->N, r->d_redpart);
+  k_multi_finish<<<9, 32, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
+  r->n_launch += 2;
+  double sums[9];
+  CK(d2h(r, sums, r->d_redout, 9 * sizeof(double)));
+  CK(cudaStreamSynchronize(r->st));
+  for (int k = 0; k < 9; ++k) out[k] = sums[k] * r->wgt;
   return DGX_OK;
+}
+
+void launch_axpy(double* z, const double* x, double a, const double* y, int64_t n, cudaStream_t st) {
+  k_axpy<<<nblk(n), 256, 0, st>>>(z, x, a, y, n);
+}
+void launch_combine(double* XA, const double* XM, const VecList& Xd, int l, double c0, const double* beta, int64_t n,
+                    int nb, cudaStream_t st) {
+  k_combine<<<nb, 256, 0, st>>>(XA, XM, Xd, l, c0, beta, n);
 }
 
 double forward_time(const dgx_loadstep* ls, int inc, int sub_step_factor, int cut_back_level) {
@@ -793,6 +599,7 @@ extern "C" void dgx_numerics_default(dgx_numerics* n) {
 
 extern "C" void dgx_rve_destroy(dgx_rve* r) {
   if (!r) return;
+  if (r->ex) executor_destroy(r->ex);
   for (auto p : r->allocs) cudaFree(p);
   for (int i = 0; i < 3; ++i) axis_destroy(&r->ax[i]);
   for (int i = 0; i < 6; ++i) if (r->ev[i]) cudaEventDestroy(r->ev[i]);
@@ -871,8 +678,8 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
   AL(&r->d_Ppart, 9 * (int64_t)r->nb_cons);
   AL(&r->d_tpart, r->nb_tan);
   AL(&r->d_divpart, r->sl.nbz);
-  AL(&r->d_redpart, 64 * (int64_t)r->nb_red);
-  AL(&r->d_redout, 64); AL(&r->d_beta, 32);
+  AL(&r->d_redpart, 128 * (int64_t)r->nb_red);   // two concurrent fused reductions of up to 64 sums
+  AL(&r->d_redout, 128); AL(&r->d_beta, 32);
   AL(&r->d_Pav, 9); AL(&r->d_Cvol, 81); AL(&r->d_Cmm, 81); AL(&r->d_Cref, 81); AL(&r->d_aim, 9); AL(&r->d_rms, 1);
   AL(&r->d_ill, 1); AL(&r->d_cnt, 1);
   AL(&r->d_xi_x, cells[0] / 2 + 1); AL(&r->d_xi_y, cells[1]); AL(&r->d_xi_z, cells[2]);
@@ -1117,90 +924,24 @@ extern "C" dgx_status dgx_solver_forward(dgx_rve* r, int32_t cutback, int32_t gu
 extern "C" dgx_status dgx_solver_solve(dgx_rve* r, int32_t* conv, int32_t* iterations, int32_t* ill_out) {
   if (!r) return DGX_ERR_ARG;
   if (!r->initialized) { set_err("dgx_solver_solve before dgx_solver_init"); return DGX_ERR_STATE; }
-  masked_compliance(r->C_volAvg, r->rot_q, r->stress_mask, r->S);
-  if (r->num.update_gamma) {
-    for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
-    CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
-  }
-  int reason = 0;
-  TRY(snes_solve(r, &reason));
-  int ill = r->terminally_ill;
-  r->terminally_ill = 0;
-  for (int k = 0; k < 9; ++k) if (r->stress_mask[k]) r->P_aim[k] = r->P_av[k];
-  if (conv) *conv = (reason > 0) && !ill;
-  if (iterations) *iterations = r->total_iter;
-  if (ill_out) *ill_out = ill;
-  return DGX_OK;
-}
-
-static dgx_status run_one_increment(dgx_rve* r, const dgx_loadstep* ls, int l, int inc, dgx_inc_record* rec) {
-  if (l != r->cur_step) { r->cur_step = l; r->t_0 = r->t; r->guess = ls->estimate_rate && l > 0; }
-  auto t0 = std::chrono::steady_clock::now();
-  const int sub_step_factor = 2;
-  r->dt_prev = r->dt;
-  r->dt = forward_time(ls, inc, sub_step_factor, r->cut_back_level);
-  int step_fraction = 0, iters = 0, cutbacks = 0;
-  int64_t ev0 = r->n_eval;
-  while (step_fraction < (int)std::pow(sub_step_factor, r->cut_back_level)) {
-    double t_remaining = ls->t + r->t_0 - r->t;
-    r->t += r->dt;
-    step_fraction++;
-    TRY(dgx_solver_forward(r, r->cut_back, r->guess, r->dt, r->dt_prev, t_remaining, ls));
-    if (!r->cut_back) TRY(commit(r));
-    int32_t conv = 0, it = 0, ill = 0;
-    TRY(dgx_solver_solve(r, &conv, &it, &ill));
-    iters += it;
-    if (conv) {
-      r->dt_prev = r->dt; r->cut_back = 0; r->guess = 1;
-    } else if (r->cut_back_level < r->num.max_cut_back) {
-      r->cut_back = 1; step_fraction = (step_fraction - 1) * sub_step_factor; r->cut_back_level++;
-      r->t -= r->dt; r->dt /= sub_step_factor; cutbacks++;
-    } else {
-      set_err("no solution found for increment %d of load step %d", inc + 1, l + 1);
-      return DGX_ERR_NOT_CONVERGED;
-    }
-  }
-  r->cut_back_level = std::max(0, r->cut_back - 1);
-  if (rec) {
-    rec->t = r->t; rec->dt = r->dt;
-    memcpy(rec->P_av, r->P_av, sizeof(rec->P_av));
-    memcpy(rec->F_aim, r->F_aim, sizeof(rec->F_aim));
-    k_plane_sums<<<r->nb_red, RB, 0, r->st>>>(r->X, r->N, r->d_redpart);
-    k_multi_finish<<<9, 32, 0, r->st>>>(r->d_redpart, r->nb_red, 9, r->d_redout);
-    r->n_launch += 2;
-    double sums[9];
-    CK(d2h(r, sums, r->d_redout, 9 * sizeof(double)));
-    CK(cudaStreamSynchronize(r->st));
-    for (int k = 0; k < 9; ++k) rec->F_av[k] = sums[k] * r->wgt;
-    rec->iterations = iters; rec->evaluations = (int32_t)(r->n_eval - ev0);
-    rec->converged = 1; rec->cutbacks = cutbacks; rec->err_div = r->err_div; rec->err_BC = r->err_BC;
-    rec->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  }
-  return DGX_OK;
+  if (r->in_batch) { set_err("RVE is driven by a batch"); return DGX_ERR_STATE; }
+  return run_single(r, 0, nullptr, 0, 0, nullptr, 0, nullptr, conv, iterations, ill_out);
 }
 
 extern "C" dgx_status dgx_run_increment(dgx_rve* r, const dgx_loadstep* step, int32_t step_index, int32_t inc,
                                         dgx_inc_record* record) {
   if (!r || !step) return DGX_ERR_ARG;
   if (!r->initialized) { set_err("dgx_run_increment before dgx_solver_init"); return DGX_ERR_STATE; }
-  return run_one_increment(r, step, step_index, inc, record);
+  if (r->in_batch) { set_err("RVE is driven by a batch"); return DGX_ERR_STATE; }
+  return run_single(r, 1, step, step_index, inc, record, 1, nullptr, nullptr, nullptr, nullptr);
 }
 
 extern "C" dgx_status dgx_run_loadcase(dgx_rve* r, int32_t nsteps, const dgx_loadstep* steps, dgx_inc_record* records,
                                        int32_t max_records, int32_t* n_records) {
   if (!r || !steps || nsteps < 1) return DGX_ERR_ARG;
+  if (r->in_batch) { set_err("RVE is driven by a batch"); return DGX_ERR_STATE; }
   TRY(dgx_solver_init(r));
-  int nrec = 0;
-  for (int l = 0; l < nsteps; ++l)
-    for (int inc = 0; inc < steps[l].N; ++inc) {
-      dgx_inc_record rec{};
-      TRY(run_one_increment(r, &steps[l], l, inc, &rec));
-      if (records && nrec < max_records) records[nrec] = rec;
-      nrec++;
-      if (n_records) *n_records = std::min(nrec, max_records);
-    }
-  if (n_records) *n_records = std::min(nrec, max_records);
-  return DGX_OK;
+  return run_single(r, 2, steps, nsteps, 0, records, max_records, n_records, nullptr, nullptr, nullptr);
 }
 
 extern "C" dgx_status dgx_get(dgx_rve* r, const char* name, double* out) {
@@ -1231,7 +972,10 @@ extern "C" void* dgx_rve_stream(const dgx_rve* r) { return r ? (void*)r->st : nu
 
 extern "C" dgx_status dgx_timers(const dgx_rve* r, double ms[3], int64_t launches[3]) {
   if (!r || !ms) return DGX_ERR_ARG;
-  for (int i = 0; i < 3; ++i) { ms[i] = r->t_ms[i]; if (launches) launches[i] = r->t_n[i]; }
+  int64_t n[3] = {0, 0, 0}, l = 0, hb = 0, db = 0;
+  for (int i = 0; i < 3; ++i) { ms[i] = r->t_ms[i]; n[i] = r->t_n[i]; }
+  if (r->ex) executor_stats(r->ex, ms, n, &l, &hb, &db);
+  if (launches) for (int i = 0; i < 3; ++i) launches[i] = n[i];
   return DGX_OK;
 }
 
@@ -1239,7 +983,10 @@ extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[8]) {
   if (!r || !out) return DGX_ERR_ARG;
   ConsCounters c{};
   CK(cudaMemcpy(&c, r->d_cnt, sizeof(c), cudaMemcpyDeviceToHost));
+  double ms[3] = {0, 0, 0};
+  int64_t n[3] = {0, 0, 0}, l = 0, hb = 0, db = 0;
+  if (r->ex) executor_stats(r->ex, ms, n, &l, &hb, &db);
   out[0] = r->n_eval; out[1] = (int64_t)c.state_iters; out[2] = (int64_t)c.lp_iters; out[3] = r->n_tangent;
-  out[4] = r->n_launch; out[5] = (int64_t)c.jac_iters; out[6] = r->bytes_h2d; out[7] = r->bytes_d2h;
+  out[4] = r->n_launch + l; out[5] = (int64_t)c.jac_iters; out[6] = r->bytes_h2d + hb; out[7] = r->bytes_d2h + db;
   return DGX_OK;
 }

@@ -104,8 +104,9 @@ __device__ typename cpx<R>::t* block_fft(typename cpx<R>::t* a, typename cpx<R>:
 // forward: real planes (ld_in) -> spectrum planes (stride Nh); one block = LX lines
 template <typename R, typename Rin>
 __global__ void k_xfwd(SpecGeom g, AxisPlan px, const Rin* __restrict__ field, long long ld_in,
-                       typename cpx<R>::t* __restrict__ spec, int LX) {
+                       typename cpx<R>::t* __restrict__ spec, int LX, const SpecItem* __restrict__ items) {
   typedef typename cpx<R>::t C;
+  if (items) { field = (const Rin*)items[blockIdx.y].in; spec = (C*)items[blockIdx.y].spec; }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* a = reinterpret_cast<C*>(smem_raw);
   C* b = a + (long)LX * g.N0;
@@ -133,8 +134,9 @@ __global__ void k_xfwd(SpecGeom g, AxisPlan px, const Rin* __restrict__ field, l
 // If `accumulate`, out += scale * result (FP64 accumulation of an update).
 template <typename R, typename Rout>
 __global__ void k_xinv(SpecGeom g, AxisPlan px, const typename cpx<R>::t* __restrict__ spec, Rout* __restrict__ field,
-                       long long ld_out, int LX) {
+                       long long ld_out, int LX, const SpecItem* __restrict__ items) {
   typedef typename cpx<R>::t C;
+  if (items) { spec = (const C*)items[blockIdx.y].spec; field = (Rout*)items[blockIdx.y].out; }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* a = reinterpret_cast<C*>(smem_raw);
   C* b = a + (long)LX * g.N0;
@@ -165,8 +167,10 @@ __global__ void k_xinv(SpecGeom g, AxisPlan px, const typename cpx<R>::t* __rest
 // ---------------------------------------------------------------- y pass
 // block = (tile of TI x-frequencies) x (component, z); lines along y, stride N0r
 template <typename R>
-__global__ void k_ypass(SpecGeom g, AxisPlan py, typename cpx<R>::t* __restrict__ spec, int TI, int sign) {
+__global__ void k_ypass(SpecGeom g, AxisPlan py, typename cpx<R>::t* __restrict__ spec, int TI, int sign,
+                        const SpecItem* __restrict__ items) {
   typedef typename cpx<R>::t C;
+  if (items) spec = (C*)items[blockIdx.y].spec;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* a = reinterpret_cast<C*>(smem_raw);
   C* b = a + (long)TI * g.N1;
@@ -192,8 +196,13 @@ __global__ void k_ypass(SpecGeom g, AxisPlan py, typename cpx<R>::t* __restrict_
 // ---------------------------------------------------------------- z pass + Gamma + div
 
 template <typename R>
-__global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict__ spec, int TI, GammaArgs ga) {
+__global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict__ spec, int TI, GammaArgs ga,
+                        const SpecItem* __restrict__ items) {
   typedef typename cpx<R>::t C;
+  if (items) {
+    const SpecItem& it = items[blockIdx.y];
+    spec = (C*)it.spec; ga.C_ref = it.C_ref; ga.aim = it.aim; ga.div_part = it.div_part;
+  }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int per = TI * g.N2;                       // lines x length per component
   C* a = reinterpret_cast<C*>(smem_raw);
@@ -312,7 +321,9 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
   }
 }
 
-__global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt, int N0, double* out) {
+__global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt, int N0, double* out,
+                             const SpecItem* __restrict__ items) {
+  if (items) { part = items[blockIdx.x].div_part; out = items[blockIdx.x].rms; }
   double s = 0.0;
   for (int b = threadIdx.x; b < nb; b += 32) s += part[b];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -411,12 +422,19 @@ SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize) {
   return L;
 }
 
+// The dynamic shared-memory limit is a property of the kernel, shared by every
+// RVE: raise it to the largest request seen so far (never lower it, or an RVE
+// created earlier with a larger grid could no longer launch).
 template <typename R>
 static void set_smem_limits(const SpecLaunch& L) {
-  cudaFuncSetAttribute(k_zpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smz);
-  cudaFuncSetAttribute(k_ypass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smy);
-  cudaFuncSetAttribute(k_xfwd<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smx);
-  cudaFuncSetAttribute(k_xinv<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smx);
+  static size_t mx = 0, my = 0, mz = 0;
+  if (L.smz > mz) { mz = L.smz; cudaFuncSetAttribute(k_zpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mz); }
+  if (L.smy > my) { my = L.smy; cudaFuncSetAttribute(k_ypass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)my); }
+  if (L.smx > mx) {
+    mx = L.smx;
+    cudaFuncSetAttribute(k_xfwd<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
+    cudaFuncSetAttribute(k_xinv<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
+  }
 }
 
 void spec_prepare(const SpecLaunch& L, bool fp32) {
@@ -424,38 +442,42 @@ void spec_prepare(const SpecLaunch& L, bool fp32) {
   else set_smem_limits<double>(L);
 }
 
-// forward transform (x, y passes) of 9 real planes into the spectrum buffer
+// full convolution of 9 real planes: forward x, y, z passes, div-RMS partials and
+// Gamma in the z pass, inverse y and x passes.  items == null: one RVE (in, field,
+// spec, ga as given); otherwise nitems RVEs of the same grid, one per blockIdx.y.
 template <typename R>
-static void fwd_xy(const SpecLaunch& L, const AxisPlan& px, const AxisPlan& py, const double* field, long long ld,
-                   void* spec, cudaStream_t st) {
+static void convolve_impl(const SpecLaunch& L, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                          const double* in, double* field, long long ld, void* spec, const GammaArgs& ga,
+                          const SpecItem* items, int nitems, cudaStream_t st) {
   typedef typename cpx<R>::t C;
-  k_xfwd<R, double><<<L.nbx, 256, L.smx, st>>>(L.g, px, field, ld, (C*)spec, L.LX);
-  k_ypass<R><<<L.nby, 256, L.smy, st>>>(L.g, py, (C*)spec, L.TIy, -1);
-}
-
-// full convolution: in (9 planes, ld) -> Gamma * in written to field; div RMS
-// partials into ga.div_part (nbz blocks)
-void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
-                   const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st) {
-  if (fp32) {
-    fwd_xy<float>(L, px, py, in, ld, spec, st);
-    k_zpass<float><<<L.nbz, 256, L.smz, st>>>(L.g, pz, (float2*)spec, L.TIz, ga);
-    if (ga.do_gamma) {
-      k_ypass<float><<<L.nby, 256, L.smy, st>>>(L.g, py, (float2*)spec, L.TIy, +1);
-      k_xinv<float, double><<<L.nbx, 256, L.smx, st>>>(L.g, px, (const float2*)spec, field, ld, L.LX);
-    }
-  } else {
-    fwd_xy<double>(L, px, py, in, ld, spec, st);
-    k_zpass<double><<<L.nbz, 256, L.smz, st>>>(L.g, pz, (double2*)spec, L.TIz, ga);
-    if (ga.do_gamma) {
-      k_ypass<double><<<L.nby, 256, L.smy, st>>>(L.g, py, (double2*)spec, L.TIy, +1);
-      k_xinv<double, double><<<L.nbx, 256, L.smx, st>>>(L.g, px, (const double2*)spec, field, ld, L.LX);
-    }
+  const unsigned ny = items ? (unsigned)nitems : 1u;
+  k_xfwd<R, double><<<dim3(L.nbx, ny), 256, L.smx, st>>>(L.g, px, in, ld, (C*)spec, L.LX, items);
+  k_ypass<R><<<dim3(L.nby, ny), 256, L.smy, st>>>(L.g, py, (C*)spec, L.TIy, -1, items);
+  k_zpass<R><<<dim3(L.nbz, ny), 256, L.smz, st>>>(L.g, pz, (C*)spec, L.TIz, ga, items);
+  if (ga.do_gamma) {
+    k_ypass<R><<<dim3(L.nby, ny), 256, L.smy, st>>>(L.g, py, (C*)spec, L.TIy, +1, items);
+    k_xinv<R, double><<<dim3(L.nbx, ny), 256, L.smx, st>>>(L.g, px, (const C*)spec, field, ld, L.LX, items);
   }
 }
 
+void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                   const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st) {
+  if (fp32) convolve_impl<float>(L, px, py, pz, in, field, ld, spec, ga, nullptr, 1, st);
+  else convolve_impl<double>(L, px, py, pz, in, field, ld, spec, ga, nullptr, 1, st);
+}
+
+void spec_convolve_batch(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                         const SpecItem* items, int nitems, const GammaArgs& ga, cudaStream_t st) {
+  if (fp32) convolve_impl<float>(L, px, py, pz, nullptr, nullptr, L.g.N, nullptr, ga, items, nitems, st);
+  else convolve_impl<double>(L, px, py, pz, nullptr, nullptr, L.g.N, nullptr, ga, items, nitems, st);
+}
+
+void spec_div_finish_batch(const SpecItem* items, int nitems, int nb, double wgt, int N0, cudaStream_t st) {
+  k_div_finish<<<nitems, 32, 0, st>>>(nullptr, nb, wgt, N0, nullptr, items);
+}
+
 void spec_div_finish(const double* part, int nb, double wgt, int N0, double* out, cudaStream_t st) {
-  k_div_finish<<<1, 32, 0, st>>>(part, nb, wgt, N0, out);
+  k_div_finish<<<1, 32, 0, st>>>(part, nb, wgt, N0, out, nullptr);
 }
 
 }  // namespace dgx

@@ -45,6 +45,17 @@ struct GammaArgs {
   double* div_part;       // per block partial of the divergence sum (FP64)
 };
 
+// one RVE of a size-grouped batched convolution (selected by blockIdx.y)
+struct SpecItem {
+  const double* in;       // 9 real planes, ld = N
+  double* out;            // 9 real planes, ld = N (Gamma * in)
+  void* spec;             // 9 Nh complex (FP64 or FP32)
+  const double* C_ref;    // 81
+  const double* aim;      // 9, zero-frequency value
+  double* div_part;       // nbz partials of the divergence sum
+  double* rms;            // divergence RMS out
+};
+
 // cos/sin of 2 pi j / n with the argument reduced to the first octant
 void twiddle(long j, long n, double* c, double* s);
 // radix factorisation (4, 2, then odd primes <= 16); number of stages or -1
@@ -55,6 +66,10 @@ SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize);
 void spec_prepare(const SpecLaunch& L, bool fp32);
 void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                    const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st);
+// nitems RVEs of the same grid (and precision) in one launch per pass; items in device memory
+void spec_convolve_batch(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                         const SpecItem* items, int nitems, const GammaArgs& ga, cudaStream_t st);
+void spec_div_finish_batch(const SpecItem* items, int nitems, int nb, double wgt, int N0, cudaStream_t st);
 void spec_div_finish(const double* part, int nb, double wgt, int N0, double* out, cudaStream_t st);
 
 }  // namespace dgx

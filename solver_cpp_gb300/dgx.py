@@ -52,7 +52,9 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_commit_increment", "dgx_divergence_rms", "dgx_gamma_convolution", "dgx_update_gamma",
            "dgx_fft_forward", "dgx_solver_init", "dgx_solver_forward", "dgx_solver_solve", "dgx_run_loadcase",
            "dgx_run_increment", "dgx_get", "dgx_counters", "dgx_timers", "dgx_rve_stream",
-           "dgx_measure_fp64_peak", "dgx_divergence_rms_static"]
+           "dgx_measure_fp64_peak", "dgx_divergence_rms_static", "dgx_batch_create", "dgx_batch_destroy",
+           "dgx_batch_add", "dgx_batch_step", "dgx_batch_run", "dgx_batch_member", "dgx_batch_remove",
+           "dgx_batch_stats", "dgx_batch_stream"]
 
 
 class DgxError(RuntimeError):
@@ -99,11 +101,23 @@ def lib():
     L.dgx_rve_stream.argtypes = [vp]
     L.dgx_rve_stream.restype = vp
     L.dgx_measure_fp64_peak.argtypes = [dp, dp]
+    L.dgx_batch_create.argtypes = [C.c_int32, C.c_int32, C.POINTER(vp)]
+    L.dgx_batch_destroy.argtypes = [vp]
+    L.dgx_batch_destroy.restype = None
+    L.dgx_batch_add.argtypes = [vp, vp, C.c_int32, C.POINTER(LoadStep), C.POINTER(IncRecord), C.c_int32, ip]
+    L.dgx_batch_step.argtypes = [vp, ip]
+    L.dgx_batch_run.argtypes = [vp]
+    L.dgx_batch_member.argtypes = [vp, C.c_int32, ip, ip, ip]
+    L.dgx_batch_remove.argtypes = [vp, C.c_int32]
+    L.dgx_batch_stats.argtypes = [vp, dp, C.POINTER(C.c_int64)]
+    L.dgx_batch_stream.argtypes = [vp]
+    L.dgx_batch_stream.restype = vp
     L.dgx_divergence_rms_static.argtypes = [ip, dp, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
     for name in SYMBOLS:
         f = getattr(L, name)
         if name not in ("dgx_material_default", "dgx_numerics_default", "dgx_rve_destroy", "dgx_last_error",
-                        "dgx_rve_points", "dgx_rve_device_bytes", "dgx_rve_stream"):
+                        "dgx_rve_points", "dgx_rve_device_bytes", "dgx_rve_stream", "dgx_batch_destroy",
+                        "dgx_batch_stream"):
             f.restype = C.c_int32
     _lib = L
     return L
