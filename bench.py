@@ -61,6 +61,12 @@ def args_():
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--no-extras", action="store_true", help="skip e2e / mixed / CPU-baseline legs")
     p.add_argument("--cpu-sample-increments", type=int, default=1)
+    p.add_argument("--batch-rves", type=int, default=256, help="RVEs of the batched leg (0: skip)")
+    p.add_argument("--batch-seconds", type=float, default=20.0, help="time bound of the batched leg")
+    p.add_argument("--batch-compare", type=int, default=24, help="RVEs of the batched-vs-plain comparison")
+    p.add_argument("--serve-requests", type=int, default=12, help="requests of each serving leg (0: skip)")
+    p.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate (requests/s)")
+    p.add_argument("--serve-seconds", type=float, default=45.0, help="time bound of each serving leg")
     return p.parse_args()
 
 
@@ -172,6 +178,159 @@ class Clocks:
 
 
 # ---------------------------------------------------------------- GPU arm
+BATCH_SIZES = (8, 16, 32, 48)
+BATCH_KINDS = ("tensionX", "tensionY", "tensionZ", "shearXY")
+
+
+def batch_population(count, seed=1000):
+    """RVEs of the batched configuration: grid uniform in {8,16,32,48}^3, 8-200
+    grains, load case uniform in tension x/y/z and shear xy (1e-3/s), per-RVE seeds."""
+    import numpy as np
+    from solver_cpp_gb300 import synthetic
+    out = []
+    for k in range(count):
+        rng = np.random.default_rng(seed + k)
+        c = int(BATCH_SIZES[rng.integers(len(BATCH_SIZES))])
+        ng = int(rng.integers(8, 201))
+        kind = BATCH_KINDS[rng.integers(len(BATCH_KINDS))]
+        mat, q = synthetic.microstructure((c, c, c), ng, seed + k)
+        out.append(((c, c, c), ng, kind, mat, q))
+    return out
+
+
+def batch_leg(g, torch, n_rves, increments, seconds, compare):
+    """Batched mixed-precision throughput on the batched configuration, and on a
+    subset the same RVEs solved one at a time in plain FP64 (throughput, P_av error)."""
+    pop = batch_population(n_rves)
+    mixed = g.numerics(precision="mixed")
+    steps = {k: [g.load_step(k, t=float(increments), N=increments)] for k in BATCH_KINDS}
+    batch = g.Batch(n_rves, cons_block=256)
+    rves = []
+    for cells, ng, kind, mat, q in pop:
+        r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=mixed)
+        rves.append((r, batch.add(r, steps[kind]), kind))
+    st = torch.cuda.ExternalStream(batch.stream)
+    s0 = batch.stats()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    t_start = time.perf_counter()
+    active = 1
+    while active and time.perf_counter() - t_start < seconds:
+        active = batch.step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    s1 = batch.stats()
+    pts = s1["point_evaluations"] - s0["point_evaluations"]
+    out = {"value": pts / (ms * 1e-3), "unit": UNIT, "rves": n_rves,
+           "points": int(sum(r.N for r, _, _ in rves)), "rounds": s1["rounds"] - s0["rounds"],
+           "seconds": ms * 1e-3, "all_done": not active,
+           "constitutive_share": (s1["constitutive_ms"] - s0["constitutive_ms"]) / ms,
+           "spectral_share": (s1["spectral_ms"] - s0["spectral_ms"]) / ms,
+           "launches": s1["launches"] - s0["launches"]}
+    batch.close()
+    for r, _, _ in rves:
+        r.close()
+    if compare:
+        # the first `compare` RVEs: batched mixed vs one-at-a-time plain FP64, `inc` increments each
+        inc = 2
+        sub = pop[:compare]
+        plain = g.numerics(precision="fp64")
+        steps2 = {k: [g.load_step(k, t=float(increments), N=increments)] for k in BATCH_KINDS}
+        ref_recs, t_seq, pts_seq = [], 0.0, 0
+        for cells, ng, kind, mat, q in sub:
+            r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=plain)
+            r.init()
+            c0 = r.counters()
+            torch.cuda.synchronize(); t0 = time.perf_counter()
+            recs = [r.run_increment(steps2[kind][0], 0, i) for i in range(inc)]
+            torch.cuda.synchronize(); t_seq += time.perf_counter() - t0
+            pts_seq += r.N * (r.counters()["evaluations"] - c0["evaluations"])
+            ref_recs.append(recs)
+            r.close()
+        # same dt (1 s) as the population's load case, `inc` increments
+        steps3 = {k: [g.load_step(k, t=float(inc), N=inc)] for k in BATCH_KINDS}
+        b2 = g.Batch(len(sub), cons_block=256)
+        members = []
+        for cells, ng, kind, mat, q in sub:
+            r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=mixed)
+            members.append((r, b2.add(r, steps3[kind])))
+        s0 = b2.stats()
+        torch.cuda.synchronize(); t0 = time.perf_counter()
+        b2.run()
+        torch.cuda.synchronize(); t_b = time.perf_counter() - t0
+        pts_b = b2.stats()["point_evaluations"] - s0["point_evaluations"]
+        err = 0.0
+        for (r, slot), rr in zip(members, ref_recs):
+            for a_, b_ in zip(b2.records(slot), rr):
+                err = max(err, float(abs(a_["P_av"] - b_["P_av"]).max() / abs(b_["P_av"]).max()))
+        b2.close()
+        for r, _ in members:
+            r.close()
+        out["vs_plain_fp64_sequential"] = {
+            "rves": compare, "increments": inc, "plain_fp64_one_at_a_time": pts_seq / t_seq,
+            "batched_mixed": pts_b / t_b, "speedup": (pts_b / t_b) / (pts_seq / t_seq),
+            "max_rel_P_av_error_vs_fp64": err, "timing": "host wall clock, both sides"}
+    return out
+
+
+SERVE_SIZES = (16, 32, 64, 96)
+
+
+def serve_leg(g, precision, rate, n_requests, seconds, seed=5000):
+    """Poisson arrivals (rate req/s) of RVE solve requests: grid uniform in
+    {16,32,64,96}^3, 10-500 grains, load case uniform in tension x/y/z and shear xy
+    (1e-3/s), 10-40 increments.  Requests are submitted at their arrival times from
+    this thread while the server's worker runs; reports per-increment and
+    per-request latency and the aggregate point-updates/s of the window."""
+    import numpy as np
+    from solver_cpp_gb300 import synthetic
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n_requests)
+    reqs = []
+    for k in range(n_requests):
+        c = int(SERVE_SIZES[rng.integers(len(SERVE_SIZES))])
+        ng = int(rng.integers(10, 501))
+        kind = BATCH_KINDS[rng.integers(len(BATCH_KINDS))]
+        n_inc = int(rng.integers(10, 41))
+        mat, q = synthetic.microstructure((c, c, c), ng, seed + k)
+        reqs.append(((c, c, c), mat, q, [g.load_step(kind, t=float(n_inc), N=n_inc)]))
+    num = g.numerics(precision=precision)
+    srv = g.Server(max_active=64, cons_block=256)
+    ids, t0 = [], time.perf_counter()
+    due = t0
+    for gap, (cells, mat, q, steps) in zip(gaps, reqs):
+        due += gap
+        d = due - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        ids.append(srv.submit(cells, (1.0, 1.0, 1.0), mat, q, steps, num=num))
+    deadline = t0 + seconds
+    done, inc_lat, req_lat, evals = [], [], [], 0
+    for rid, (cells, _, _, _) in zip(ids, reqs):
+        st = srv.status(rid, wait=max(0.0, deadline - time.perf_counter()), max_records=64)
+        if st["state"] != "done":
+            continue
+        done.append(rid)
+        req_lat.append(st["t_done"] - st["t_submit"])
+        for r in st["records"]:
+            inc_lat.append(r["seconds"])
+            evals += r["evaluations"] * cells[0] * cells[1] * cells[2]
+    window = time.perf_counter() - t0
+    info = srv.stats()
+    srv.close()
+
+    def pct(v, p):
+        return float(np.percentile(v, p)) if v else None
+    return {"precision": precision, "rate_req_per_s": rate, "requests": n_requests, "completed": len(done),
+            "window_s": window, "value": evals / window, "unit": UNIT,
+            "p50_increment_ms": 1e3 * pct(inc_lat, 50) if inc_lat else None,
+            "p99_increment_ms": 1e3 * pct(inc_lat, 99) if inc_lat else None,
+            "p50_request_s": pct(req_lat, 50), "p99_request_s": pct(req_lat, 99), "rounds": info["rounds"],
+            "note": "value counts the completed requests' point-updates over the whole window (wall clock)"}
+
+
 def run_increments(rve, step, start, count, n_inc, read_back=False):
     """Run `count` increments starting at global index `start` (load case cycled)."""
     lat = []
@@ -289,6 +448,11 @@ def gpu_arm(a):
             line["mixed"] = {"value": n * evm / tm, "unit": UNIT, "increments": m_inc,
                              "max_rel_P_av_error_vs_fp64": max(errs), "per_increment_error": errs}
             ref.close(); mix.close()
+        if a.batch_rves > 0:
+            line["batched"] = batch_leg(g, torch, a.batch_rves, 20, a.batch_seconds, a.batch_compare)
+        if a.serve_requests > 0:
+            line["serving"] = [serve_leg(g, p, a.serve_rate, a.serve_requests, a.serve_seconds)
+                               for p in ("fp64", "mixed")]
         if rank == 0:
             threads = os.cpu_count() or 1
             try:

@@ -89,6 +89,9 @@ dgx_status dgx_rve_create(const int32_t cells[3], const double size[3], const in
                           const dgx_numerics* num, dgx_rve** out);
 void dgx_rve_destroy(dgx_rve* rve);
 const char* dgx_last_error(void);
+/* Device bytes dgx_rve_create would allocate for this grid and numerics (admission
+ * control).  No reference counterpart. */
+dgx_status dgx_rve_footprint(const int32_t cells[3], const dgx_numerics* num, int32_t n_materials, int64_t* bytes);
 int64_t dgx_rve_points(const dgx_rve* rve);
 /* device bytes held by the RVE (fields, state, NGMRES history, scratch) */
 int64_t dgx_rve_device_bytes(const dgx_rve* rve);
@@ -199,6 +202,51 @@ dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
  * [7] d2h bytes of the executor. */
 dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[8]);
 void* dgx_batch_stream(const dgx_batch* batch);
+
+/* ---- Serving (no counterpart in the reference).  A server owns one worker thread, the
+ * device and a dgx_batch.  Requests from any thread are queued; in arrival order a
+ * request is admitted when a batch slot is free and its device footprint
+ * (dgx_rve_footprint) fits the HBM budget beside the resident requests; its RVE is
+ * created and joins the batch between two rounds, runs its load case with its state
+ * resident on the device, and leaves (memory freed) when done.  Results equal those
+ * of the same solve run alone. */
+typedef struct dgx_server dgx_server;
+typedef struct {
+  int32_t cells[3];
+  double size[3];
+  const int32_t* material_at;      /* N0*N1*N2 0-based material indices (copied at submit) */
+  int32_t n_materials;
+  const double* orientations;      /* 4 per material, w,x,y,z (copied) */
+  dgx_material material;
+  dgx_numerics numerics;
+  int32_t nsteps;
+  const dgx_loadstep* steps;       /* copied */
+} dgx_request;
+typedef struct {
+  int32_t state;                   /* 0 queued, 1 running, 2 done, 3 failed */
+  int32_t status;                  /* dgx_status of the solve */
+  int32_t n_records;               /* increments recorded */
+  double t_submit, t_admit, t_done;   /* seconds since the server started */
+  int64_t device_bytes, points;
+  char error[160];
+} dgx_request_status;
+typedef struct {
+  int32_t queued, running;
+  int64_t completed, failed, rounds, budget_bytes, used_bytes;
+  double now;                      /* seconds since the server started */
+  int32_t status;                  /* DGX_OK unless a device error stopped the service */
+} dgx_server_info;
+/* hbm_budget_bytes <= 0: 85 % of the free device memory at creation */
+dgx_status dgx_server_create(int64_t hbm_budget_bytes, int32_t max_active, int32_t cons_block, dgx_server** out);
+/* stops the worker; queued and running requests end as failed ("server stopped") */
+void dgx_server_destroy(dgx_server* server);
+dgx_status dgx_server_submit(dgx_server* server, const dgx_request* request, int64_t* id);
+/* status (waiting up to wait_s seconds for completion); records copied once done */
+dgx_status dgx_server_poll(dgx_server* server, int64_t id, double wait_s, dgx_request_status* status,
+                           dgx_inc_record* records, int32_t max_records);
+/* forget a finished request */
+dgx_status dgx_server_release(dgx_server* server, int64_t id);
+dgx_status dgx_server_stats(dgx_server* server, dgx_server_info* info);
 
 /* FP64 FMA throughput of the current device (TFLOP/s, best of 5), the
  * denominator of the constitutive kernel's roofline.  No reference counterpart. */

@@ -16,7 +16,7 @@ from . import dgx as _d
 from .dgx import DgxError  # noqa: F401
 from .loadcase import load_step, parse_load_yaml, parse_numerics_yaml  # noqa: F401
 
-__all__ = ["RVE", "Batch", "material", "numerics", "load_step", "DgxError"]
+__all__ = ["RVE", "Batch", "Server", "footprint", "material", "numerics", "load_step", "DgxError"]
 
 
 def material(**kw):
@@ -274,3 +274,87 @@ class Batch:
     @property
     def stream(self):
         return int(_d.lib().dgx_batch_stream(self.h) or 0)
+
+
+def footprint(cells, num=None, n_materials=1):
+    """Device bytes an RVE of this grid and numerics holds (dgx_rve_footprint)."""
+    b = C.c_int64(0)
+    num = num if num is not None else numerics()
+    _d.check(_d.lib().dgx_rve_footprint((C.c_int32 * 3)(*[int(c) for c in cells]), C.byref(num), int(n_materials),
+                                        C.byref(b)), "dgx_rve_footprint")
+    return int(b.value)
+
+
+class Server:
+    """Continuous-batching service of RVE solves (dgx_server_*).
+
+    ``submit`` queues a solve (inputs are copied) and returns its id; the worker
+    thread admits requests in arrival order as batch slots and HBM budget free up,
+    runs them together and frees each one's memory when it is done.  ``result``
+    waits for a request and returns its status and per-increment records.
+    """
+
+    STATES = ("queued", "running", "done", "failed")
+
+    def __init__(self, hbm_budget_bytes=0, max_active=64, cons_block=128):
+        h = C.c_void_p()
+        _d.check(_d.lib().dgx_server_create(int(hbm_budget_bytes), int(max_active), int(cons_block), C.byref(h)),
+                 "dgx_server_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            _d.lib().dgx_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, cells, size, material_at, orientations, steps, mat=None, num=None):
+        ma = np.ascontiguousarray(np.asarray(material_at, dtype=np.int32).ravel())
+        q = np.ascontiguousarray(np.asarray(orientations, dtype=np.float64).reshape(-1, 4))
+        arr = (_d.LoadStep * len(steps))(*steps)
+        req = _d.Request()
+        for i in range(3):
+            req.cells[i] = int(cells[i]); req.size[i] = float(size[i])
+        req.material_at = ma.ctypes.data_as(C.POINTER(C.c_int32))
+        req.n_materials = q.shape[0]
+        req.orientations = _d.dptr(q)
+        req.material = mat if mat is not None else material()
+        req.numerics = num if num is not None else numerics()
+        req.nsteps = len(steps)
+        req.steps = arr
+        rid = C.c_int64(0)
+        _d.check(_d.lib().dgx_server_submit(self.h, C.byref(req), C.byref(rid)), "dgx_server_submit")
+        return int(rid.value)
+
+    def status(self, rid, wait=0.0, max_records=0):
+        st = _d.RequestStatus()
+        recs = (_d.IncRecord * max(1, max_records))()
+        _d.check(_d.lib().dgx_server_poll(self.h, int(rid), float(wait), C.byref(st), recs, int(max_records)),
+                 "dgx_server_poll")
+        out = dict(state=self.STATES[st.state], status=st.status, n_records=st.n_records, t_submit=st.t_submit,
+                   t_admit=st.t_admit, t_done=st.t_done, device_bytes=st.device_bytes, points=st.points,
+                   error=st.error.decode(errors="replace"))
+        if max_records and st.state == 2:
+            out["records"] = [_record(r) for r in recs[:min(st.n_records, max_records)]]
+        return out
+
+    def result(self, rid, timeout=3600.0, max_records=100000):
+        """Wait for the request; its status with the records."""
+        st = self.status(rid, wait=timeout, max_records=max_records)
+        if st["state"] not in ("done", "failed"):
+            raise TimeoutError(f"request {rid} not finished after {timeout} s")
+        return st
+
+    def release(self, rid):
+        _d.check(_d.lib().dgx_server_release(self.h, int(rid)), "dgx_server_release")
+
+    def stats(self):
+        i = _d.ServerInfo()
+        _d.check(_d.lib().dgx_server_stats(self.h, C.byref(i)), "dgx_server_stats")
+        return dict(queued=i.queued, running=i.running, completed=i.completed, failed=i.failed, rounds=i.rounds,
+                    budget_bytes=i.budget_bytes, used_bytes=i.used_bytes, now=i.now, status=i.status)

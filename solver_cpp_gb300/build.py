@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdgx.so")
 SOURCES = ["constitutive.cu", "spectral.cu", "solver.cu", "peak.cu", "noalloc.cu", "batch.cu"]
-HOST_SOURCES = ["ref_stiffness.cpp"]
+HOST_SOURCES = ["ref_stiffness.cpp", "server.cpp"]
 HEADERS = ["dgx_internal.cuh", "spectral.cuh", "rve.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -40,7 +40,9 @@ def _flags(verbose_ptxas=False):
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     if src.endswith(".cpp"):
-        cmd = ["g++", "-c", os.path.join(CSRC, src), "-o", obj, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
+        cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+        cmd = ["g++", "-c", os.path.join(CSRC, src), "-o", obj, "-O2", "-std=c++17", "-fPIC", "-pthread",
+               "-ffp-contract=off", "-I", cuda_inc]
     else:
         cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + _flags(verbose_ptxas)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -64,7 +66,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
             sys.stderr.write(log)
     objs = [o for o, _ in results]
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

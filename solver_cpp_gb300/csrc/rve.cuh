@@ -72,6 +72,7 @@ struct dgx_rve {
   dgx::Executor* ex = nullptr;
   cudaStream_t home_st = nullptr;
   int in_batch = 0;
+  bool dry = false;           // size-only pass of the buffer allocation (footprint)
 };
 
 namespace dgx {

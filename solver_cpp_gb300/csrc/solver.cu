@@ -390,6 +390,7 @@ namespace dgx {
 
 template <typename T>
 dgx_status dalloc(dgx_rve* r, T** p, size_t count) {
+  if (r->dry) { r->bytes += (int64_t)(count * sizeof(T)); *p = nullptr; return DGX_OK; }
   void* v = nullptr;
   cudaError_t e = cudaMalloc(&v, std::max<size_t>(count, 1) * sizeof(T));
   if (e != cudaSuccess) { set_err("cudaMalloc(%zu): %s", count * sizeof(T), cudaGetErrorString(e)); return DGX_ERR_NOMEM; }
@@ -607,6 +608,49 @@ extern "C" void dgx_rve_destroy(dgx_rve* r) {
   delete r;
 }
 
+// Every device buffer of an RVE.  With r->dry set nothing is allocated and r->bytes
+// only adds up the sizes: the footprint used for admission control.
+static dgx_status allocate_buffers(dgx_rve* r, const int32_t cells[3], const dgx_numerics* num, int n_materials) {
+  const int64_t N = r->N;
+  dgx_status s = DGX_OK;
+#define AL(p, c) do { s = dalloc(r, p, c); if (s != DGX_OK) return s; } while (0)
+  r->ps.n = N; r->ps.ld = N;
+  AL(&r->ps.F, 9 * N); AL(&r->ps.F0, 9 * N); AL(&r->ps.Fp0, 9 * N); AL(&r->ps.Lp0, 9 * N); AL(&r->ps.S0, 9 * N);
+  AL(&r->ps.st0, 24 * N); AL(&r->ps.Fp, 9 * N); AL(&r->ps.Lp, 9 * N); AL(&r->ps.S, 9 * N); AL(&r->ps.Fe, 9 * N);
+  AL(&r->ps.st, 24 * N); AL(&r->ps.P, 9 * N); AL(&r->ps.status, N);
+  AL(&r->X, 9 * N); AL(&r->R, 9 * N); AL(&r->XM, 9 * N); AL(&r->FM, 9 * N); AL(&r->XA, 9 * N); AL(&r->FA, 9 * N);
+  AL(&r->F_last_inc, 9 * N); AL(&r->F_dot, 9 * N);
+  int m = num->solver == 0 ? num->ngmres_m : 0;
+  r->Xdot.resize(m); r->Fdot.resize(m);
+  for (int i = 0; i < m; ++i) { AL(&r->Xdot[i], 9 * N); AL(&r->Fdot[i], 9 * N); }
+  bool fp32 = num->precision == 1;
+  r->sl = spec_launch(cells[0], cells[1], cells[2], fp32 ? sizeof(float2) : sizeof(double2));
+  {
+    double* sp = nullptr;
+    AL(&sp, (fp32 ? 1 : 2) * 9 * r->sl.g.Nh);
+    r->spec = sp;
+  }
+  r->nb_cons = (int)((N + 63) / 64);            // P_av partials: one per 64 cells
+  {
+    const char* env = std::getenv("DGX_CONS_BLOCK");
+    int b = env ? std::atoi(env) : 128;
+    r->cons_block = (b == 64 || b == 256) ? b : 128;
+  }
+  r->nb_tan = (int)((N + 63) / 64);
+  r->nb_red = (int)std::min<int64_t>(608, std::max<int64_t>(1, (9 * N + 1023) / 1024));
+  AL(&r->d_Ppart, 9 * (int64_t)r->nb_cons);
+  AL(&r->d_tpart, r->nb_tan);
+  AL(&r->d_divpart, r->sl.nbz);
+  AL(&r->d_redpart, 128 * (int64_t)r->nb_red);   // two concurrent fused reductions of up to 64 sums
+  AL(&r->d_redout, 128); AL(&r->d_beta, 32);
+  AL(&r->d_Pav, 9); AL(&r->d_Cvol, 81); AL(&r->d_Cmm, 81); AL(&r->d_Cref, 81); AL(&r->d_aim, 9); AL(&r->d_rms, 1);
+  AL(&r->d_ill, 1); AL(&r->d_cnt, 1);
+  AL(&r->d_xi_x, cells[0] / 2 + 1); AL(&r->d_xi_y, cells[1]); AL(&r->d_xi_z, cells[2]);
+  AL(&r->d_mat, N); AL(&r->d_Rm, 9 * (int64_t)n_materials);
+#undef AL
+  return DGX_OK;
+}
+
 extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3], const int32_t* material_at,
                                      int32_t n_materials, const double* orientations, const dgx_material* mat,
                                      const dgx_numerics* num, dgx_rve** out) {
@@ -648,43 +692,10 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
   if (ce != cudaSuccess) { set_err("cudaStreamCreate: %s", cudaGetErrorString(ce)); delete r; return DGX_ERR_CUDA; }
   r->owns_stream = true;
   for (int i = 0; i < 6; ++i) cudaEventCreate(&r->ev[i]);
+  dgx_status s = allocate_buffers(r, cells, num, n_materials);
+  if (s != DGX_OK) { dgx_rve_destroy(r); return s; }
   const int64_t N = r->N;
-  dgx_status s = DGX_OK;
-#define AL(p, c) do { s = dalloc(r, p, c); if (s != DGX_OK) { dgx_rve_destroy(r); return s; } } while (0)
-  r->ps.n = N; r->ps.ld = N;
-  AL(&r->ps.F, 9 * N); AL(&r->ps.F0, 9 * N); AL(&r->ps.Fp0, 9 * N); AL(&r->ps.Lp0, 9 * N); AL(&r->ps.S0, 9 * N);
-  AL(&r->ps.st0, 24 * N); AL(&r->ps.Fp, 9 * N); AL(&r->ps.Lp, 9 * N); AL(&r->ps.S, 9 * N); AL(&r->ps.Fe, 9 * N);
-  AL(&r->ps.st, 24 * N); AL(&r->ps.P, 9 * N); AL(&r->ps.status, N);
-  AL(&r->X, 9 * N); AL(&r->R, 9 * N); AL(&r->XM, 9 * N); AL(&r->FM, 9 * N); AL(&r->XA, 9 * N); AL(&r->FA, 9 * N);
-  AL(&r->F_last_inc, 9 * N); AL(&r->F_dot, 9 * N);
-  int m = num->solver == 0 ? num->ngmres_m : 0;
-  r->Xdot.resize(m); r->Fdot.resize(m);
-  for (int i = 0; i < m; ++i) { AL(&r->Xdot[i], 9 * N); AL(&r->Fdot[i], 9 * N); }
   bool fp32 = num->precision == 1;
-  r->sl = spec_launch(cells[0], cells[1], cells[2], fp32 ? sizeof(float2) : sizeof(double2));
-  {
-    double* sp = nullptr;
-    AL(&sp, (fp32 ? 1 : 2) * 9 * r->sl.g.Nh);
-    r->spec = sp;
-  }
-  r->nb_cons = (int)((N + 63) / 64);            // P_av partials: one per 64 cells
-  {
-    const char* env = std::getenv("DGX_CONS_BLOCK");
-    int b = env ? std::atoi(env) : 128;
-    r->cons_block = (b == 64 || b == 256) ? b : 128;
-  }
-  r->nb_tan = (int)((N + 63) / 64);
-  r->nb_red = (int)std::min<int64_t>(608, std::max<int64_t>(1, (9 * N + 1023) / 1024));
-  AL(&r->d_Ppart, 9 * (int64_t)r->nb_cons);
-  AL(&r->d_tpart, r->nb_tan);
-  AL(&r->d_divpart, r->sl.nbz);
-  AL(&r->d_redpart, 128 * (int64_t)r->nb_red);   // two concurrent fused reductions of up to 64 sums
-  AL(&r->d_redout, 128); AL(&r->d_beta, 32);
-  AL(&r->d_Pav, 9); AL(&r->d_Cvol, 81); AL(&r->d_Cmm, 81); AL(&r->d_Cref, 81); AL(&r->d_aim, 9); AL(&r->d_rms, 1);
-  AL(&r->d_ill, 1); AL(&r->d_cnt, 1);
-  AL(&r->d_xi_x, cells[0] / 2 + 1); AL(&r->d_xi_y, cells[1]); AL(&r->d_xi_z, cells[2]);
-  AL(&r->d_mat, N); AL(&r->d_Rm, 9 * (int64_t)n_materials);
-#undef AL
   for (int i = 0; i < 3; ++i)
     if (!axis_create(&r->ax[i], cells[i])) { set_err("FFT plan for length %d failed", cells[i]); dgx_rve_destroy(r); return DGX_ERR_UNSUPPORTED; }
   spec_prepare(r->sl, fp32);
@@ -730,6 +741,18 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
   memset(r->S, 0, sizeof(r->S));
   r->rot_q[0] = 1; r->rot_q[1] = r->rot_q[2] = r->rot_q[3] = 0;
   *out = r;
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_rve_footprint(const int32_t cells[3], const dgx_numerics* num, int32_t n_materials,
+                                        int64_t* bytes) {
+  if (!cells || !num || !bytes || n_materials < 1) return DGX_ERR_ARG;
+  for (int i = 0; i < 3; ++i) if (cells[i] < 1 || cells[i] > 4096) return DGX_ERR_ARG;
+  dgx_rve r;
+  r.dry = true;
+  r.N = (int64_t)cells[0] * cells[1] * cells[2];
+  TRY(allocate_buffers(&r, cells, num, n_materials));
+  *bytes = r.bytes;
   return DGX_OK;
 }
 

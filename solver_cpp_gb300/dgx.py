@@ -47,6 +47,24 @@ class IncRecord(C.Structure):
                 ("err_BC", C.c_double), ("seconds", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("cells", C.c_int32 * 3), ("size", C.c_double * 3), ("material_at", C.POINTER(C.c_int32)),
+                ("n_materials", C.c_int32), ("orientations", C.POINTER(C.c_double)), ("material", Material),
+                ("numerics", Numerics), ("nsteps", C.c_int32), ("steps", C.POINTER(LoadStep))]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("n_records", C.c_int32), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("device_bytes", C.c_int64),
+                ("points", C.c_int64), ("error", C.c_char * 160)]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("queued", C.c_int32), ("running", C.c_int32), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("rounds", C.c_int64), ("budget_bytes", C.c_int64), ("used_bytes", C.c_int64), ("now", C.c_double),
+                ("status", C.c_int32)]
+
+
 SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dgx_rve_destroy", "dgx_last_error",
            "dgx_rve_points", "dgx_rve_device_bytes", "dgx_constitutive_response", "dgx_averages",
            "dgx_commit_increment", "dgx_divergence_rms", "dgx_gamma_convolution", "dgx_update_gamma",
@@ -54,7 +72,8 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_run_increment", "dgx_get", "dgx_counters", "dgx_timers", "dgx_rve_stream",
            "dgx_measure_fp64_peak", "dgx_divergence_rms_static", "dgx_batch_create", "dgx_batch_destroy",
            "dgx_batch_add", "dgx_batch_step", "dgx_batch_run", "dgx_batch_member", "dgx_batch_remove",
-           "dgx_batch_stats", "dgx_batch_stream"]
+           "dgx_batch_stats", "dgx_batch_stream", "dgx_rve_footprint", "dgx_server_create", "dgx_server_destroy",
+           "dgx_server_submit", "dgx_server_poll", "dgx_server_release", "dgx_server_stats"]
 
 
 class DgxError(RuntimeError):
@@ -112,12 +131,21 @@ def lib():
     L.dgx_batch_stats.argtypes = [vp, dp, C.POINTER(C.c_int64)]
     L.dgx_batch_stream.argtypes = [vp]
     L.dgx_batch_stream.restype = vp
+    L.dgx_rve_footprint.argtypes = [ip, C.POINTER(Numerics), C.c_int32, i64p]
+    L.dgx_server_create.argtypes = [C.c_int64, C.c_int32, C.c_int32, C.POINTER(vp)]
+    L.dgx_server_destroy.argtypes = [vp]
+    L.dgx_server_destroy.restype = None
+    L.dgx_server_submit.argtypes = [vp, C.POINTER(Request), i64p]
+    L.dgx_server_poll.argtypes = [vp, C.c_int64, C.c_double, C.POINTER(RequestStatus), C.POINTER(IncRecord),
+                                  C.c_int32]
+    L.dgx_server_release.argtypes = [vp, C.c_int64]
+    L.dgx_server_stats.argtypes = [vp, C.POINTER(ServerInfo)]
     L.dgx_divergence_rms_static.argtypes = [ip, dp, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
     for name in SYMBOLS:
         f = getattr(L, name)
         if name not in ("dgx_material_default", "dgx_numerics_default", "dgx_rve_destroy", "dgx_last_error",
                         "dgx_rve_points", "dgx_rve_device_bytes", "dgx_rve_stream", "dgx_batch_destroy",
-                        "dgx_batch_stream"):
+                        "dgx_batch_stream", "dgx_server_destroy"):
             f.restype = C.c_int32
     _lib = L
     return L
