@@ -146,10 +146,40 @@ dgx_status dgx_solver_solve(dgx_rve* rve, int32_t* converged, int32_t* iteration
  * solver init; records[k] per increment (up to max_records). */
 dgx_status dgx_run_loadcase(dgx_rve* rve, int32_t nsteps, const dgx_loadstep* steps,
                             dgx_inc_record* records, int32_t max_records, int32_t* n_records);
+/* dgx_run_loadcase with output: result (may be null) receives increment 0 and every
+ * f_out-th increment of each step (numbered by the increments completed so far); a
+ * restart file is written to restart_path every restart_every increments (0: never). */
+dgx_status dgx_run_loadcase_output(dgx_rve* rve, int32_t nsteps, const dgx_loadstep* steps,
+                                   dgx_inc_record* records, int32_t max_records, int32_t* n_records,
+                                   struct dgx_result* result, const char* restart_path, int32_t restart_every);
 /* incremental variant: dgx_solver_init once, then one increment per call
  * (state carried on the device between calls) */
 dgx_status dgx_run_increment(dgx_rve* rve, const dgx_loadstep* step, int32_t step_index, int32_t inc,
                              dgx_inc_record* record);
+
+/* MechSolverBasic::update_coords (mech_solver_basic.cpp:222-238, mech_base.cpp:45-154):
+ * displacements of the deformed grid from the current solution F, as written to the
+ * results: u_n (3 per node, (N0+1)(N1+1)(N2+1) nodes) and u_p (3 per cell), x fastest;
+ * either may be null. */
+dgx_status dgx_update_coords(dgx_rve* rve, double* u_n, double* u_p);
+
+/* ---- DADF5 results (f_materialpoint_result, damask_grid.h:18; result.f90:80-160).
+ * open: file with root / geometry / cell_to / setup groups for the RVE's grid;
+ * write_increment: group increment_<inc> (attribute t/s) with geometry/{u_n,u_p} and
+ * phase/<phase>/mechanical/{F,F_e,F_p,L_p,O,P,xi_sl}; close: writes the metadata (the
+ * file is valid after close).  phase / homogenization default to "phase" / "SX". */
+typedef struct dgx_result dgx_result;
+dgx_status dgx_result_open(const char* path, const dgx_rve* rve, const char* phase, const char* homogenization,
+                           dgx_result** out);
+/* an input file stored under /setup/<name> */
+dgx_status dgx_result_add_setup(dgx_result* res, const char* name, const char* content, int64_t length);
+dgx_status dgx_result_write_increment(dgx_result* res, dgx_rve* rve, int32_t inc, double t);
+dgx_status dgx_result_close(dgx_result* res);
+/* Restart (materialpoint.f90:163-202, phase_mechanical.f90:1264-1298): the RVE's
+ * complete state after an increment; read into an RVE created with the same inputs,
+ * the load case continues bitwise as if uninterrupted. */
+dgx_status dgx_restart_write(dgx_rve* rve, const char* path);
+dgx_status dgx_restart_read(dgx_rve* rve, const char* path);
 
 /* Copy a per-point field out in the reference layout.  name: "F", "P", "Fp", "Lp",
  * "Fe", "S" (9 per cell), "xi", "gamma" (12 per cell), "dPdF" (81 per cell, last

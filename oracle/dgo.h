@@ -95,6 +95,13 @@ enum { DGO_DIVCORR_NONE = 0, DGO_DIVCORR_SIZE = 1, DGO_DIVCORR_SIZE_GRID = 2 };
 
 /* xi1st, xi2nd: complex (3, N0r, N2, N1) */
 void dgo_xi(const int cells[3], const double geom[3], int derivative, double* xi1st, double* xi2nd);
+/* cell-centre (u_p, 3 per cell) and nodal (u_n, 3 per node) displacements of F */
+void dgo_update_coords(const int cells[3], const double geom[3], int derivative, const double* F,
+                       double* u_n, double* u_p);
+/* orientation output: rotational part of F (closed form), quaternion of R^T */
+void dgo_rotational_part(const double F[9], double R[9]);
+void dgo_om2qu(const double om[9], double qu[4]);
+void dgo_orientation_output(const double Fe[9], double qu[4]);
 void dgo_scaled_geom(const int cells[3], const double geom[3], int divcorr, double out[3]);
 double dgo_divergence_rms_spec(const int cells[3], const double geom[3], const double scaled[3],
                                const double* xi1st, const double* spec);

@@ -87,6 +87,10 @@ def lib():
         L.dgo_fft_c2r.argtypes = [ip, C.c_int, dp, dp]
         L.dgo_xi.argtypes = [ip, dp, C.c_int, dp, dp]
         L.dgo_scaled_geom.argtypes = [ip, dp, C.c_int, dp]
+        L.dgo_update_coords.argtypes = [ip, dp, C.c_int, dp, dp, dp]
+        L.dgo_rotational_part.argtypes = [dp, dp]
+        L.dgo_om2qu.argtypes = [dp, dp]
+        L.dgo_orientation_output.argtypes = [dp, dp]
         L.dgo_divergence_rms_spec.argtypes = [ip, dp, dp, dp, dp]
         L.dgo_divergence_rms_spec.restype = C.c_double
         L.dgo_divergence_rms.argtypes = [ip, dp, dp, dp, dp]
@@ -234,6 +238,25 @@ def xi(cells, geom, derivative=0):
     lib().dgo_xi(_cells(cells), _p(f64(geom)), int(derivative),
                  x1.ctypes.data_as(C.POINTER(C.c_double)), x2.ctypes.data_as(C.POINTER(C.c_double)))
     return x1, x2
+
+
+def update_coords(cells, geom, F9, derivative=0):
+    """(u_n (nodes, 3), u_p (cells, 3)) of the F field (N, 9 column-major)."""
+    N0, N1, N2 = cells
+    un = np.zeros(((N0 + 1) * (N1 + 1) * (N2 + 1), 3))
+    up = np.zeros((N0 * N1 * N2, 3))
+    F9 = np.ascontiguousarray(F9, dtype=np.float64)
+    lib().dgo_update_coords(_cells(cells), _p(f64(geom)), int(derivative), _p(F9), _p(un), _p(up))
+    return un, up
+
+
+def orientation_output(Fe9):
+    """Quaternions (N, 4) written as the crystal orientation O for elastic deformation gradients (N, 9)."""
+    Fe9 = np.ascontiguousarray(np.asarray(Fe9, dtype=np.float64).reshape(-1, 9))
+    out = np.zeros((Fe9.shape[0], 4))
+    for k in range(Fe9.shape[0]):
+        lib().dgo_orientation_output(_p(Fe9[k]), _p(out[k]))
+    return out
 
 
 def scaled_geom(cells, geom, divcorr):

@@ -221,3 +221,79 @@ void dgo_rotate4(const double q[4], const double T[81], double out[81], int acti
     out[i + 3 * j + 9 * k + 27 * l] = s;
   }
 }
+
+/* ------------------------------------------------------------------ orientation output
+ * Rotational part R of F (polar decomposition F = R U) in the closed form of the
+ * reference (src/math.f90:1117-1156, invariants of C = F^T F and of U, Hoger &
+ * Carlson 1984), then the crystal orientation written to the results:
+ * quaternion of R^T (src/phase.f90:590, rotations.f90:518-546: trace branch, w >= 0,
+ * P = -1 sign convention on the vector part, normalised). */
+static double clip(double x, double lo, double hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+void dgo_rotational_part(const double F[9], double R[9]) {
+  double C[9], FF[9];
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) {
+    double c = 0.0, f = 0.0;
+    for (int k = 0; k < 3; ++k) { c += F[k + 3 * i] * F[k + 3 * j]; f += F[i + 3 * k] * F[k + 3 * j]; }
+    C[i + 3 * j] = c; FF[i + 3 * j] = f;
+  }
+  double I1 = C[0] + C[4] + C[8];
+  double I2 = C[0] * C[4] + C[4] * C[8] + C[8] * C[0] - C[3] * C[3] - C[7] * C[7] - C[6] * C[6];
+  double I3 = C[0] * (C[4] * C[8] - C[7] * C[5]) - C[3] * (C[1] * C[8] - C[7] * C[2]) + C[6] * (C[1] * C[5] - C[4] * C[2]);
+  double trF = F[0] + F[4] + F[8], trFF = FF[0] + FF[4] + FF[8];
+  double IF1 = trF, IF2 = 0.5 * (trF * trF - trFF);
+  double x = pow(clip(I1 * I1 - 3.0 * I2, 0.0, INFINITY), 1.5);
+  double lam[3];
+  if (x != 0.0) {
+    double Phi = acos(clip((I1 * I1 * I1 - 4.5 * I1 * I2 + 13.5 * I3) / x, -1.0, 1.0));
+    for (int k = 0; k < 3; ++k) {
+      double l = I1 + (2.0 * sqrt(clip(I1 * I1 - 3.0 * I2, 0.0, INFINITY))) *
+                 cos((Phi - 6.283185307179586476925286766559 * (k + 1.0)) / 3.0);
+      lam[k] = sqrt(clip(l, 0.0, INFINITY) / 3.0);
+    }
+  } else {
+    for (int k = 0; k < 3; ++k) lam[k] = sqrt(I1 / 3.0);
+  }
+  double IU1 = lam[0] + lam[1] + lam[2];
+  double IU2 = lam[0] * lam[1] + lam[1] * lam[2] + lam[2] * lam[0];
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) {
+    double FC = 0.0;
+    for (int k = 0; k < 3; ++k) FC += F[i + 3 * k] * C[k + 3 * j];
+    R[i + 3 * j] = (i == j ? IU1 * IF2 : 0.0) + (IU1 * IU1 - IU2) * F[i + 3 * j] - IU1 * IF1 * F[j + 3 * i]
+                 + IU1 * FF[j + 3 * i] - FC;
+  }
+  double d = R[0] * (R[4] * R[8] - R[7] * R[5]) - R[3] * (R[1] * R[8] - R[7] * R[2]) + R[6] * (R[1] * R[5] - R[4] * R[2]);
+  double s = pow(d, -1.0 / 3.0);
+  for (int k = 0; k < 9; ++k) R[k] *= s;
+}
+
+void dgo_om2qu(const double om[9], double qu[4]) {
+#define OM(i, j) om[(i - 1) + 3 * (j - 1)]
+  double tr = OM(1, 1) + OM(2, 2) + OM(3, 3), s;
+  if (tr > 0.0) {
+    s = 0.5 / sqrt(tr + 1.0);
+    qu[0] = 0.25 / s; qu[1] = (OM(3, 2) - OM(2, 3)) * s; qu[2] = (OM(1, 3) - OM(3, 1)) * s; qu[3] = (OM(2, 1) - OM(1, 2)) * s;
+  } else if (OM(1, 1) > OM(2, 2) && OM(1, 1) > OM(3, 3)) {
+    s = 2.0 * sqrt(1.0 + OM(1, 1) - OM(2, 2) - OM(3, 3));
+    qu[0] = (OM(3, 2) - OM(2, 3)) / s; qu[1] = 0.25 * s; qu[2] = (OM(1, 2) + OM(2, 1)) / s; qu[3] = (OM(1, 3) + OM(3, 1)) / s;
+  } else if (OM(2, 2) > OM(3, 3)) {
+    s = 2.0 * sqrt(1.0 + OM(2, 2) - OM(1, 1) - OM(3, 3));
+    qu[0] = (OM(1, 3) - OM(3, 1)) / s; qu[1] = (OM(1, 2) + OM(2, 1)) / s; qu[2] = 0.25 * s; qu[3] = (OM(2, 3) + OM(3, 2)) / s;
+  } else {
+    s = 2.0 * sqrt(1.0 + OM(3, 3) - OM(1, 1) - OM(2, 2));
+    qu[0] = (OM(2, 1) - OM(1, 2)) / s; qu[1] = (OM(1, 3) + OM(3, 1)) / s; qu[2] = (OM(2, 3) + OM(3, 2)) / s; qu[3] = 0.25 * s;
+  }
+#undef OM
+  if (copysign(1.0, qu[0]) < 0.0) for (int k = 0; k < 4; ++k) qu[k] = -qu[k];
+  for (int k = 1; k < 4; ++k) if (qu[k] != 0.0) qu[k] = -qu[k];           /* P = -1 */
+  double n = sqrt(qu[0] * qu[0] + qu[1] * qu[1] + qu[2] * qu[2] + qu[3] * qu[3]);
+  for (int k = 0; k < 4; ++k) qu[k] /= n;
+}
+
+/* O written for a point: quaternion of (rotational part of Fe)^T */
+void dgo_orientation_output(const double Fe[9], double qu[4]) {
+  double R[9], Rt[9];
+  dgo_rotational_part(Fe, R);
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) Rt[i + 3 * j] = R[j + 3 * i];
+  dgo_om2qu(Rt, qu);
+}

@@ -370,3 +370,72 @@ double dgo_form_residual_bc(const double S[81], const double P_av[9], const doub
   dgo_rotate2(q, dF, rotated, 1);
   return err;
 }
+
+/* ------------------------------------------------------------------ coordinates
+ * Cell-centre and nodal displacements of the deformed grid (the grid solver's
+ * coordinate update; reference src/grid/mech_base.cpp:45-154, with the cell-centre
+ * positions x_p = u~ + Favg (i + 1/2) step of the Fortran grid solver that wrote the
+ * reference's DADF5 results).  F: 9 per cell (column-major 3x3), cells x fastest.
+ * u_p[3*cell + k] = x_p - (i + 1/2) step ; u_n[3*node + k] = x_n - i step, nodes
+ * (N0+1)(N1+1)(N2+1) x fastest.  Fluctuation: u~^(xi) = F^(xi) xi / sum conj(-xi) xi
+ * with xi = xi2nd, zero at xi = 0, backward FFT times wgt. */
+void dgo_update_coords(const int cells[3], const double geom[3], int derivative, const double* F,
+                       double* u_n, double* u_p) {
+  const int N0 = cells[0], N1 = cells[1], N2 = cells[2], N0r = N0 / 2 + 1;
+  const size_t N = (size_t)N0 * N1 * N2, Nh = (size_t)N0r * N1 * N2;
+  const double wgt = pow((double)N, -1.0);
+  cplx* Fh = (cplx*)malloc(sizeof(cplx) * 9 * Nh);
+  cplx* uh = (cplx*)malloc(sizeof(cplx) * 3 * Nh);
+  cplx* x1 = (cplx*)malloc(sizeof(cplx) * 3 * Nh);
+  cplx* x2 = (cplx*)malloc(sizeof(cplx) * 3 * Nh);
+  double* ut = (double*)malloc(sizeof(double) * 3 * N);
+  dgo_fft_r2c(cells, 9, F, (double*)Fh);
+  dgo_xi(cells, geom, derivative, (double*)x1, (double*)x2);
+  double Favg[9];
+  for (int c = 0; c < 9; ++c) Favg[c] = creal(Fh[c]) * wgt;          /* zero frequency, (i,z,y) = 0 */
+  for (size_t f = 0; f < Nh; ++f) {
+    const cplx* xi = x2 + 3 * f;
+    if (f == 0) { uh[0] = uh[1] = uh[2] = 0.0; continue; }
+    cplx den = 0.0;
+    for (int m = 0; m < 3; ++m) den += conj(-xi[m]) * xi[m];
+    for (int l = 0; l < 3; ++l) {
+      cplx s = 0.0;
+      for (int m = 0; m < 3; ++m) s += Fh[9 * f + l + 3 * m] * xi[m];
+      uh[3 * f + l] = s / den;
+    }
+  }
+  dgo_fft_c2r(cells, 3, (const double*)uh, ut);
+  for (size_t k = 0; k < 3 * N; ++k) ut[k] *= wgt;
+  const double step[3] = {geom[0] / N0, geom[1] / N1, geom[2] / N2};
+  for (int z = 0; z < N2; ++z)
+    for (int y = 0; y < N1; ++y)
+      for (int x = 0; x < N0; ++x) {
+        size_t e = (size_t)x + N0 * ((size_t)y + N1 * z);
+        double pos[3] = {(x + 0.5) * step[0], (y + 0.5) * step[1], (z + 0.5) * step[2]};
+        for (int l = 0; l < 3; ++l) {
+          double v = ut[3 * e + l];
+          for (int m = 0; m < 3; ++m) v += Favg[l + 3 * m] * pos[m];
+          u_p[3 * e + l] = v - pos[l];
+        }
+      }
+  for (int z = 0; z <= N2; ++z)
+    for (int y = 0; y <= N1; ++y)
+      for (int x = 0; x <= N0; ++x) {
+        size_t nd = (size_t)x + (N0 + 1) * ((size_t)y + (N1 + 1) * z);
+        double pos[3] = {x * step[0], y * step[1], z * step[2]};
+        double v[3];
+        for (int l = 0; l < 3; ++l) {
+          v[l] = 0.0;
+          for (int m = 0; m < 3; ++m) v[l] += Favg[l + 3 * m] * pos[m];
+        }
+        for (int dz = 0; dz < 2; ++dz)
+          for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+              int cx = (x + dx - 1 + N0) % N0, cy = (y + dy - 1 + N1) % N1, cz = (z + dz - 1 + N2) % N2;
+              size_t e = (size_t)cx + N0 * ((size_t)cy + N1 * cz);
+              for (int l = 0; l < 3; ++l) v[l] += ut[3 * e + l] * 0.125;
+            }
+        for (int l = 0; l < 3; ++l) u_n[3 * nd + l] = v[l] - pos[l];
+      }
+  free(Fh); free(uh); free(x1); free(x2); free(ut);
+}

@@ -155,19 +155,55 @@ class RVE:
         _d.check(_d.lib().dgx_solver_solve(self.h, C.byref(conv), C.byref(it), C.byref(ill)), "dgx_solver_solve")
         return dict(converged=bool(conv.value), required_iterations=it.value, terminally_ill=bool(ill.value))
 
-    def loop_over_loadcase(self, steps, max_records=100000):
+    def loop_over_loadcase(self, steps, max_records=100000, result=None, restart=None, restart_every=0,
+                           phase="phase", homogenization="SX", setup=None):
+        """DamaskGrid::loop_over_loadcase from solver init.  result: DADF5 file written
+        at increment 0 and every f_out-th increment; restart: restart file rewritten
+        every restart_every increments; setup: {name: text} stored under /setup."""
         arr = (_d.LoadStep * len(steps))(*steps)
         nrec = sum(int(s.N) for s in steps)
         recs = (_d.IncRecord * max(1, min(nrec, max_records)))()
         n = C.c_int32(0)
-        _d.check(_d.lib().dgx_run_loadcase(self.h, len(steps), arr, recs, len(recs), C.byref(n)), "dgx_run_loadcase")
+        L = _d.lib()
+        if result is None and restart is None:
+            _d.check(L.dgx_run_loadcase(self.h, len(steps), arr, recs, len(recs), C.byref(n)), "dgx_run_loadcase")
+            return [_record(r) for r in recs[:n.value]]
+        res = C.c_void_p()
+        if result is not None:
+            _d.check(L.dgx_result_open(str(result).encode(), self.h, phase.encode(), homogenization.encode(),
+                                       C.byref(res)), "dgx_result_open")
+            for name, text in (setup or {}).items():
+                t = text.encode()
+                _d.check(L.dgx_result_add_setup(res, name.encode(), t, len(t)), "dgx_result_add_setup")
+        try:
+            _d.check(L.dgx_run_loadcase_output(self.h, len(steps), arr, recs, len(recs), C.byref(n), res,
+                                               str(restart).encode() if restart else None, int(restart_every)),
+                     "dgx_run_loadcase_output")
+        finally:
+            if res:
+                _d.check(L.dgx_result_close(res), "dgx_result_close")
         return [_record(r) for r in recs[:n.value]]
+
+    def write_restart(self, path):
+        _d.check(_d.lib().dgx_restart_write(self.h, str(path).encode()), "dgx_restart_write")
+
+    def read_restart(self, path):
+        """Continue from a restart file written by an RVE created with the same inputs."""
+        _d.check(_d.lib().dgx_restart_read(self.h, str(path).encode()), "dgx_restart_read")
 
     def run_increment(self, step, step_index, inc):
         rec = _d.IncRecord()
         _d.check(_d.lib().dgx_run_increment(self.h, C.byref(step), int(step_index), int(inc), C.byref(rec)),
                  "dgx_run_increment")
         return _record(rec)
+
+    def update_coords(self):
+        """MechSolverBasic::update_coords: (u_n (nodes, 3), u_p (cells, 3)) displacements."""
+        N0, N1, N2 = self.cells
+        un = np.zeros(3 * (N0 + 1) * (N1 + 1) * (N2 + 1))
+        up = np.zeros(3 * self.N)
+        _d.check(_d.lib().dgx_update_coords(self.h, _d.dptr(un), _d.dptr(up)), "dgx_update_coords")
+        return un.reshape(-1, 3), up.reshape(-1, 3)
 
     def get(self, name):
         width = {"xi": 12, "gamma": 12}.get(name, 9)

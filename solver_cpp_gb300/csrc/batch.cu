@@ -340,6 +340,8 @@ struct Task {
   int nsteps = 0, l = 0, inc = 0;
   dgx_inc_record* records = nullptr;
   int max_records = 0, nrec = 0;
+  Output out{nullptr, nullptr, 0};    // optional result / restart output (load case mode)
+  int total = 0;                      // increments completed (the results' increment number)
   int32_t conv = 0, sit = 0, sill = 0;
   TState pc = T_LC_BEGIN;
   dgx_status err = DGX_OK;
@@ -383,7 +385,8 @@ static dgx_status advance(Task& t) {
   for (;;) {
     switch (t.pc) {
       case T_LC_BEGIN:
-        t.l = 0; t.inc = 0; t.nrec = 0;
+        t.l = 0; t.inc = 0; t.nrec = 0; t.total = 0;
+        if (t.out.result) TRY(result_write_impl(t.out.result, r, 0, r->t));
         t.pc = t.nsteps > 0 ? T_INC_BEGIN : T_DONE;
         break;
       case T_INC_BEGIN: {
@@ -580,6 +583,15 @@ static dgx_status advance(Task& t) {
           rec.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t.t0).count();
         }
         t.nrec++;
+        t.total++;
+        if (t.mode == 2) {
+          // DamaskGrid::loop_over_loadcase output (the Fortran grid solver's cadence,
+          // 1-based increment within the step)
+          const int f_out = std::max(1, (int)t.cur_step()->f_out);
+          if (t.out.result && (t.inc + 1) % f_out == 0) TRY(result_write_impl(t.out.result, r, t.total, r->t));
+          if (t.out.restart_every > 0 && t.total % t.out.restart_every == 0)
+            TRY(restart_write_impl(r, t.out.restart_path));
+        }
         if (t.mode == 1) { t.pc = T_DONE; break; }
         if (++t.inc >= t.steps[t.l].N) { t.l++; t.inc = 0; }
         t.pc = t.l < t.nsteps ? T_INC_BEGIN : T_DONE;
@@ -621,9 +633,10 @@ static dgx_status ensure_executor(dgx_rve* r) {
 // a solve (mode 0), one increment (mode 1) or a load case (mode 2) of one RVE as a batch of one
 dgx_status run_single(dgx_rve* r, int mode, const dgx_loadstep* steps, int n_or_index, int inc,
                       dgx_inc_record* records, int max_records, int32_t* n_records, int32_t* conv, int32_t* iterations,
-                      int32_t* ill) {
+                      int32_t* ill, const Output* out) {
   TRY(ensure_executor(r));
   Task t;
+  if (out) t.out = *out;
   t.r = r; t.mode = mode; t.steps = steps; t.records = records; t.max_records = max_records;
   if (mode == 0) t.pc = T_SOLVE_BEGIN;
   else if (mode == 1) { t.pc = T_INC_BEGIN; t.l = n_or_index; t.inc = inc; t.nsteps = 1; }

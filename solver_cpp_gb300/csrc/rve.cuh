@@ -36,6 +36,7 @@ struct dgx_rve {
   dgx::ConsCounters* d_cnt = nullptr;
   double *d_xi_x = nullptr, *d_xi_y = nullptr, *d_xi_z = nullptr;
   double* d_dPdF = nullptr;        // optional (81 planes) for the boundary call
+  double *d_un = nullptr, *d_up = nullptr, *d_Favg = nullptr;   // optional: coordinate update
   int32_t* d_mat = nullptr;
   double* d_Rm = nullptr;
   int n_materials = 0;
@@ -130,8 +131,19 @@ void executor_destroy(Executor* e);
 void executor_stats(const Executor* e, double ms[3], int64_t n[3], int64_t* launches, int64_t* h2d_b, int64_t* d2h_b);
 // a solve (mode 0), one increment (mode 1: steps = that step, n_or_index = its index)
 // or a load case (mode 2: n_or_index = number of steps) of one RVE, as a batch of one
+// result / restart output of a load case (increment 0 at the start, then every
+// f_out-th increment of a step; a restart file every restart_every-th increment)
+struct Output {
+  dgx_result* result;
+  const char* restart_path;
+  int restart_every;
+};
 dgx_status run_single(dgx_rve* r, int mode, const dgx_loadstep* steps, int n_or_index, int inc,
                       dgx_inc_record* records, int max_records, int32_t* n_records, int32_t* conv, int32_t* iterations,
-                      int32_t* ill);
+                      int32_t* ill, const Output* out = nullptr);
+// the unguarded bodies of dgx_update_coords / dgx_result_write_increment / dgx_restart_write
+dgx_status update_coords_impl(dgx_rve* r, double* u_n, double* u_p);
+dgx_status result_write_impl(dgx_result* res, dgx_rve* r, int32_t inc, double t);
+dgx_status restart_write_impl(dgx_rve* r, const char* path);
 
 }  // namespace dgx

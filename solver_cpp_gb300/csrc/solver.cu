@@ -967,6 +967,42 @@ extern "C" dgx_status dgx_run_loadcase(dgx_rve* r, int32_t nsteps, const dgx_loa
   return run_single(r, 2, steps, nsteps, 0, records, max_records, n_records, nullptr, nullptr, nullptr);
 }
 
+extern "C" dgx_status dgx_run_loadcase_output(dgx_rve* r, int32_t nsteps, const dgx_loadstep* steps,
+                                              dgx_inc_record* records, int32_t max_records, int32_t* n_records,
+                                              dgx_result* result, const char* restart_path, int32_t restart_every) {
+  if (!r || !steps || nsteps < 1) return DGX_ERR_ARG;
+  if (r->in_batch) { set_err("RVE is driven by a batch"); return DGX_ERR_STATE; }
+  if (restart_every > 0 && !restart_path) return DGX_ERR_ARG;
+  TRY(dgx_solver_init(r));
+  Output out{result, restart_path, restart_every};
+  return run_single(r, 2, steps, nsteps, 0, records, max_records, n_records, nullptr, nullptr, nullptr, &out);
+}
+
+// MechSolverBasic::update_coords / MechBase::base_update_coords (mech_solver_basic.cpp:222-238,
+// mech_base.cpp:45-154) on the current solution field X
+dgx_status dgx::update_coords_impl(dgx_rve* r, double* u_n, double* u_p) {
+  const int64_t Nn = (int64_t)(r->cells[0] + 1) * (r->cells[1] + 1) * (r->cells[2] + 1);
+  if (!r->d_un) {
+    TRY(dalloc(r, &r->d_un, 3 * Nn));
+    TRY(dalloc(r, &r->d_up, 3 * r->N));
+    TRY(dalloc(r, &r->d_Favg, 9));
+  }
+  spec_update_coords(r->sl, r->num.precision == 1, r->ax[0].plan, r->ax[1].plan, r->ax[2].plan, r->X, r->N, r->spec,
+                     r->XA, r->geom, r->num.derivative, r->wgt, r->d_Favg, r->d_un, r->d_up, r->st);
+  r->n_launch += 8;
+  if (u_n) CK(d2h(r, u_n, r->d_un, sizeof(double) * 3 * Nn));
+  if (u_p) CK(d2h(r, u_p, r->d_up, sizeof(double) * 3 * r->N));
+  CK(cudaStreamSynchronize(r->st));
+  CK(cudaGetLastError());
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_update_coords(dgx_rve* r, double* u_n, double* u_p) {
+  if (!r) return DGX_ERR_ARG;
+  if (r->in_batch) { set_err("RVE is driven by a batch"); return DGX_ERR_STATE; }
+  return update_coords_impl(r, u_n, u_p);
+}
+
 extern "C" dgx_status dgx_get(dgx_rve* r, const char* name, double* out) {
   if (!r || !name || !out) return DGX_ERR_ARG;
   std::string s(name);

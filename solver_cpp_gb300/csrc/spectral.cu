@@ -223,10 +223,10 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
     a[((long)c * ti + i) * g.N2 + z] = spec[c * g.Nh + z * zs + (long long)y * g.N0r + i0 + i];
   }
   __syncthreads();
-  C* res = block_fft<R>(a, b, 9 * ti, pz, -1);
+  C* res = block_fft<R>(a, b, 9 * ti, pz, (ga.store_fwd && !ga.do_gamma && ga.zsign > 0) ? +1 : -1);
   C* other = (res == a) ? b : a;
   double dsum = 0.0;
-  for (int t = threadIdx.x; t < ti * g.N2; t += blockDim.x) {
+  for (int t = threadIdx.x; (ga.do_div || ga.do_gamma) && t < ti * g.N2; t += blockDim.x) {
     int i = t / g.N2, z = t - i * g.N2;
     int ix = i0 + i;
     double ax = ga.xi_x[ix], ay = ga.xi_y[y], az = ga.xi_z[z];
@@ -321,6 +321,102 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
   }
 }
 
+// ---------------------------------------------------------------- coordinates
+// per half-spectrum frequency: u^ = F^ xi2nd / sum conj(-xi2nd) xi2nd (xi2nd = i a,
+// purely imaginary for the continuous and central derivatives: u^_l = -i (F^ a)_l / |a|^2),
+// zero at the zero frequency, whose real part gives Favg; components 3..8 cleared
+template <typename R>
+__global__ void k_coords_freq(SpecGeom g, typename cpx<R>::t* __restrict__ spec, double s0, double s1, double s2,
+                              int derivative, double wgt, double* __restrict__ Favg) {
+  typedef typename cpx<R>::t C;
+  const long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (f >= g.Nh) return;
+  const double TAU = 6.283185307179586476925286766559;
+  const int i = (int)(f % g.N0r);
+  const long long yz = f / g.N0r;
+  const int y = (int)(yz % g.N1), z = (int)(yz / g.N1);
+  const int k[3] = {i, y > g.N1 / 2 ? y - g.N1 : y, z > g.N2 / 2 ? z - g.N2 : z};
+  const int n[3] = {g.N0, g.N1, g.N2};
+  const double sz[3] = {s0, s1, s2};
+  double a[3], a2 = 0.0;
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    a[p] = derivative == 0 ? TAU * k[p] / sz[p] : sin(TAU * k[p] / n[p]) / (2.0 * sz[p] / n[p]);
+    a2 += a[p] * a[p];
+  }
+  C Fh[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) Fh[c] = spec[c * g.Nh + f];
+  if (f == 0) {
+#pragma unroll
+    for (int c = 0; c < 9; ++c) Favg[c] = (double)Fh[c].x * wgt;
+  }
+  C out[3];
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    double nr = 0.0, ni = 0.0;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) { nr += (double)Fh[l + 3 * m].x * a[m]; ni += (double)Fh[l + 3 * m].y * a[m]; }
+    // -i (nr + i ni) / a2 = (ni - i nr) / a2
+    bool zero = (f == 0) || !(a2 > 0.0);
+    out[l].x = zero ? (R)0 : (R)(ni / a2);
+    out[l].y = zero ? (R)0 : (R)(-nr / a2);
+  }
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {
+    C v; v.x = 0; v.y = 0;
+    if (c < 3) v = out[c];
+    spec[c * g.Nh + f] = v;
+  }
+}
+
+// cell-centre and nodal displacements from the fluctuation planes ut (wgt applied here)
+__global__ void k_coords_out(SpecGeom g, const double* __restrict__ ut, long long ld, double wgt, const double* Favg,
+                             double st0, double st1, double st2, double* __restrict__ u_n, double* __restrict__ u_p) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long Nn = (long long)(g.N0 + 1) * (g.N1 + 1) * (g.N2 + 1);
+  double F[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) F[c] = Favg[c];
+  const double step[3] = {st0, st1, st2};
+  if (t < g.N) {
+    const int x = (int)(t % g.N0);
+    const long long yz = t / g.N0;
+    const int y = (int)(yz % g.N1), z = (int)(yz / g.N1);
+    const double pos[3] = {(x + 0.5) * step[0], (y + 0.5) * step[1], (z + 0.5) * step[2]};
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+      double v = ut[l * ld + t] * wgt;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) v += F[l + 3 * m] * pos[m];
+      u_p[3 * t + l] = v - pos[l];
+    }
+  }
+  if (t < Nn) {
+    const int x = (int)(t % (g.N0 + 1));
+    const long long yz = t / (g.N0 + 1);
+    const int y = (int)(yz % (g.N1 + 1)), z = (int)(yz / (g.N1 + 1));
+    const double pos[3] = {x * step[0], y * step[1], z * step[2]};
+    double v[3];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+      v[l] = 0.0;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) v[l] += F[l + 3 * m] * pos[m];
+    }
+    for (int dz = 0; dz < 2; ++dz)
+      for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+          const int cx = (x + dx - 1 + g.N0) % g.N0, cy = (y + dy - 1 + g.N1) % g.N1, cz = (z + dz - 1 + g.N2) % g.N2;
+          const long long e = cx + (long long)g.N0 * (cy + (long long)g.N1 * cz);
+#pragma unroll
+          for (int l = 0; l < 3; ++l) v[l] += ut[l * ld + e] * wgt * 0.125;
+        }
+#pragma unroll
+    for (int l = 0; l < 3; ++l) u_n[3 * t + l] = v[l] - pos[l];
+  }
+}
+
 __global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt, int N0, double* out,
                              const SpecItem* __restrict__ items) {
   if (items) { part = items[blockIdx.x].div_part; out = items[blockIdx.x].rms; }
@@ -337,6 +433,7 @@ __global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt
 }  // namespace dgx
 
 // ------------------------------------------------------------------ host side
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -470,6 +567,35 @@ void spec_convolve_batch(const SpecLaunch& L, bool fp32, const AxisPlan& px, con
                          const SpecItem* items, int nitems, const GammaArgs& ga, cudaStream_t st) {
   if (fp32) convolve_impl<float>(L, px, py, pz, nullptr, nullptr, L.g.N, nullptr, ga, items, nitems, st);
   else convolve_impl<double>(L, px, py, pz, nullptr, nullptr, L.g.N, nullptr, ga, items, nitems, st);
+}
+
+void spec_update_coords(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                        const double* F, long long ld, void* spec, double* scratch, const double size[3],
+                        int derivative, double wgt, double* Favg, double* u_n, double* u_p, cudaStream_t st) {
+  GammaArgs ga{};
+  ga.store_fwd = 1; ga.zsign = -1;
+  const SpecGeom& g = L.g;
+  const long long Nn = (long long)(g.N0 + 1) * (g.N1 + 1) * (g.N2 + 1);
+  const int nbf = (int)((g.Nh + 255) / 256), nbo = (int)((std::max(g.N, Nn) + 255) / 256);
+  if (fp32) {
+    typedef float2 C;
+    convolve_impl<float>(L, px, py, pz, F, nullptr, ld, spec, ga, nullptr, 1, st);
+    k_coords_freq<float><<<nbf, 256, 0, st>>>(g, (C*)spec, size[0], size[1], size[2], derivative, wgt, Favg);
+    ga.zsign = +1;
+    k_zpass<float><<<L.nbz, 256, L.smz, st>>>(g, pz, (C*)spec, L.TIz, ga, nullptr);
+    k_ypass<float><<<L.nby, 256, L.smy, st>>>(g, py, (C*)spec, L.TIy, +1, nullptr);
+    k_xinv<float, double><<<L.nbx, 256, L.smx, st>>>(g, px, (const C*)spec, scratch, ld, L.LX, nullptr);
+  } else {
+    typedef double2 C;
+    convolve_impl<double>(L, px, py, pz, F, nullptr, ld, spec, ga, nullptr, 1, st);
+    k_coords_freq<double><<<nbf, 256, 0, st>>>(g, (C*)spec, size[0], size[1], size[2], derivative, wgt, Favg);
+    ga.zsign = +1;
+    k_zpass<double><<<L.nbz, 256, L.smz, st>>>(g, pz, (C*)spec, L.TIz, ga, nullptr);
+    k_ypass<double><<<L.nby, 256, L.smy, st>>>(g, py, (C*)spec, L.TIy, +1, nullptr);
+    k_xinv<double, double><<<L.nbx, 256, L.smx, st>>>(g, px, (const C*)spec, scratch, ld, L.LX, nullptr);
+  }
+  k_coords_out<<<nbo, 256, 0, st>>>(g, scratch, ld, wgt, Favg, size[0] / g.N0, size[1] / g.N1, size[2] / g.N2, u_n,
+                                    u_p);
 }
 
 void spec_div_finish_batch(const SpecItem* items, int nitems, int nb, double wgt, int N0, cudaStream_t st) {

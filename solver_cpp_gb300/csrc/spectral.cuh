@@ -41,7 +41,8 @@ struct GammaArgs {
   const double* C_ref;    // 81, device
   const double* aim;      // 9, device (zero-frequency value), may be null when !gamma
   int do_gamma, do_div;
-  int store_fwd;          // without gamma: write the forward z transform back
+  int store_fwd;          // without gamma: write the z transform back (forward, or inverse if zsign > 0)
+  int zsign;              // with store_fwd: -1 forward (default 0 means forward), +1 inverse
   double* div_part;       // per block partial of the divergence sum (FP64)
 };
 
@@ -66,6 +67,12 @@ SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize);
 void spec_prepare(const SpecLaunch& L, bool fp32);
 void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                    const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st);
+// Displacements of the deformed grid from the deformation gradient planes F (ld):
+// u_p (3 per cell) and u_n (3 per node, (N0+1)(N1+1)(N2+1)), AoS, x fastest.
+// scratch: 9 real planes (ld); Favg: 9 doubles out (device).
+void spec_update_coords(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
+                        const double* F, long long ld, void* spec, double* scratch, const double size[3],
+                        int derivative, double wgt, double* Favg, double* u_n, double* u_p, cudaStream_t st);
 // nitems RVEs of the same grid (and precision) in one launch per pass; items in device memory
 void spec_convolve_batch(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                          const SpecItem* items, int nitems, const GammaArgs& ga, cudaStream_t st);

@@ -73,7 +73,9 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_measure_fp64_peak", "dgx_divergence_rms_static", "dgx_batch_create", "dgx_batch_destroy",
            "dgx_batch_add", "dgx_batch_step", "dgx_batch_run", "dgx_batch_member", "dgx_batch_remove",
            "dgx_batch_stats", "dgx_batch_stream", "dgx_rve_footprint", "dgx_server_create", "dgx_server_destroy",
-           "dgx_server_submit", "dgx_server_poll", "dgx_server_release", "dgx_server_stats"]
+           "dgx_server_submit", "dgx_server_poll", "dgx_server_release", "dgx_server_stats",
+           "dgx_update_coords", "dgx_result_open", "dgx_result_add_setup", "dgx_result_write_increment",
+           "dgx_result_close", "dgx_restart_write", "dgx_restart_read", "dgx_run_loadcase_output"]
 
 
 class DgxError(RuntimeError):
@@ -131,6 +133,15 @@ def lib():
     L.dgx_batch_stats.argtypes = [vp, dp, C.POINTER(C.c_int64)]
     L.dgx_batch_stream.argtypes = [vp]
     L.dgx_batch_stream.restype = vp
+    L.dgx_update_coords.argtypes = [vp, dp, dp]
+    L.dgx_result_open.argtypes = [C.c_char_p, vp, C.c_char_p, C.c_char_p, C.POINTER(vp)]
+    L.dgx_result_add_setup.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int64]
+    L.dgx_result_write_increment.argtypes = [vp, vp, C.c_int32, C.c_double]
+    L.dgx_result_close.argtypes = [vp]
+    L.dgx_restart_write.argtypes = [vp, C.c_char_p]
+    L.dgx_restart_read.argtypes = [vp, C.c_char_p]
+    L.dgx_run_loadcase_output.argtypes = [vp, C.c_int32, C.POINTER(LoadStep), C.POINTER(IncRecord), C.c_int32, ip, vp,
+                                          C.c_char_p, C.c_int32]
     L.dgx_rve_footprint.argtypes = [ip, C.POINTER(Numerics), C.c_int32, i64p]
     L.dgx_server_create.argtypes = [C.c_int64, C.c_int32, C.c_int32, C.POINTER(vp)]
     L.dgx_server_destroy.argtypes = [vp]

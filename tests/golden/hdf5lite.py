@@ -108,6 +108,67 @@ class HDF5File:
     def keys(self, path="/"):
         return sorted(self._group_entries(self.lookup(path)))
 
+    # ---------------------------------------------------------------- datatypes
+    def _dtype(self, p):
+        """numpy dtype of the datatype message at p and its encoded size."""
+        b = self.b
+        cls, ver = b[p] & 0x0F, b[p] >> 4
+        bits = b[p + 1] | (b[p + 2] << 8)
+        esize = struct.unpack_from("<I", b, p + 4)[0]
+        order = ">" if bits & 1 else "<"
+        if cls == 1:
+            return np.dtype(order + {4: "f4", 8: "f8"}[esize]), 20
+        if cls == 0:
+            return np.dtype(order + ("i" if bits & 8 else "u") + str(esize)), 12
+        if cls == 3:
+            return np.dtype("S%d" % esize), 8
+        if cls == 6:
+            q, fields = p + 8, []
+            for _ in range(bits & 0xFFFF):
+                e = b.index(b"\0", q)
+                name = b[q:e].decode()
+                if ver == 1:
+                    q = q + ((e - q) // 8 + 1) * 8
+                    off = struct.unpack_from("<I", b, q)[0]
+                    q += 32
+                else:
+                    q = e + 1
+                    nb = 1 if esize < 256 else 2 if esize < 65536 else 4
+                    off = int.from_bytes(b[q:q + nb], "little")
+                    q += nb
+                mdt, msz = self._dtype(q)
+                q += msz
+                fields.append((name, mdt, off))
+            return np.dtype({"names": [f[0] for f in fields], "formats": [f[1] for f in fields],
+                             "offsets": [f[2] for f in fields], "itemsize": esize}), q - p
+        if cls == 9:                              # variable length: data in the global heap
+            return None, 8
+        raise NotImplementedError("datatype class %d" % cls)
+
+    def attrs(self, path="/"):
+        """Attributes (version-1 messages) of an object: name -> numpy value or str."""
+        b = self.b
+        out = {}
+        for mtype, p, size in self._messages(self.lookup(path)):
+            if mtype != 0x0C or b[p] != 1:
+                continue
+            nsz, dsz, ssz = struct.unpack_from("<HHH", b, p + 2)
+            q = p + 8
+            name = b[q:q + nsz - 1].decode()
+            q += (nsz + 7) // 8 * 8
+            dt, _ = self._dtype(q)
+            q += (dsz + 7) // 8 * 8
+            if dt is None:
+                out[name] = None
+                continue
+            rank = b[q + 1]
+            shape = tuple(self._l(q + 8 + 8 * i) for i in range(rank))
+            q += (ssz + 7) // 8 * 8
+            n = int(np.prod(shape)) if shape else 1
+            v = np.frombuffer(b[q:q + n * dt.itemsize], dtype=dt).reshape(shape)
+            out[name] = v.item().rstrip(b"\0").decode() if dt.kind == "S" and not shape else v.copy()
+        return out
+
     # ---------------------------------------------------------------- datasets
     def read(self, path):
         b = self.b
@@ -120,17 +181,7 @@ class HDF5File:
                 q = p + (8 if ver == 1 else 4)
                 shape = tuple(self._l(q + i * self.sl) for i in range(rank))
             elif mtype == 0x03:
-                cls = b[p] & 0x0F
-                bits = b[p + 1]
-                esize = struct.unpack_from("<I", b, p + 4)[0]
-                order = ">" if bits & 1 else "<"
-                if cls == 1:
-                    dtype = np.dtype(order + {4: "f4", 8: "f8"}[esize])
-                elif cls == 0:
-                    signed = bool(bits & 8)
-                    dtype = np.dtype(order + ("i" if signed else "u") + str(esize))
-                else:
-                    raise NotImplementedError("datatype class %d" % cls)
+                dtype, _ = self._dtype(p)
             elif mtype == 0x08:
                 ver = b[p]
                 if ver == 3:

@@ -6,7 +6,9 @@ Source (reference tree, read-only): python/tests/resources/Result/
   dot_F_yy = 1e-3/s, P_xx = P_zz = 0, t = 20 s, N = 40, f_out = 4, default numerics)
 Writes tests/golden/damask_6grains6x7x8_tensionY.npz with the material map,
 orientations, volume averages of F and P at every written increment and the
-fields F, P, F_p, L_p, xi_sl at increments 20 and 40 (HDF5 C order: [cell][i][j]).
+fields F, P, F_e, F_p, L_p, xi_sl, O (orientation quaternion) and the displacements
+u_p (cell centres) and u_n (nodes) at increments 20 and 40 (HDF5 C order:
+[cell][i][j]), and the list of datasets of one increment group (DADF5 layout).
 
     python tests/golden/make_damask_fixture.py /path/to/reference
 """
@@ -53,8 +55,16 @@ def main(ref):
     out = dict(cells=np.array(cells), size=np.array(size), material_at=mat, orientations=O,
                increments=np.array(incs), P_av=P_av, F_av=F_av)
     for inc in (20, 40):
-        for name in ("F", "P", "F_p", "L_p", "xi_sl"):
+        for name in ("F", "P", "F_e", "F_p", "L_p", "xi_sl", "O"):
             out[f"{name}_{inc}"] = f.read(f"/increment_{inc}{ph}{name}")
+        for name in ("u_p", "u_n"):
+            out[f"{name}_{inc}"] = f.read(f"/increment_{inc}/geometry/{name}")
+    layout = []
+    for g in ("geometry", "phase/pheno_fcc/mechanical", "homogenization/SX/mechanical"):
+        for k in f.keys(f"/increment_40/{g}"):
+            layout.append(f"{g}/{k}")
+    out["layout_increment"] = np.array(sorted(layout))
+    out["layout_root"] = np.array(sorted(f.keys("/")))
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "damask_6grains6x7x8_tensionY.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst, os.path.getsize(dst), "bytes")

@@ -46,3 +46,16 @@ def test_fields_final_increment(run):
         assert rel < 1e-9, (name, rel)
     xi = s.get("xi")
     assert np.abs(xi - fx["xi_sl_40"]).max() / fx["xi_sl_40"].max() < 1e-10
+
+
+def test_oracle_coordinates_and_orientations_vs_damask():
+    """Coordinate update (u_p, u_n) and orientation output (O) of the oracle against the
+    Fortran DAMASK result, computed from that result's own F and F_e fields."""
+    from tests import cases
+    fx = cases.damask_6grains()
+    for inc in (20, 40):
+        un, up = dgo.update_coords(fx["cells"], fx["size"], dgo.fortran9(fx[f"F_{inc}"]))
+        assert np.abs(up - fx[f"u_p_{inc}"]).max() < 1e-12 * np.abs(fx[f"u_p_{inc}"]).max()
+        assert np.abs(un - fx[f"u_n_{inc}"]).max() < 1e-12 * np.abs(fx[f"u_n_{inc}"]).max()
+        O = dgo.orientation_output(dgo.fortran9(fx[f"F_e_{inc}"]))
+        assert np.abs(O - fx[f"O_{inc}"]).max() < 1e-13
