@@ -3,7 +3,8 @@
 ``parse_load_yaml`` reads the load file of ``DAMASK_grid -l`` (reference
 src/grid/config.cpp:247-358: solver.mechanical, loadstep list with
 boundary_conditions.mechanical {dot_F|F|L} and {P|dot_P} 3x3 matrices where 'x'
-marks an unprescribed component, optional R quaternion, discretization {t, N, r},
+marks an unprescribed component (a step without P / dot_P prescribes no stress, as
+in the reference's examples/grid/shearZX.yaml), optional R quaternion, discretization {t, N, r},
 f_out, estimate_rate) and returns dgx_loadstep structures.  ``parse_numerics_yaml``
 reads solver.grid (config.cpp:360-464).  The YAML subset understood here is
 block mappings/sequences plus flow sequences and flow mappings -- what the
@@ -230,10 +231,14 @@ def parse_load_yaml(text):
         bc = item["boundary_conditions"]["mechanical"]
         defs = [k for k in ("F", "dot_F", "L") if k in bc]
         strs = [k for k in ("P", "dot_P") if k in bc]
-        if len(defs) != 1 or len(strs) != 1:
-            raise ValueError("exactly one deformation and one stress specification per load step")
+        if len(defs) != 1 or len(strs) > 1:
+            raise ValueError("exactly one deformation and at most one stress specification per load step")
         dv, dm = _matrix(bc[defs[0]])
-        sv, sm = _matrix(bc[strs[0]])
+        if strs:
+            sv, sm = _matrix(bc[strs[0]])
+        else:                  # no stress specification: no stress component prescribed
+            strs = ["P"]
+            sv, sm = np.zeros((3, 3)), np.ones((3, 3), dtype=int)
         disc = item["discretization"]
         rot = bc.get("R", (1.0, 0.0, 0.0, 0.0))
         steps.append(make_step(defs[0], dv, dm, strs[0], sv, sm, disc["t"], disc["N"], r=disc.get("r", 1.0),

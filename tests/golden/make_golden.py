@@ -1,5 +1,9 @@
 """Extract the reference's known-answer vectors into tests/golden/reference_knowns.json.
 
+Also stored as text: the example inputs of examples/grid (load cases, material.yaml,
+numerics.yaml) and the geometry and material.yaml of the 6-grain result in
+python/tests/resources/Result, used as input-format test cases.
+
 Reads the reference's own GoogleTest sources as text (the Eigen ``setValues`` literals and
 scalar expectations) and writes them out as JSON, keeping each value exactly as printed.
 Run in a checkout that has the reference tree:
@@ -106,6 +110,12 @@ def main(ref):
     m = re.search(r'vti_file_content = \(R""""\((.*?)\)""""\);', dg, re.S)
     out["vti_16x16x16"] = {"content": m.group(1), "cells": [16, 16, 16], "size": [1, 1, 1],
                            "origin": [0, 0, 0]}
+    ex = os.path.join(ref, "examples", "grid")
+    out["examples_grid"] = {n: open(os.path.join(ex, n)).read()
+                            for n in ("tensionX.yaml", "shearXY.yaml", "shearZX.yaml", "material.yaml", "numerics.yaml")}
+    res = os.path.join(ref, "python", "tests", "resources", "Result")
+    out["material_yaml_6grains"] = open(os.path.join(res, "6grains6x7x8_single_phase.material.yaml")).read()
+    out["vti_6grains"] = open(os.path.join(res, "6grains6x7x8_single_phase.vti")).read()
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_knowns.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1)

@@ -21,6 +21,13 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
+def knowns():
+    import json
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_knowns.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="module")
 def gpu():
     import solver_cpp_gb300 as g
     from solver_cpp_gb300 import build
@@ -88,3 +95,31 @@ def test_restart_continues_bitwise(gpu, tmp_path):
         assert a["iterations"] == b["iterations"]
     for key in ("F", "P", "Fp", "xi"):
         assert np.array_equal(cont.get(key), full.get(key)), key
+
+
+TENSION_Y = """solver:
+  mechanical: spectral_basic
+loadstep:
+  - boundary_conditions:
+      mechanical:
+        dot_F: [[x, 0, 0], [0, 1.0e-3, 0], [0, 0, x]]
+        P: [[0, x, x], [x, x, x], [x, x, 0]]
+    discretization: {t: 20, N: 40}
+    f_out: 4
+"""
+
+
+def test_grid_job_from_input_files(gpu, tmp_path, knowns):
+    """DAMASK_grid-style job from the 6-grain geometry (VTI) and material.yaml of the
+    Fortran run: averages equal the Fortran result; inputs stored under /setup."""
+    from solver_cpp_gb300.inputs import grid_job
+    fx = cases.damask_6grains()
+    path = tmp_path / "job.hdf5"
+    rve, recs = grid_job(knowns["vti_6grains"], knowns["material_yaml_6grains"], TENSION_Y, result=path)
+    assert len(recs) == 40
+    for k, inc in enumerate(fx["increments"]):
+        if inc:
+            assert rel(recs[inc - 1]["P_av"], fx["P_av"][k]) < 1e-9
+    f = HDF5File(str(path))
+    assert sorted(f.keys("/setup")) == ["geometry.vti", "load.yaml", "material.yaml"]
+    assert f.read("/setup/load.yaml").item().rstrip(b"\0").decode() == TENSION_Y

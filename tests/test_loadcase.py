@@ -1,34 +1,15 @@
 """Host-side input parsing (load case and numerics YAML of the reference)."""
 import numpy as np
 
-TENSION_X = """
----
+def _examples():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_knowns.json")) as f:
+        return json.load(f)["examples_grid"]
 
-solver:
-  mechanical: spectral_basic
 
-loadstep:
-  - boundary_conditions:
-      mechanical:
-        dot_F: [[1.0e-3, 0, 0],
-                [0,      x, 0],
-                [0,      0, x]]
-        P: [[x, x, x],
-            [x, 0, x],
-            [x, x, 0]]
-    discretization:
-      t: 5
-      N: 10
-    f_out: 4
-"""
-
-NUMERICS = """
-solver:
-  grid:
-    mechanical:
-      N_iter_min: 4
-      N_iter_max: 40
-"""
+TENSION_X = _examples()["tensionX.yaml"]
+NUMERICS = _examples()["numerics.yaml"]
 
 
 def test_parse_load_yaml_tensionX():

@@ -119,3 +119,21 @@ def test_fft_round_trip_and_numpy():
         assert np.allclose(spec, np.transpose(ref, (1, 0, 2, 3)), atol=1e-10, rtol=1e-12)
         back = dgo.fft_c2r(cells, spec).reshape(N2, N1, N0, 9) / (N0 * N1 * N2)
         assert np.allclose(back, f, atol=1e-12, rtol=0)
+
+
+def test_update_coords_identity(knowns):
+    """MechBaseTestUpdateCoords (test_mech_base.cpp): F = I on 2x1x1 cells of 1e-5."""
+    k = knowns["update_coords_2x1x1_identity"]
+    cells, geom = [2, 1, 1], [2e-5, 1e-5, 1e-5]
+    F9 = dgo.fortran9(np.tile(np.eye(3), (2, 1, 1)))
+    un, up = dgo.update_coords(cells, geom, F9)
+    x_n = np.array(k["x_n"])          # [p][i][j][k]
+    x_p = np.array(k["x_p"])
+    step = np.array(geom) / np.array(cells)
+    for i in range(3):
+        for j in range(2):
+            for kk in range(2):
+                node = i + 3 * (j + 2 * kk)
+                assert np.allclose(un[node] + step * [i, j, kk], x_n[:, i, j, kk], rtol=0, atol=1e-20)
+    for i in range(2):
+        assert np.allclose(up[i] + step * (np.array([i, 0, 0]) + 0.5), x_p[:, i, 0, 0], rtol=0, atol=1e-20)
