@@ -204,7 +204,7 @@ def batch_leg(g, torch, n_rves, increments, seconds, compare):
     pop = batch_population(n_rves)
     mixed = g.numerics(precision="mixed")
     steps = {k: [g.load_step(k, t=float(increments), N=increments)] for k in BATCH_KINDS}
-    batch = g.Batch(n_rves, cons_block=256)
+    batch = g.Batch(n_rves)
     rves = []
     for cells, ng, kind, mat, q in pop:
         r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=mixed)
@@ -228,7 +228,7 @@ def batch_leg(g, torch, n_rves, increments, seconds, compare):
            "seconds": ms * 1e-3, "all_done": not active,
            "constitutive_share": (s1["constitutive_ms"] - s0["constitutive_ms"]) / ms,
            "spectral_share": (s1["spectral_ms"] - s0["spectral_ms"]) / ms,
-           "launches": s1["launches"] - s0["launches"]}
+           "launches": s1["launches"] - s0["launches"], "autotuned": batch.tuning()}
     batch.close()
     for r, _, _ in rves:
         r.close()
@@ -251,7 +251,7 @@ def batch_leg(g, torch, n_rves, increments, seconds, compare):
             r.close()
         # same dt (1 s) as the population's load case, `inc` increments
         steps3 = {k: [g.load_step(k, t=float(inc), N=inc)] for k in BATCH_KINDS}
-        b2 = g.Batch(len(sub), cons_block=256)
+        b2 = g.Batch(len(sub))
         members = []
         for cells, ng, kind, mat, q in sub:
             r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=mixed)
@@ -297,7 +297,7 @@ def serve_leg(g, precision, rate, n_requests, seconds, seed=5000):
         mat, q = synthetic.microstructure((c, c, c), ng, seed + k)
         reqs.append(((c, c, c), mat, q, [g.load_step(kind, t=float(n_inc), N=n_inc)]))
     num = g.numerics(precision=precision)
-    srv = g.Server(max_active=64, cons_block=256)
+    srv = g.Server(max_active=64)
     ids, t0 = [], time.perf_counter()
     due = t0
     for gap, (cells, mat, q, steps) in zip(gaps, reqs):

@@ -209,7 +209,9 @@ void* dgx_rve_stream(const dgx_rve* rve);
  * single-RVE calls until it is removed. */
 typedef struct dgx_batch dgx_batch;
 /* capacity: most members at once; cons_block: points per constitutive block (64,
- * 128 or 256; other values mean 128) */
+ * 128 or 256), or 0 to let the batch's autotuner pick it from the first rounds (it
+ * also picks each grid's FFT tile shape; DGX_AUTOTUNE=0 turns both off).  Results do
+ * not depend on these choices. */
 dgx_status dgx_batch_create(int32_t capacity, int32_t cons_block, dgx_batch** out);
 void dgx_batch_destroy(dgx_batch* batch);
 /* Add an RVE that runs the load case steps[0..nsteps) from solver init (as
@@ -232,6 +234,9 @@ dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
  * [7] d2h bytes of the executor. */
 dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[8]);
 void* dgx_batch_stream(const dgx_batch* batch);
+/* autotuner state: [0] constitutive points per block (0 while still tuning), [1] grids
+ * with a chosen FFT tile shape, [2] block size still being tuned, [3] tile tuning on */
+dgx_status dgx_batch_tuning(const dgx_batch* batch, int32_t out[4]);
 
 /* ---- Serving (no counterpart in the reference).  A server owns one worker thread, the
  * device and a dgx_batch.  Requests from any thread are queued; in arrival order a

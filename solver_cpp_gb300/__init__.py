@@ -249,7 +249,7 @@ class Batch:
     all members are done.  Members can be added between rounds.
     """
 
-    def __init__(self, capacity, cons_block=128):
+    def __init__(self, capacity, cons_block=0):
         h = C.c_void_p()
         _d.check(_d.lib().dgx_batch_create(int(capacity), int(cons_block), C.byref(h)), "dgx_batch_create")
         self.h = h
@@ -307,6 +307,11 @@ class Batch:
                     lp_iterations=a[2], rounds=a[3], launches=a[4], jacobians=a[5], h2d_bytes=a[6],
                     d2h_bytes=a[7])
 
+    def tuning(self):
+        a = (C.c_int32 * 4)()
+        _d.check(_d.lib().dgx_batch_tuning(self.h, a), "dgx_batch_tuning")
+        return dict(cons_block=a[0], tuned_grids=a[1], tuning_block=bool(a[2]), tuning_tiles=bool(a[3]))
+
     @property
     def stream(self):
         return int(_d.lib().dgx_batch_stream(self.h) or 0)
@@ -332,7 +337,7 @@ class Server:
 
     STATES = ("queued", "running", "done", "failed")
 
-    def __init__(self, hbm_budget_bytes=0, max_active=64, cons_block=128):
+    def __init__(self, hbm_budget_bytes=0, max_active=64, cons_block=0):
         h = C.c_void_p()
         _d.check(_d.lib().dgx_server_create(int(hbm_budget_bytes), int(max_active), int(cons_block), C.byref(h)),
                  "dgx_server_create")

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -114,6 +115,16 @@ struct Executor {
   ConsCounters* cnt = nullptr;
   bool own_cnt = false;
   int cons_block = 128, resident = 0;
+  // autotuner: constitutive points per block, chosen online from the cost per counted
+  // FP64 flop of the first rounds (each candidate twice), and per grid the FFT tile
+  // shape, timed on the first round's own data (results do not depend on either)
+  bool tune_cons = true, tune_spec = true;
+  int res_by_block[3] = {0, 0, 0};
+  double cons_cost[3] = {0, 0, 0};
+  int cons_trials[3] = {0, 0, 0}, cons_round = 0;
+  ConsCounters cnt_last{};
+  ConsCounters* h_cnt = nullptr;
+  std::map<std::tuple<int, int, int, double, double, double, int, int, int>, SpecLaunch> spec_tuned;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double t_ms[3] = {0, 0, 0};
   int64_t t_n[3] = {0, 0, 0};
@@ -146,7 +157,7 @@ static dgx_status ex_alloc(Executor* e, T** d, T** h, size_t n) {
 dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons_block, Executor** out) {
   Executor* e = new Executor();
   e->st = st; e->cap = cap;
-  e->cons_block = (cons_block == 64 || cons_block == 256) ? cons_block : 128;
+  e->cons_block = (cons_block == 64 || cons_block == 256) ? cons_block : 128;   // <= 0: autotuned
   dgx_status s = DGX_OK;
 #define EA(d, h, n) do { s = ex_alloc(e, d, h, n); if (s != DGX_OK) { executor_destroy(e); return s; } } while (0)
   EA(&e->d_cons, &e->h_cons, cap);
@@ -158,11 +169,19 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   EA(&e->d_rms, &e->h_rms, cap);
   EA(&e->d_mout, &e->h_mout, 64 * 2 * cap);
   EA(&e->d_queue, (unsigned long long**)nullptr, 16);
+  EA((ConsCounters**)nullptr, &e->h_cnt, 1);
   if (cnt) e->cnt = cnt;
   else { EA(&e->cnt, (ConsCounters**)nullptr, 1); e->own_cnt = true; cudaMemset(e->cnt, 0, sizeof(ConsCounters)); }
 #undef EA
   for (auto& v : e->ev) cudaEventCreate(&v);
+  for (int k = 0; k < 3; ++k) e->res_by_block[k] = constitutive_batch_resident(64 << k);
   e->resident = constitutive_batch_resident(e->cons_block);
+  const char* at = std::getenv("DGX_AUTOTUNE");
+  const bool tune = !(at && at[0] == '0');
+  e->tune_cons = tune && cons_block <= 0;       // an explicit block size is kept
+  e->tune_spec = tune;
+  if (cudaMemcpyAsync(&e->cnt_last, e->cnt, sizeof(ConsCounters), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) { executor_destroy(e); set_err("executor: counters"); return DGX_ERR_CUDA; }
   *out = e;
   return DGX_OK;
 }
@@ -190,6 +209,49 @@ static GridKey grid_key(const dgx_rve* r) {
                  r->num.derivative, r->num.divergence_correction);
 }
 
+// FFT tile shape of a grid: the tuned one, or (first time, when tuning) the fastest
+// of the default and its halved / doubled x-line, y-tile and z-tile counts, each timed
+// on this group's own convolution (every candidate computes the same result)
+static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0, const SpecItem* items, int cnt,
+                                    const GammaArgs& ga) {
+  auto it = e->spec_tuned.find(key);
+  if (it != e->spec_tuned.end()) return it->second;
+  const SpecLaunch& base = r0->sl;
+  if (!e->tune_spec) return e->spec_tuned.emplace(key, base).first->second;
+  const bool fp32 = r0->num.precision == 1;
+  const size_t cs = fp32 ? sizeof(float2) : sizeof(double2);
+  const SpecGeom& g = base.g;
+  std::vector<SpecLaunch> cands{base};
+  const int f[2] = {2, -2};
+  for (int k = 0; k < 2; ++k) {
+    auto sc = [&](int v) { return f[k] > 0 ? v * 2 : std::max(1, v / 2); };
+    cands.push_back(spec_launch_tiles(g.N0, g.N1, g.N2, cs, sc(base.LX), base.TIy, base.TIz));
+    cands.push_back(spec_launch_tiles(g.N0, g.N1, g.N2, cs, base.LX, sc(base.TIy), base.TIz));
+    cands.push_back(spec_launch_tiles(g.N0, g.N1, g.N2, cs, base.LX, base.TIy, sc(base.TIz)));
+  }
+  int best = 0;
+  float best_ms = 1e30f;
+  for (size_t c = 0; c < cands.size(); ++c) {
+    const SpecLaunch& L = cands[c];
+    bool dup = false;
+    for (size_t d = 0; d < c; ++d)
+      dup |= cands[d].LX == L.LX && cands[d].TIy == L.TIy && cands[d].TIz == L.TIz;
+    if (dup || !spec_launch_fits(L)) continue;
+    spec_prepare(L, fp32);
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e->ev[2], e->st);
+      spec_convolve_batch(L, fp32, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan, items, cnt, ga, e->st);
+      cudaEventRecord(e->ev[3], e->st);
+      cudaEventSynchronize(e->ev[3]);
+      cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]);
+    }
+    e->launches += 10;
+    if (cudaGetLastError() == cudaSuccess && ms < best_ms) { best_ms = ms; best = (int)c; }
+  }
+  return e->spec_tuned.emplace(key, cands[best]).first->second;
+}
+
 // residual evaluations R = Gamma * P(X) of every request (form_residual)
 static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
   const int n = (int)q.size();
@@ -203,7 +265,13 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
     if (c != 0) return c < 0;
     return q[a].r->N > q[b].r->N;
   });
-  const int BS = e->cons_block;
+  int cand = -1;
+  if (e->tune_cons) {
+    cand = e->cons_round % 3;
+    if (e->cons_trials[cand] >= 2) cand = -1;
+  }
+  const int BS = cand >= 0 ? (64 << cand) : e->cons_block;
+  const int resident = cand >= 0 ? e->res_by_block[cand] : e->resident;
   std::vector<int> slot_of(n);
   for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
   CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, e->st));
@@ -234,7 +302,7 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
     int j0 = groups[g].first;
     int j1 = g + 1 < groups.size() ? groups[g + 1].first : n;
     long long tiles = groups[g].second;
-    int grid = (int)std::min<long long>(tiles, e->resident);
+    int grid = (int)std::min<long long>(tiles, resident);
     launch_constitutive_batch(q[order[j0]].r->mp, e->d_cons + j0, j1 - j0, tiles, e->d_queue + g, e->cnt, e->st, BS,
                               std::max(grid, 1));
     e->launches++;
@@ -244,11 +312,29 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
   e->launches++;
   TRY(ex_d2h(e, e->h_Pav, e->d_Pav, sizeof(double) * 9 * n));
   TRY(ex_d2h(e, e->h_ill, e->d_ill, sizeof(int) * n));
+  if (e->tune_cons) TRY(ex_d2h(e, e->h_cnt, e->cnt, sizeof(ConsCounters)));
   CK(cudaStreamSynchronize(e->st));
   CK(cudaGetLastError());
   {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[0] += ms; e->t_n[0]++;
+    if (e->tune_cons) {
+      // cost per counted flop (the constitutive roofline's own flop model)
+      const ConsCounters& c1 = *e->h_cnt;
+      double flops = 724.0 * (double)(c1.lp_iters - e->cnt_last.lp_iters) +
+                     2535.0 * (double)(c1.jac_iters - e->cnt_last.jac_iters) +
+                     1400.0 * (double)(c1.state_iters - e->cnt_last.state_iters);
+      e->cnt_last = c1;
+      if (cand >= 0 && flops > 0.0) { e->cons_cost[cand] += ms / flops; e->cons_trials[cand]++; }
+      e->cons_round++;
+      if (e->cons_trials[0] >= 2 && e->cons_trials[1] >= 2 && e->cons_trials[2] >= 2) {
+        int best = 0;
+        for (int k = 1; k < 3; ++k) if (e->cons_cost[k] < e->cons_cost[best]) best = k;
+        e->cons_block = 64 << best;
+        e->resident = e->res_by_block[best];
+        e->tune_cons = false;
+      }
+    }
   }
   // host BC step of every RVE
   for (int i = 0; i < n; ++i) {
@@ -274,16 +360,27 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
   }
   TRY(ex_h2d(e, e->d_aim, e->h_aim, sizeof(double) * 9 * n));
   TRY(ex_h2d(e, e->d_spec, e->h_spec, sizeof(SpecItem) * n));
+  // tile shapes first (a grid seen for the first time is tuned on its own data)
+  std::vector<const SpecLaunch*> Ls;
+  std::vector<GammaArgs> gas;
+  {
+    size_t gi = 0;
+    for (auto& kv : gg) {
+      dgx_rve* r0 = q[kv.second[0]].r;
+      gas.push_back(gamma_args(r0, true, true));
+      Ls.push_back(&spec_tiles(e, kv.first, r0, e->d_spec + spans[gi].first, spans[gi].second, gas.back()));
+      ++gi;
+    }
+  }
   CK(cudaEventRecord(e->ev[2], e->st));
   {
     size_t gi = 0;
     for (auto& kv : gg) {
       dgx_rve* r0 = q[kv.second[0]].r;
-      GammaArgs ga = gamma_args(r0, true, true);
       const int o = spans[gi].first, cnt = spans[gi].second;
-      spec_convolve_batch(r0->sl, r0->num.precision == 1, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan, e->d_spec + o,
-                          cnt, ga, e->st);
-      spec_div_finish_batch(e->d_spec + o, cnt, r0->sl.nbz, r0->wgt, r0->cells[0], e->st);
+      spec_convolve_batch(*Ls[gi], r0->num.precision == 1, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan,
+                          e->d_spec + o, cnt, gas[gi], e->st);
+      spec_div_finish_batch(e->d_spec + o, cnt, r0->sl.ndiv, r0->wgt, r0->cells[0], e->st);
       e->launches += 6;
       ++gi;
     }
@@ -627,7 +724,7 @@ static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks) {
 
 static dgx_status ensure_executor(dgx_rve* r) {
   if (r->ex) return DGX_OK;
-  return executor_create(1, r->st, r->d_cnt, r->cons_block, &r->ex);
+  return executor_create(1, r->st, r->d_cnt, r->cons_block_forced ? r->cons_block : 0, &r->ex);
 }
 
 // a solve (mode 0), one increment (mode 1) or a load case (mode 2) of one RVE as a batch of one
@@ -773,3 +870,13 @@ extern "C" dgx_status dgx_batch_stats(const dgx_batch* b, double ms[3], int64_t 
 }
 
 extern "C" void* dgx_batch_stream(const dgx_batch* b) { return b ? (void*)b->st : nullptr; }
+
+extern "C" dgx_status dgx_batch_tuning(const dgx_batch* b, int32_t out[4]) {
+  if (!b || !out) return DGX_ERR_ARG;
+  const Executor* e = b->ex;
+  out[0] = e->tune_cons ? 0 : e->cons_block;
+  out[1] = (int32_t)e->spec_tuned.size();
+  out[2] = e->tune_cons ? 1 : 0;
+  out[3] = e->tune_spec ? 1 : 0;
+  return DGX_OK;
+}

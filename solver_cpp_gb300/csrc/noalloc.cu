@@ -35,7 +35,7 @@ constexpr long long OFF_SPEC = OFF_PLANAR + 9 * MAXC; // <= 9 * MAXC complex
 constexpr long long OFF_TW = OFF_SPEC + 18 * MAXC;    // twiddles: 2 doubles + 1 float2 per entry
 constexpr long long TW_LEN = MAXC + 64;               // per-axis capacity (entries)
 constexpr long long OFF_XI = OFF_TW + 3 * 3 * TW_LEN; // xi_x, xi_y, xi_z
-constexpr long long OFF_PART = OFF_XI + 3 * TW_LEN;   // z-pass partials
+constexpr long long OFF_PART = OFF_XI + 3 * TW_LEN;   // divergence partials, N0r * N1 <= MAXC
 constexpr long long SCRATCH_DOUBLES = OFF_PART + MAXC + 64;
 
 static __device__ __align__(256) double g_scratch[SCRATCH_DOUBLES];
@@ -105,7 +105,6 @@ extern "C" dgx_status dgx_divergence_rms_static(const int32_t cells[3], const do
   dgx::SpecLaunch L = dgx::spec_launch(cells[0], cells[1], cells[2], sizeof(double2));
   const size_t SMEM_MAX = 227 * 1024;                  // one line tile per pass must fit shared memory
   if (L.smx > SMEM_MAX || L.smy > SMEM_MAX || L.smz > SMEM_MAX) return DGX_ERR_UNSUPPORTED;
-  if (L.nbz > MAXC) return DGX_ERR_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return DGX_ERR_CUDA;
   if (!g_scratch_ptr[dev]) {
@@ -150,6 +149,6 @@ extern "C" dgx_status dgx_divergence_rms_static(const int32_t cells[3], const do
   ga.do_gamma = 0; ga.do_div = 1; ga.store_fwd = 0;
   ga.div_part = base + OFF_PART;
   dgx::spec_convolve(L, false, plan[0], plan[1], plan[2], planes, planes, N, spec, ga, st);
-  dgx::spec_div_finish(ga.div_part, L.nbz, std::pow((double)N, -1.0), cells[0], rms_device, st);
+  dgx::spec_div_finish(ga.div_part, L.ndiv, std::pow((double)N, -1.0), cells[0], rms_device, st);
   return cudaGetLastError() == cudaSuccess ? DGX_OK : DGX_ERR_CUDA;
 }

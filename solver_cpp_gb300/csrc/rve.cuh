@@ -45,7 +45,8 @@ struct dgx_rve {
   dgx::AxisHost ax[3];
   dgx::SpecLaunch sl{};
   int nb_cons = 0, nb_tan = 0, nb_red = 0;
-  int cons_block = 128;
+  int cons_block = 128;            // direct (unbatched) constitutive launches
+  bool cons_block_forced = false;  // DGX_CONS_BLOCK set: the executor keeps it (no autotuning)
   // host solver state (MechBase / MechSolverBasic members)
   double F_aim[9], F_aim_last_inc[9], F_aim_dot[9], P_aim[9], P_av[9];
   double C_volAvg[81], C_minMaxAvg[81], C_volAvgLastInc[81], C_minMaxAvgLastInc[81], C_ref[81], S[81];

@@ -635,12 +635,13 @@ static dgx_status allocate_buffers(dgx_rve* r, const int32_t cells[3], const dgx
     const char* env = std::getenv("DGX_CONS_BLOCK");
     int b = env ? std::atoi(env) : 128;
     r->cons_block = (b == 64 || b == 256) ? b : 128;
+    r->cons_block_forced = env != nullptr;
   }
   r->nb_tan = (int)((N + 63) / 64);
   r->nb_red = (int)std::min<int64_t>(608, std::max<int64_t>(1, (9 * N + 1023) / 1024));
   AL(&r->d_Ppart, 9 * (int64_t)r->nb_cons);
   AL(&r->d_tpart, r->nb_tan);
-  AL(&r->d_divpart, r->sl.nbz);
+  AL(&r->d_divpart, r->sl.ndiv);
   AL(&r->d_redpart, 128 * (int64_t)r->nb_red);   // two concurrent fused reductions of up to 64 sums
   AL(&r->d_redout, 128); AL(&r->d_beta, 32);
   AL(&r->d_Pav, 9); AL(&r->d_Cvol, 81); AL(&r->d_Cmm, 81); AL(&r->d_Cref, 81); AL(&r->d_aim, 9); AL(&r->d_rms, 1);
@@ -811,7 +812,7 @@ extern "C" dgx_status dgx_divergence_rms(dgx_rve* r, const double* P, double* rm
   GammaArgs ga = gamma_args(r, false, true);
   spec_convolve(r->sl, r->num.precision == 1, r->ax[0].plan, r->ax[1].plan, r->ax[2].plan, r->XA, r->XA, r->N, r->spec,
                 ga, r->st);
-  spec_div_finish(r->d_divpart, r->sl.nbz, r->wgt, r->cells[0], r->d_rms, r->st);
+  spec_div_finish(r->d_divpart, r->sl.ndiv, r->wgt, r->cells[0], r->d_rms, r->st);
   r->n_launch += 4;
   CK(d2h(r, rms, r->d_rms, sizeof(double)));
   CK(cudaStreamSynchronize(r->st));

@@ -207,8 +207,8 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
   const int per = TI * g.N2;                       // lines x length per component
   C* a = reinterpret_cast<C*>(smem_raw);
   C* b = a + 9L * per;
+  double* s_val = reinterpret_cast<double*>(b + 9L * per);   // weighted |div|^2 per frequency of the tile
   __shared__ double s_C[81];
-  __shared__ double s_red[256];
   const int ntile = (g.N0r + TI - 1) / TI;
   const int tile = blockIdx.x % ntile;
   const int y = blockIdx.x / ntile;
@@ -225,7 +225,6 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
   __syncthreads();
   C* res = block_fft<R>(a, b, 9 * ti, pz, (ga.store_fwd && !ga.do_gamma && ga.zsign > 0) ? +1 : -1);
   C* other = (res == a) ? b : a;
-  double dsum = 0.0;
   for (int t = threadIdx.x; (ga.do_div || ga.do_gamma) && t < ti * g.N2; t += blockDim.x) {
     int i = t / g.N2, z = t - i * g.N2;
     int ix = i0 + i;
@@ -243,7 +242,7 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
         double ui = (double)Ph[l].y * bx + (double)Ph[l + 3].y * by + (double)Ph[l + 6].y * bz;
         s += ur * ur + ui * ui;
       }
-      dsum += wgt * s;
+      s_val[t] = wgt * s;
     }
     if (ga.do_gamma) {
       C out[9];
@@ -295,13 +294,16 @@ __global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict_
     }
   }
   if (ga.do_div) {
-    s_red[threadIdx.x] = dsum;
+    // one partial per frequency line (x-frequency i, y): the z sum in a fixed order that
+    // does not depend on the tile shape, so tile choices never change the result
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) s_red[threadIdx.x] += s_red[threadIdx.x + s];
-      __syncthreads();
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int line = threadIdx.x >> 5; line < ti; line += nw) {
+      double v = 0.0;
+      for (int z = lane; z < g.N2; z += 32) v += s_val[line * g.N2 + z];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) ga.div_part[(long long)y * g.N0r + i0 + line] = v;
     }
-    if (threadIdx.x == 0) ga.div_part[blockIdx.x] = s_red[0];
   }
   if (!ga.do_gamma) {
     if (ga.store_fwd)
@@ -497,26 +499,38 @@ void axis_destroy(AxisHost* ax) {
 }
 
 
-SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize) {
+SpecLaunch spec_launch_tiles(int N0, int N1, int N2, size_t csize, int LX, int TIy, int TIz) {
   SpecLaunch L;
   L.g.N0 = N0; L.g.N1 = N1; L.g.N2 = N2; L.g.N0r = N0 / 2 + 1;
   L.g.N = (long long)N0 * N1 * N2;
   L.g.Nh = (long long)L.g.N0r * N1 * N2;
-  L.LX = N0 >= 256 ? 1 : 256 / N0;
-  L.TIy = N1 >= 256 ? 1 : 256 / N1;
-  if (L.TIy > L.g.N0r) L.TIy = L.g.N0r;
-  L.TIz = N2 >= 256 ? 1 : 256 / N2;
-  if (L.TIz > L.g.N0r) L.TIz = L.g.N0r;
-  // keep the z-pass tile within 200 KB of shared memory (9 components x 2 buffers)
-  while (L.TIz > 1 && 2 * 9 * (size_t)L.TIz * N2 * csize > 200 * 1024) L.TIz /= 2;
+  L.LX = std::max(1, LX);
+  L.TIy = std::max(1, std::min(TIy, L.g.N0r));
+  L.TIz = std::max(1, std::min(TIz, L.g.N0r));
   L.smx = 2 * (size_t)L.LX * N0 * csize;
   L.smy = 2 * (size_t)L.TIy * N1 * csize;
-  L.smz = 2 * 9 * (size_t)L.TIz * N2 * csize;
+  L.smz = 2 * 9 * (size_t)L.TIz * N2 * csize + (size_t)L.TIz * N2 * sizeof(double);
   long long nlines = 9LL * N1 * N2;
   L.nbx = (int)((nlines + L.LX - 1) / L.LX);
   L.nby = ((L.g.N0r + L.TIy - 1) / L.TIy) * 9 * N2;
   L.nbz = ((L.g.N0r + L.TIz - 1) / L.TIz) * N1;
+  L.ndiv = L.g.N0r * N1;
   return L;
+}
+
+bool spec_launch_fits(const SpecLaunch& L) {
+  const size_t mx = 227 * 1024;
+  return L.smx <= mx && L.smy <= mx && L.smz <= mx;
+}
+
+SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize) {
+  int LX = N0 >= 256 ? 1 : 256 / N0;
+  int TIy = N1 >= 256 ? 1 : 256 / N1;
+  int TIz = N2 >= 256 ? 1 : 256 / N2;
+  TIz = std::min(TIz, N0 / 2 + 1);
+  // keep the z-pass tile within 200 KB of shared memory (9 components x 2 buffers)
+  while (TIz > 1 && (2 * 9 * (size_t)TIz * N2 * csize + (size_t)TIz * N2 * 8) > 200 * 1024) TIz /= 2;
+  return spec_launch_tiles(N0, N1, N2, csize, LX, TIy, TIz);
 }
 
 // The dynamic shared-memory limit is a property of the kernel, shared by every

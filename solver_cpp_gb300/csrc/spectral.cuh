@@ -28,9 +28,10 @@ struct SpecGeom {
 // launch configuration shared by the spectral kernels
 struct SpecLaunch {
   SpecGeom g;
-  int LX, TIy, TIz;
+  int LX, TIy, TIz;       // x lines per block; x-frequencies per y / z block
   size_t smx, smy, smz;
   int nbx, nby, nbz;
+  int ndiv;               // divergence partials: one per (x-frequency, y) line = N0r * N1
 };
 
 struct GammaArgs {
@@ -43,7 +44,7 @@ struct GammaArgs {
   int do_gamma, do_div;
   int store_fwd;          // without gamma: write the z transform back (forward, or inverse if zsign > 0)
   int zsign;              // with store_fwd: -1 forward (default 0 means forward), +1 inverse
-  double* div_part;       // per block partial of the divergence sum (FP64)
+  double* div_part;       // N0r * N1 partials of the divergence sum, one per frequency line (FP64)
 };
 
 // one RVE of a size-grouped batched convolution (selected by blockIdx.y)
@@ -53,7 +54,7 @@ struct SpecItem {
   void* spec;             // 9 Nh complex (FP64 or FP32)
   const double* C_ref;    // 81
   const double* aim;      // 9, zero-frequency value
-  double* div_part;       // nbz partials of the divergence sum
+  double* div_part;       // ndiv partials of the divergence sum
   double* rms;            // divergence RMS out
 };
 
@@ -64,6 +65,9 @@ int factorize(int n, int* rad);
 bool axis_create(AxisHost* ax, int n);
 void axis_destroy(AxisHost* ax);
 SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize);
+// explicit tile shape (autotuner); spec_launch_fits: shared memory within the limit
+SpecLaunch spec_launch_tiles(int N0, int N1, int N2, size_t csize, int LX, int TIy, int TIz);
+bool spec_launch_fits(const SpecLaunch& L);
 void spec_prepare(const SpecLaunch& L, bool fp32);
 void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                    const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st);

@@ -96,3 +96,22 @@ def test_batch_capacity_and_state_errors(gpu):
     batch.remove(0)
     a.loop_over_loadcase(sa)                 # back on its own stream
     batch.close()
+
+
+def test_autotuned_tiles_and_blocks_do_not_change_results(gpu, monkeypatch):
+    """The autotuner picks points per block and FFT tiles; results are identical to
+    a fixed configuration (DGX_AUTOTUNE=0, 64 points per block)."""
+    monkeypatch.setenv("DGX_AUTOTUNE", "0")
+    monkeypatch.setenv("DGX_CONS_BLOCK", "64")
+    fixed, steps = _make(gpu, CASES[1], N=6)
+    ref = fixed.loop_over_loadcase(steps)
+    monkeypatch.delenv("DGX_AUTOTUNE")
+    monkeypatch.delenv("DGX_CONS_BLOCK")
+    batch = gpu.Batch(2)
+    tuned, steps2 = _make(gpu, CASES[1], N=6)
+    slot = batch.add(tuned, steps2)
+    batch.run()
+    t = batch.tuning()
+    assert t["tuned_grids"] >= 1 and not t["tuning_block"] and t["cons_block"] in (64, 128, 256)
+    _same(batch.records(slot), ref)
+    batch.close()
