@@ -39,11 +39,6 @@ METRIC = "point-updates/s, mixed vs FP64 GPU at ≤1e-5 rel. P error; p50/p99 RV
 UNIT = "point-updates/s"
 SEED = 42
 
-# algorithmic FP64 flops of the constitutive kernel's restatement (FMA = 2), per unit:
-#   every Lp iteration (B, Fe, Hooke S, 12-system kinetics, Lp, residual norms)   724
-#   every Lp Jacobian + 9x9 LU solve (rank-12 J: 12 x (WQ_a + 6x9 FMA), LU)       2535
-#   every state iteration (dotState, damper, state update, stress-call overhead)   1400
-FLOPS_LP, FLOPS_JAC, FLOPS_STATE = 724.0, 2535.0, 1400.0
 # DRAM traffic of one constitutive launch per cell, from the ncu capture summarised in
 # profiles/constitutive_64cube.md (dram__bytes_read.sum + dram__bytes_write.sum / cells)
 TRAFFIC_BYTES_PER_CELL = None
@@ -395,7 +390,9 @@ def gpu_arm(a):
     d_st = c1["state_iterations"] - c0["state_iterations"]
     launches = t1["constitutive_launches"] - t0["constitutive_launches"]
     kms = t1["constitutive_ms"] - t0["constitutive_ms"]
-    flops = FLOPS_LP * d_lp + FLOPS_JAC * d_jac + FLOPS_STATE * d_st
+    d_fpi = c1["fpi_iterations"] - c0["fpi_iterations"]
+    fm = g.flop_model()          # algorithmic FP64 flops per counted unit (FMA = 2), from the library
+    flops = fm["lp"] * d_lp + fm["jacobian"] * d_jac + fm["state"] * d_st + fm["fpi"] * d_fpi
     achieved = flops / (kms * 1e-3) / 1e12 if kms > 0 else 0.0
     traffic = TRAFFIC_BYTES_PER_CELL * n if TRAFFIC_BYTES_PER_CELL else None
     spec_ms = t1["spectral_ms"] - t0["spectral_ms"]
@@ -407,6 +404,9 @@ def gpu_arm(a):
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                          "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
                          "kernel": "k_constitutive", "flops_per_launch": flops / max(1, launches),
+                         "units_per_evaluation": {k: v / max(1, evals * n) for k, v in
+                                                  (("lp", d_lp), ("jacobian", d_jac), ("state", d_st),
+                                                   ("fpi", d_fpi))},
                          "ms_per_launch": kms / max(1, launches),
                          "peak_source": "measured: dgx_measure_fp64_peak DFMA probe (MEASURED_PEAKS.json has no FP64)"},
             "kernel_time_share": {"constitutive": kms / ms, "spectral": spec_ms / ms,

@@ -187,11 +187,16 @@ dgx_status dgx_restart_read(dgx_rve* rve, const char* path);
  * "C_ref", "S_compliance". */
 dgx_status dgx_get(dgx_rve* rve, const char* name, double* out);
 
-/* Work counters since creation: [0] residual evaluations, [1] constitutive
- * state (FPI) iterations, [2] Lp Newton iterations, [3] tangent evaluations,
+/* Work counters since creation: [0] residual evaluations, [1] constitutive state
+ * integrations (sub-steps), [2] Lp Newton iterations, [3] tangent evaluations,
  * [4] kernel launches issued by the library, [5] Lp Jacobian factorisations,
- * [6] host-to-device bytes, [7] device-to-host bytes copied by the library. */
-dgx_status dgx_counters(const dgx_rve* rve, int64_t out[8]);
+ * [6] host-to-device bytes, [7] device-to-host bytes copied by the library,
+ * [8] fixed-point state iterations, [9] reserved. */
+dgx_status dgx_counters(const dgx_rve* rve, int64_t out[10]);
+/* FP64 flops per counted unit of the constitutive kernel (FMA = 2): [0] Lp iteration,
+ * [1] Jacobian, [2] state integration, [3] fixed-point iteration.  No reference
+ * counterpart; the numerator of the kernel's roofline. */
+void dgx_flop_model(double out[4]);
 /* CUDA-event time (ms, accumulated) and launch counts of [0] the constitutive
  * kernel, [1] the spectral chain (FFT + Gamma + div-RMS), [2] the tangent kernel,
  * measured on the RVE's stream. */
@@ -229,10 +234,10 @@ dgx_status dgx_batch_member(const dgx_batch* batch, int32_t slot, int32_t* done,
 /* Detach a finished member: the RVE returns to its own stream and the single-RVE calls. */
 dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
 /* ms: CUDA-event time of [0] constitutive launches, [1] spectral chains, [2] unused;
- * out: [0] point evaluations, [1] state iterations, [2] Lp iterations, [3] rounds,
+ * out: [0] point evaluations, [1] state integrations, [2] Lp iterations, [3] rounds,
  * [4] launches of the batched kernels, [5] Jacobian factorisations, [6] h2d bytes,
- * [7] d2h bytes of the executor. */
-dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[8]);
+ * [7] d2h bytes of the executor, [8] fixed-point iterations, [9] reserved. */
+dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[10]);
 void* dgx_batch_stream(const dgx_batch* batch);
 /* autotuner state: [0] constitutive points per block (0 while still tuning), [1] grids
  * with a chosen FFT tile shape, [2] block size still being tuned, [3] tile tuning on */

@@ -217,10 +217,10 @@ class RVE:
         return _unf9(out, self.N) if width == 9 else out.reshape(self.N, width)
 
     def counters(self):
-        a = (C.c_int64 * 8)()
+        a = (C.c_int64 * 10)()
         _d.check(_d.lib().dgx_counters(self.h, a), "dgx_counters")
         return dict(evaluations=a[0], state_iterations=a[1], lp_iterations=a[2], tangents=a[3], launches=a[4],
-                    jacobians=a[5], h2d_bytes=a[6], d2h_bytes=a[7])
+                    jacobians=a[5], h2d_bytes=a[6], d2h_bytes=a[7], fpi_iterations=a[8])
 
     def timers(self):
         ms = (C.c_double * 3)(); n = (C.c_int64 * 3)()
@@ -301,11 +301,11 @@ class Batch:
         self._keep.pop(slot, None)
 
     def stats(self):
-        ms = (C.c_double * 3)(); a = (C.c_int64 * 8)()
+        ms = (C.c_double * 3)(); a = (C.c_int64 * 10)()
         _d.check(_d.lib().dgx_batch_stats(self.h, ms, a), "dgx_batch_stats")
         return dict(constitutive_ms=ms[0], spectral_ms=ms[1], point_evaluations=a[0], state_iterations=a[1],
                     lp_iterations=a[2], rounds=a[3], launches=a[4], jacobians=a[5], h2d_bytes=a[6],
-                    d2h_bytes=a[7])
+                    d2h_bytes=a[7], fpi_iterations=a[8])
 
     def tuning(self):
         a = (C.c_int32 * 4)()
@@ -315,6 +315,13 @@ class Batch:
     @property
     def stream(self):
         return int(_d.lib().dgx_batch_stream(self.h) or 0)
+
+
+def flop_model():
+    """FP64 flops per counted unit of the constitutive kernel (dgx_flop_model)."""
+    a = (C.c_double * 4)()
+    _d.lib().dgx_flop_model(a)
+    return dict(lp=a[0], jacobian=a[1], state=a[2], fpi=a[3])
 
 
 def footprint(cells, num=None, n_materials=1):

@@ -321,9 +321,10 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
     if (e->tune_cons) {
       // cost per counted flop (the constitutive roofline's own flop model)
       const ConsCounters& c1 = *e->h_cnt;
-      double flops = 724.0 * (double)(c1.lp_iters - e->cnt_last.lp_iters) +
-                     2535.0 * (double)(c1.jac_iters - e->cnt_last.jac_iters) +
-                     1400.0 * (double)(c1.state_iters - e->cnt_last.state_iters);
+      double flops = FLOPS_LP * (double)(c1.lp_iters - e->cnt_last.lp_iters) +
+                     FLOPS_JAC * (double)(c1.jac_iters - e->cnt_last.jac_iters) +
+                     FLOPS_STATE * (double)(c1.state_iters - e->cnt_last.state_iters) +
+                     FLOPS_FPI * (double)(c1.fpi_iters - e->cnt_last.fpi_iters);
       e->cnt_last = c1;
       if (cand >= 0 && flops > 0.0) { e->cons_cost[cand] += ms / flops; e->cons_trials[cand]++; }
       e->cons_round++;
@@ -856,7 +857,7 @@ extern "C" dgx_status dgx_batch_remove(dgx_batch* b, int32_t slot) {
   return DGX_OK;
 }
 
-extern "C" dgx_status dgx_batch_stats(const dgx_batch* b, double ms[3], int64_t out[8]) {
+extern "C" dgx_status dgx_batch_stats(const dgx_batch* b, double ms[3], int64_t out[10]) {
   if (!b) return DGX_ERR_ARG;
   const Executor* e = b->ex;
   if (ms) for (int i = 0; i < 3; ++i) ms[i] = e->t_ms[i];
@@ -865,6 +866,7 @@ extern "C" dgx_status dgx_batch_stats(const dgx_batch* b, double ms[3], int64_t 
     CK(cudaMemcpy(&c, e->cnt, sizeof(c), cudaMemcpyDeviceToHost));
     out[0] = e->point_evals; out[1] = (int64_t)c.state_iters; out[2] = (int64_t)c.lp_iters; out[3] = e->rounds;
     out[4] = e->launches; out[5] = (int64_t)c.jac_iters; out[6] = e->bytes_h2d; out[7] = e->bytes_d2h;
+    out[8] = (int64_t)c.fpi_iters; out[9] = 0;
   }
   return DGX_OK;
 }

@@ -74,6 +74,10 @@ __device__ __forceinline__ double nrm9(const double* a) {
 
 // x^(n-1) for small integer n by binary powering, x^(q/4) via square roots
 __device__ __forceinline__ double pow_nm1(double x, const MatParams& mp) {
+  if (mp.n_int == 20) {                      // x^19 = x^16 x^2 x (the configurations' n)
+    double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8;
+    return x16 * (x2 * x);
+  }
   if (mp.n_int > 0) {
     int e = mp.n_int - 1;
     double r = 1.0, b = x;
@@ -140,11 +144,17 @@ __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, c
 }
 
 // phenopowerlaw dotState: [dot xi (12), |gdot| (12)]
-__device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, double* dot) {
-  double rxi[NSLIP], g[NSLIP];
+// gdot: the slip rates of S if already known (the last Lp iteration evaluated them
+// for the same S and xi), else null
+__device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, const double* rxi,
+                                          double* dot, const double* gdot = nullptr) {
+  double g[NSLIP];
+  if (gdot) {
 #pragma unroll
-  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / xi[a];
-  kinetics(mp, S, rxi, g, nullptr);
+    for (int a = 0; a < NSLIP; ++a) g[a] = gdot[a];
+  } else {
+    kinetics(mp, S, rxi, g, nullptr);
+  }
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) g[a] = fabs(g[a]);
 #pragma unroll
@@ -159,11 +169,45 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
   }
 }
 
-// LU with partial pivoting of a 9x9 row-major matrix M[r][c], solving M x = b
-// for nrhs right-hand sides stored column by column in B (B[c * 9 + r]).
+// LU with partial pivoting of an NxN row-major matrix M[r][c], solving M x = b in place
+// (one right-hand side).  Returns false for an exactly singular pivot.
+template <int N>
+__device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
+  int piv[N];
+  double rp[N];                                  // reciprocal pivots: one division per pivot
+  for (int k = 0; k < N; ++k) {
+    int p = k;
+    double mx = fabs(M[N * k + k]);
+    for (int i = k + 1; i < N; ++i) {
+      double v = fabs(M[N * i + k]);
+      if (v > mx) { mx = v; p = i; }
+    }
+    piv[k] = p;
+    if (M[N * p + k] == 0.0) return false;
+    if (p != k)
+      for (int j = 0; j < N; ++j) { double t = M[N * k + j]; M[N * k + j] = M[N * p + j]; M[N * p + j] = t; }
+    double r = 1.0 / M[N * k + k];
+    rp[k] = r;
+    for (int i = k + 1; i < N; ++i) {
+      double l = M[N * i + k] * r;
+      M[N * i + k] = l;
+      for (int j = k + 1; j < N; ++j) M[N * i + j] = fma(-l, M[N * k + j], M[N * i + j]);
+    }
+  }
+  for (int k = 0; k < N; ++k) { int p = piv[k]; if (p != k) { double t = x[k]; x[k] = x[p]; x[p] = t; } }
+  for (int i = 1; i < N; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s = fma(-M[N * i + j], x[j], s); x[i] = s; }
+  for (int i = N - 1; i >= 0; --i) {
+    double s = x[i];
+    for (int j = i + 1; j < N; ++j) s = fma(-M[N * i + j], x[j], s);
+    x[i] = s * rp[i];
+  }
+  return true;
+}
+
+// multi-right-hand-side 9x9 form used by the tangent
 __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) {
   int piv[9];
-  double rp[9];                                  // reciprocal pivots: one division per pivot
+  double rp[9];
   for (int k = 0; k < 9; ++k) {
     int p = k;
     double mx = fabs(M[9 * k + k]);
@@ -196,18 +240,12 @@ __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) 
   return true;
 }
 
-// integrateStress with Fi = I.  Returns true if broken.  On success writes
-// P, S, Lp, Fp (regularised), Fe.
-__device__ bool integrate_stress(const MatParams& mp, const double* F, const double* Fp0, double dt,
-                                 const double* xi, double* Lp, double* S, double* P, double* Fp, double* Fe,
-                                 unsigned* lp_iters, unsigned* jac_iters) {
-  double invFp0[9], A[9];
-  if (!inv33(Fp0, invFp0)) return true;
-  mm(F, invFp0, A);
-  double rxi[NSLIP];
-#pragma unroll
-  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / xi[a];
-
+// integrateStress with Fi = I for fixed F and Fp0 (invFp0 = Fp0^-1, A = F invFp0) and
+// slip resistances xi (rxi = 1 / xi).  Returns true if broken.  On success writes P,
+// S, Lp, Fp (regularised), Fe.
+__device__ bool integrate_stress(const MatParams& mp, const double* F, const double* invFp0, const double* A,
+                                 double dt, const double* rxi, double* Lp, double* S, double* P, double* Fp,
+                                 double* Fe, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters) {
   double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
@@ -245,7 +283,11 @@ __device__ bool integrate_stress(const MatParams& mp, const double* F, const dou
     for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nLc2 = fma(Lpc[k], Lpc[k], nLc2); nr2 = fma(res[k], res[k], nr2); }
     double atol2 = fmax(mp.eps_rel_Lp2 * fmax(nLg2, nLc2), mp.eps_abs_Lp2);
     if (isnan(nr2)) return true;
-    if (nr2 < atol2) break;
+    if (nr2 < atol2) {
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) gdot_out[a] = gdot[a];   // slip rates of the final S
+      break;
+    }
     if (it == 1 || nr2 < res_old_n) {
       res_old_n = nr2;
 #pragma unroll
@@ -260,40 +302,68 @@ __device__ bool integrate_stress(const MatParams& mp, const double* F, const dou
     if (jaco % mp.f_update_jacobi_Lp == 0) {
       ++jaco;
       (*jac_iters)++;
-      // J[3k+l][3p+q] = delta + dt |dg_a| P_a(k,l) (W Q_a)(p,q), W = A^T Fe;
-      // P_a(k,l) = pval * s_a(k,l) with compile-time signs s in {-1,0,1}
+      // Jacobian of R(Lp) = Lp - sum_a gdot_a(tau_a(Lp)) P_a:
+      //   J(kl, pq) = delta + sum_r W(p, r) T(kl; r, q),  W = A^T Fe,
+      //   T(kl; r, q) = sum_a dt |dg_a| P_a(k, l) (C : P_a)(r, q).
+      // With P_a = pval s_a (signs in {-1, 0, 1}, compile-time) and the cubic C : P_a
+      // (= (C11 - C12) P_a on the diagonal, C44 (P_a + P_a^T) off it, P_a traceless), T is
+      // a signed sum of c_a = dt pval^2 |dg_a| times C11 - C12 or C44.  Lp and the
+      // residual are traceless, so component (2, 2) is eliminated (x22 = -x00 - x11):
+      // 8 equations (rows kl = 3k + l < 8) in 8 unknowns.
       double W[9];
       mtm(A, Fe_, W);
-      double J[81];
+      double c[NSLIP];
+      const double cdt = dt * mp.pval * mp.pval;
 #pragma unroll
-      for (int k = 0; k < 81; ++k) J[k] = (k % 10) == 0 ? 1.0 : 0.0;
+      for (int a = 0; a < NSLIP; ++a) c[a] = cdt * dg[a];
+      double J[64];
 #pragma unroll
-      for (int a = 0; a < NSLIP; ++a) {
-        double c = (dt * mp.pval) * dg[a];
-        double V[9];
-        mm(W, mp.Q[a], V);
+      for (int kl = 0; kl < 8; ++kl) {
+        const int k = kl / 3, l = kl % 3;
+        double Td[3] = {0.0, 0.0, 0.0}, To[3] = {0.0, 0.0, 0.0};   // T(r, r); T of the pairs (1,2), (0,2), (0,1)
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < NSLIP; ++a) {
+          if (fcc_s(a, k, l) == 0) continue;
+          const double v = fcc_s(a, k, l) > 0 ? c[a] : -c[a];
 #pragma unroll
-          for (int l = 0; l < 3; ++l) {
-            if (fcc_s(a, k, l) == 0) continue;
-            double pc = fcc_s(a, k, l) > 0 ? c : -c;
+          for (int r = 0; r < 3; ++r) {
+            if (fcc_s(a, r, r) > 0) Td[r] += v;
+            else if (fcc_s(a, r, r) < 0) Td[r] -= v;
+          }
 #pragma unroll
-            for (int p = 0; p < 3; ++p)
+          for (int m = 0; m < 3; ++m) {
+            const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
+            const int sg = fcc_s(a, r, q) + fcc_s(a, q, r);
+            if (sg == 1) To[m] += v;
+            else if (sg == -1) To[m] -= v;
+            else if (sg == 2) To[m] = fma(2.0, v, To[m]);
+            else if (sg == -2) To[m] = fma(-2.0, v, To[m]);
+          }
+        }
 #pragma unroll
-              for (int q = 0; q < 3; ++q) J[9 * (3 * k + l) + 3 * p + q] = fma(pc, V[p + 3 * q], J[9 * (3 * k + l) + 3 * p + q]);
+        for (int r = 0; r < 3; ++r) { Td[r] *= mp.C11mC12; To[r] *= mp.C44; }
+        // T as a symmetric 3x3: T(r, r) = Td[r], T(1,2) = To[0], T(0,2) = To[1], T(0,1) = To[2]
+        const double T[9] = {Td[0], To[2], To[1], To[2], Td[1], To[0], To[1], To[0], Td[2]};
+        double M[9];
+        mm(W, T, M);                               // M(p, q) = sum_r W(p, r) T(r, q)
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const int col = 3 * p + q;
+            if (col == 8) continue;
+            double v = M[p + 3 * q];
+            if (col == 0 || col == 4) v -= M[8];   // x22 = -x00 - x11
+            J[8 * kl + col] = (col == kl ? 1.0 : 0.0) + v;
           }
       }
-      double x[9];
+      double x[8];
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
+      for (int kl = 0; kl < 8; ++kl) x[kl] = res[kl / 3 + 3 * (kl % 3)];
+      if (!lu_solve<8>(J, x)) return true;
 #pragma unroll
-        for (int l = 0; l < 3; ++l) x[3 * k + l] = res[k + 3 * l];
-      if (!lu_solve9(J, x, 1)) return true;
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int l = 0; l < 3; ++l) dLp[k + 3 * l] = -x[3 * k + l];
+      for (int kl = 0; kl < 8; ++kl) dLp[kl / 3 + 3 * (kl % 3)] = -x[kl];
+      dLp[8] = x[0] + x[4];
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg[k]);
@@ -307,7 +377,8 @@ __device__ bool integrate_stress(const MatParams& mp, const double* F, const dou
   double dFp = Fp_new[0] * (Fp_new[4] * Fp_new[8] - Fp_new[7] * Fp_new[5])
              - Fp_new[3] * (Fp_new[1] * Fp_new[8] - Fp_new[7] * Fp_new[2])
              + Fp_new[6] * (Fp_new[1] * Fp_new[5] - Fp_new[4] * Fp_new[2]);
-  double rs = 1.0 / pow(dFp, 1.0 / 3.0);
+  // Fp / det(Fp)^(1/3); a non-positive determinant gives NaN as the power would
+  const double rs = dFp > 0.0 ? rcbrt(dFp) : __longlong_as_double(0x7ff8000000000000LL);
 #pragma unroll
   for (int k = 0; k < 9; ++k) { Fp[k] = Fp_new[k] * rs; Lp[k] = Lpg[k]; Fe[k] = t1[k]; }
   return false;
@@ -325,13 +396,20 @@ __device__ __forceinline__ double damper(const double* o0, const double* o1, con
 }
 
 // integrateStateFPI; returns true if broken.  S on entry: stress used for the
-// first dot state (restored committed stress); state in/out.
+// first dot state (restored committed stress); state in/out.  F and Fp0 are fixed for
+// the whole iteration, so Fp0^-1 and F Fp0^-1 are formed once.
 __device__ bool integrate_state(const MatParams& mp, const double* F, const double* Fp0, const double* state0,
                                 double dt, double* state, double* Lp, double* S, double* P, double* Fp,
-                                double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters) {
-  double dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
+                                double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
+                                unsigned* fpi_iters) {
+  double dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP], rxi[NSLIP], gdot[NSLIP];
   (*st_iters)++;
-  dot_state(mp, S, state, dot);
+  double invFp0[9], A[9];
+  if (!inv33(Fp0, invFp0)) return true;
+  mm(F, invFp0, A);
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / state[a];
+  dot_state(mp, S, state, rxi, dot);
 #pragma unroll
   for (int i = 0; i < 2 * NSLIP; ++i) {
     if (isnan(dot[i])) return true;
@@ -342,9 +420,12 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) { last2[i] = it > 1 ? last1[i] : 0.0; last1[i] = dot[i]; }
-    broken = integrate_stress(mp, F, Fp0, dt, state, Lp, S, P, Fp, Fe, lp_iters, jac_iters);
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / state[a];
+    (*fpi_iters)++;
+    broken = integrate_stress(mp, F, invFp0, A, dt, rxi, Lp, S, P, Fp, Fe, gdot, lp_iters, jac_iters);
     if (broken) break;
-    dot_state(mp, S, state, dot);
+    dot_state(mp, S, state, rxi, dot, gdot);
     bool nan = false;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) nan |= isnan(dot[i]);
@@ -375,7 +456,7 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
                                           ConsCounters* cnt, int64_t tile) {
   const int64_t e = tile * BS + threadIdx.x;
   double P[9];
-  unsigned lp_iters = 0, st_iters = 0, jac_iters = 0;
+  unsigned lp_iters = 0, st_iters = 0, jac_iters = 0, fpi_iters = 0;
   bool ok = true;
   if (e < ps.n) {
     double F[9], F0c[9], Fphase0[9], Fp0[9], Lp[9], Lp0[9], S[9], S0[9], state0[2 * NSLIP], state[2 * NSLIP];
@@ -423,7 +504,7 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
         converged = !integrate_state(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &jac_iters,
-                                     &st_iters);
+                                     &st_iters, &fpi_iters);
       }
     }
     ok = converged;
@@ -463,16 +544,18 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
   }
   if (cnt) {
     // per-warp aggregation of the work counters
-    unsigned lp = lp_iters, st = st_iters, jc = jac_iters;
+    unsigned lp = lp_iters, st = st_iters, jc = jac_iters, fp = fpi_iters;
     for (int o = 16; o > 0; o >>= 1) {
       lp += __shfl_down_sync(0xffffffffu, lp, o);
       st += __shfl_down_sync(0xffffffffu, st, o);
       jc += __shfl_down_sync(0xffffffffu, jc, o);
+      fp += __shfl_down_sync(0xffffffffu, fp, o);
     }
     if ((threadIdx.x & 31) == 0) {
       atomicAdd(&cnt->lp_iters, (unsigned long long)lp);
       atomicAdd(&cnt->state_iters, (unsigned long long)st);
       atomicAdd(&cnt->jac_iters, (unsigned long long)jc);
+      atomicAdd(&cnt->fpi_iters, (unsigned long long)fp);
     }
   }
 }

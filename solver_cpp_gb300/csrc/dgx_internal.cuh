@@ -24,6 +24,7 @@ struct MatParams {
   double h[NSLIP][NSLIP];    // slip-slip interaction, h[reacting][acting]
   double xi_inf, h0, n, gdot0, a, c1, c2;
   double C11mC12, C12, C44x2;  // cubic stiffness: C11 - C12, C12, 2 C44
+  double C44;
   double ngdot0, rxi_inf;      // n * gdot0, 1 / xi_inf
   double pval;                 // magnitude of the non-zero Schmid entries (1/sqrt2 * 1/sqrt3)
   double atol_xi, atol_gamma;
@@ -64,8 +65,17 @@ struct TangentPartial {
 
 // Counters of constitutive work (for the FP64 roofline), accumulated per launch.
 struct ConsCounters {
-  unsigned long long state_iters, lp_iters, jac_iters, points;
+  unsigned long long state_iters, lp_iters, jac_iters, points, fpi_iters;
 };
+
+// Algorithmic FP64 flops of the constitutive kernel per counted unit (FMA = 2, division
+// and square root = 1), counted from its arithmetic: one Lp Newton iteration (B, Fe,
+// Hooke, 12-system kinetics with derivatives, Lp, residual and norms), one Jacobian
+// (W, signed-sum T, W T for 8 rows, 8x8 LU with one right-hand side), one state
+// integration call (Fp0^-1, F Fp0^-1, 1/xi, first dot state, predictor) and one
+// fixed-point iteration (1/xi, stress epilogue: Fp^-1, P, det, Fp scaling; hardening
+// from the slip rates of the last Lp iteration; damper; state update).
+constexpr double FLOPS_LP = 537.0, FLOPS_JAC = 1184.0, FLOPS_STATE = 783.0, FLOPS_FPI = 1060.0;
 
 // One RVE of a batched constitutive launch (device table, ordered by tile0).
 struct ConsItem {

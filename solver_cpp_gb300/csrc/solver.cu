@@ -374,7 +374,7 @@ MatParams make_params(const dgx_material& m) {
   p.N_iter_state_max = m.N_iter_state_max; p.N_iter_Lp_max = m.N_iter_Lp_max;
   p.f_update_jacobi_Lp = m.f_update_jacobi_Lp < 1 ? 1 : m.f_update_jacobi_Lp;
   p.n_int = (m.n == std::floor(m.n) && m.n >= 1 && m.n <= 64) ? (int)m.n : -1;
-  p.C11mC12 = m.C11 - m.C12; p.C12 = m.C12; p.C44x2 = 2.0 * m.C44;
+  p.C11mC12 = m.C11 - m.C12; p.C12 = m.C12; p.C44x2 = 2.0 * m.C44; p.C44 = m.C44;
   p.ngdot0 = m.n * m.dot_gamma_0; p.rxi_inf = 1.0 / m.xi_inf;
   p.pval = std::fabs(p.P[0][1]);                       // (1/sqrt2)(1/sqrt3), as the host computed P
   p.eps_rel_Lp2 = m.eps_rel_Lp * m.eps_rel_Lp; p.eps_abs_Lp2 = m.eps_abs_Lp * m.eps_abs_Lp;
@@ -1039,7 +1039,7 @@ extern "C" dgx_status dgx_timers(const dgx_rve* r, double ms[3], int64_t launche
   return DGX_OK;
 }
 
-extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[8]) {
+extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[10]) {
   if (!r || !out) return DGX_ERR_ARG;
   ConsCounters c{};
   CK(cudaMemcpy(&c, r->d_cnt, sizeof(c), cudaMemcpyDeviceToHost));
@@ -1048,5 +1048,11 @@ extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[8]) {
   if (r->ex) executor_stats(r->ex, ms, n, &l, &hb, &db);
   out[0] = r->n_eval; out[1] = (int64_t)c.state_iters; out[2] = (int64_t)c.lp_iters; out[3] = r->n_tangent;
   out[4] = r->n_launch + l; out[5] = (int64_t)c.jac_iters; out[6] = r->bytes_h2d + hb; out[7] = r->bytes_d2h + db;
+  out[8] = (int64_t)c.fpi_iters; out[9] = 0;
   return DGX_OK;
+}
+
+extern "C" void dgx_flop_model(double out[4]) {
+  if (!out) return;
+  out[0] = FLOPS_LP; out[1] = FLOPS_JAC; out[2] = FLOPS_STATE; out[3] = FLOPS_FPI;
 }
