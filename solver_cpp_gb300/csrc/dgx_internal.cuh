@@ -72,10 +72,10 @@ struct ConsCounters {
 // and square root = 1), counted from its arithmetic: one Lp Newton iteration (B, Fe,
 // Hooke, 12-system kinetics with derivatives, Lp, residual and norms), one Jacobian
 // (W, signed-sum T, W T for 8 rows, 8x8 LU with one right-hand side), one state
-// integration call (Fp0^-1, F Fp0^-1, 1/xi, first dot state, predictor) and one
-// fixed-point iteration (1/xi, stress epilogue: Fp^-1, P, det, Fp scaling; hardening
-// from the slip rates of the last Lp iteration; damper; state update).
-constexpr double FLOPS_LP = 537.0, FLOPS_JAC = 1184.0, FLOPS_STATE = 783.0, FLOPS_FPI = 1060.0;
+// integration call (Fp0^-1, F Fp0^-1, 1/xi, first dot state, predictor, and once the
+// iteration ends Fp^-1, P, det and Fp scaling) and one fixed-point iteration (1/xi,
+// hardening from the slip rates of the last Lp iteration, damper, state update).
+constexpr double FLOPS_LP = 537.0, FLOPS_JAC = 1184.0, FLOPS_STATE = 1028.0, FLOPS_FPI = 815.0;
 
 // One RVE of a batched constitutive launch (device table, ordered by tile0).
 struct ConsItem {
