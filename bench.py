@@ -40,8 +40,9 @@ UNIT = "point-updates/s"
 SEED = 42
 
 # DRAM traffic of one constitutive launch per cell, from the ncu capture summarised in
-# profiles/constitutive_64cube.md (dram__bytes_read.sum + dram__bytes_write.sum / cells)
-TRAFFIC_BYTES_PER_CELL = None
+# profiles/constitutive_64cube.md (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch / 262,144 cells; mostly register-spill write-back)
+TRAFFIC_BYTES_PER_CELL = 6466.0
 
 
 def args_():

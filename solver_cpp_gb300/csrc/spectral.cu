@@ -195,8 +195,10 @@ __global__ void k_ypass(SpecGeom g, AxisPlan py, typename cpx<R>::t* __restrict_
 
 // ---------------------------------------------------------------- z pass + Gamma + div
 
+// 2 blocks of 256 threads per SM (register cap 128): the per-frequency Gamma work
+// otherwise takes every register and leaves one block per SM
 template <typename R>
-__global__ void k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict__ spec, int TI, GammaArgs ga,
+__global__ void __launch_bounds__(256, 2) k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict__ spec, int TI, GammaArgs ga,
                         const SpecItem* __restrict__ items) {
   typedef typename cpx<R>::t C;
   if (items) {
