@@ -60,6 +60,8 @@ def args_():
     p.add_argument("--batch-rves", type=int, default=256, help="RVEs of the batched leg (0: skip)")
     p.add_argument("--batch-seconds", type=float, default=20.0, help="time bound of the batched leg")
     p.add_argument("--batch-compare", type=int, default=24, help="RVEs of the batched-vs-plain comparison")
+    p.add_argument("--mixed-large", action="store_true",
+                   help="also run the 128^3 / 1000-grain tension-then-shear mixed-precision configuration (~2 min)")
     p.add_argument("--serve-requests", type=int, default=12, help="requests of each serving leg (0: skip)")
     p.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate (requests/s)")
     p.add_argument("--serve-seconds", type=float, default=45.0, help="time bound of each serving leg")
@@ -271,6 +273,37 @@ def batch_leg(g, torch, n_rves, increments, seconds, compare):
     return out
 
 
+def mixed_large_leg(g, torch, cells=128, grains=1000, inc_each=30):
+    """The mixed-precision configuration: 128^3 cells, 1000 grains, tension x then
+    shear xy (1e-3/s, 30 increments each).  The same load case in plain FP64 on the GPU
+    is the reference for the per-increment error of the volume-averaged P."""
+    from solver_cpp_gb300.synthetic import microstructure
+    c3 = (cells, cells, cells)
+    mat_at, q = microstructure(c3, grains, SEED + 1)
+    steps = [g.load_step("tensionX", t=float(inc_each), N=inc_each),
+             g.load_step("shearXY", t=float(inc_each), N=inc_each)]
+    out = {"workload": f"{cells}^3 cells, {grains} grains (seed {SEED + 1}), tension x then shear xy, "
+                       f"{inc_each} + {inc_each} increments"}
+    recs = {}
+    for prec in ("mixed", "fp64"):
+        rve = g.RVE(c3, (1.0, 1.0, 1.0), mat_at, q, num=g.numerics(precision=prec))
+        st = torch.cuda.ExternalStream(rve.stream)
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        recs[prec] = rve.loop_over_loadcase(steps)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        ev = rve.counters()["evaluations"]
+        out[prec] = {"value": rve.N * ev / (ms * 1e-3), "unit": UNIT, "seconds": ms * 1e-3, "evaluations": ev}
+        rve.close()
+    errs = [float(abs(a["P_av"] - b["P_av"]).max() / abs(b["P_av"]).max()) for a, b in zip(recs["mixed"], recs["fp64"])]
+    out["max_rel_P_av_error_vs_fp64"] = max(errs)
+    out["per_increment_error"] = errs
+    return out
+
+
 SERVE_SIZES = (16, 32, 64, 96)
 
 
@@ -451,6 +484,8 @@ def gpu_arm(a):
             ref.close(); mix.close()
         if a.batch_rves > 0:
             line["batched"] = batch_leg(g, torch, a.batch_rves, 20, a.batch_seconds, a.batch_compare)
+        if a.mixed_large:
+            line["mixed_128"] = mixed_large_leg(g, torch)
         if a.serve_requests > 0:
             line["serving"] = [serve_leg(g, p, a.serve_rate, a.serve_requests, a.serve_seconds)
                                for p in ("fp64", "mixed")]

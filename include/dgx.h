@@ -239,6 +239,11 @@ dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
  * [7] d2h bytes of the executor, [8] fixed-point iterations, [9] reserved. */
 dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[10]);
 void* dgx_batch_stream(const dgx_batch* batch);
+/* Cap the residual evaluations served per round at `points` cells (0: no cap).  Above
+ * the cap, members with the least remaining work (cells x increments left) go first;
+ * a member passed over gains priority every round it waits.  Lowers the latency of
+ * small members without starving large ones; results are unchanged. */
+dgx_status dgx_batch_set_round_points(dgx_batch* batch, int64_t points);
 /* autotuner state: [0] constitutive points per block (0 while still tuning), [1] grids
  * with a chosen FFT tile shape, [2] block size still being tuned, [3] tile tuning on */
 dgx_status dgx_batch_tuning(const dgx_batch* batch, int32_t out[4]);
@@ -287,6 +292,8 @@ dgx_status dgx_server_poll(dgx_server* server, int64_t id, double wait_s, dgx_re
 /* forget a finished request */
 dgx_status dgx_server_release(dgx_server* server, int64_t id);
 dgx_status dgx_server_stats(dgx_server* server, dgx_server_info* info);
+/* the server batch's per-round point cap (dgx_batch_set_round_points); default 4 M cells */
+dgx_status dgx_server_set_round_points(dgx_server* server, int64_t points);
 
 /* FP64 FMA throughput of the current device (TFLOP/s, best of 5), the
  * denominator of the constitutive kernel's roofline.  No reference counterpart. */

@@ -307,6 +307,10 @@ class Batch:
                     lp_iterations=a[2], rounds=a[3], launches=a[4], jacobians=a[5], h2d_bytes=a[6],
                     d2h_bytes=a[7], fpi_iterations=a[8])
 
+    def set_round_points(self, points):
+        """Cap the residual evaluations per round (cells); 0 serves every request."""
+        _d.check(_d.lib().dgx_batch_set_round_points(self.h, int(points)), "dgx_batch_set_round_points")
+
     def tuning(self):
         a = (C.c_int32 * 4)()
         _d.check(_d.lib().dgx_batch_tuning(self.h, a), "dgx_batch_tuning")
@@ -344,11 +348,13 @@ class Server:
 
     STATES = ("queued", "running", "done", "failed")
 
-    def __init__(self, hbm_budget_bytes=0, max_active=64, cons_block=0):
+    def __init__(self, hbm_budget_bytes=0, max_active=64, cons_block=0, round_points=None):
         h = C.c_void_p()
         _d.check(_d.lib().dgx_server_create(int(hbm_budget_bytes), int(max_active), int(cons_block), C.byref(h)),
                  "dgx_server_create")
         self.h = h
+        if round_points is not None:
+            _d.check(_d.lib().dgx_server_set_round_points(h, int(round_points)), "dgx_server_set_round_points")
 
     def close(self):
         if getattr(self, "h", None):

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -455,6 +456,7 @@ struct Task {
   std::chrono::steady_clock::time_point t0;
   // SNESSolve locals
   int reason = 0, k = 0, k_restart = 1, lh = 1, ivec = 0, restart_count = 0;
+  int skips = 0;                      // rounds this task's residual request was passed over
   double *X = nullptr, *F = nullptr;
   double fnorm = 0.0, fminnorm = 0.0, fMnorm = 0.0;
   std::vector<double> qm, beta, xi, tmp, tmpA;
@@ -703,19 +705,48 @@ static dgx_status advance(Task& t) {
 
 // one round: serve every parked request, then advance the tasks that were served.
 // A task that fails is finished with its error; the others go on.
-static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks) {
-  std::vector<ResReq> rq;
+// cells x increments still to run (including the current one): the work left
+static double remaining_work(const Task& t) {
+  if (t.mode != 2) return (double)t.r->N;
+  double inc = 0.0;
+  for (int l = t.l; l < t.nsteps; ++l) inc += (l == t.l) ? (t.steps[l].N - t.inc) : t.steps[l].N;
+  return (double)t.r->N * std::max(1.0, inc);
+}
+
+// One round: serve the parked requests, then advance the tasks that were served.  With
+// a point budget, residual evaluations are served least remaining work first until the
+// budget is filled (at least one per round); a task passed over gains priority each
+// round it waits (its work counts half per skipped round), so none starves.  Fused
+// reductions are cheap and always served.  A task that fails is finished with its
+// error; the others go on.
+static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks, int64_t point_budget) {
+  std::vector<Task*> res_tasks, served;
   std::vector<MultiReq> mq;
   for (Task* t : tasks) {
     if (t->done() || t->want == 0) continue;
-    if (t->want == 1) rq.push_back({t->r, t->rin, t->rout});
-    else for (int i = 0; i < t->nmq; ++i) mq.push_back(t->mq[i]);
+    if (t->want == 1) res_tasks.push_back(t);
+    else { for (int i = 0; i < t->nmq; ++i) mq.push_back(t->mq[i]); served.push_back(t); }
   }
+  int64_t total = 0;
+  for (Task* t : res_tasks) total += t->r->N;
+  if (point_budget > 0 && total > point_budget) {
+    std::stable_sort(res_tasks.begin(), res_tasks.end(), [](const Task* a, const Task* b) {
+      return std::ldexp(remaining_work(*a), -std::min(a->skips, 60)) <
+             std::ldexp(remaining_work(*b), -std::min(b->skips, 60));
+    });
+    int64_t used = 0;
+    size_t take = 0;
+    while (take < res_tasks.size() && (take == 0 || used + res_tasks[take]->r->N <= point_budget))
+      used += res_tasks[take++]->r->N;
+    for (size_t k = take; k < res_tasks.size(); ++k) res_tasks[k]->skips++;
+    res_tasks.resize(take);
+  }
+  std::vector<ResReq> rq;
+  for (Task* t : res_tasks) { rq.push_back({t->r, t->rin, t->rout}); t->skips = 0; served.push_back(t); }
   TRY(ex_residual(e, rq));
   TRY(ex_multi(e, mq));
   e->rounds++;
-  for (Task* t : tasks) {
-    if (t->done() || t->want == 0) continue;
+  for (Task* t : served) {
     t->want = 0; t->nmq = 0;
     dgx_status s = advance(*t);
     if (s != DGX_OK) { t->err = s; t->pc = T_DONE; }
@@ -742,7 +773,7 @@ dgx_status run_single(dgx_rve* r, int mode, const dgx_loadstep* steps, int n_or_
   std::vector<Task*> tasks{&t};
   dgx_status s = advance(t);
   while (s == DGX_OK && !t.done()) {
-    s = serve_round(r->ex, tasks);
+    s = serve_round(r->ex, tasks, 0);
     if (s == DGX_OK && t.err != DGX_OK) s = t.err;
   }
   if (s == DGX_OK) s = t.err;
@@ -762,6 +793,7 @@ struct dgx_batch {
   int cap = 0;
   struct Member { dgx_rve* r; Task* t; int active; };
   std::vector<Member> members;      // slot = index; removed members keep their slot (r = null)
+  std::atomic<int64_t> round_points{0};   // residual points served per round (0: all)
 };
 
 extern "C" dgx_status dgx_batch_create(int32_t capacity, int32_t cons_block, dgx_batch** out) {
@@ -820,7 +852,7 @@ extern "C" dgx_status dgx_batch_step(dgx_batch* b, int32_t* n_active) {
   if (!b) return DGX_ERR_ARG;
   std::vector<Task*> tasks;
   for (auto& m : b->members) if (m.r && !m.t->done()) tasks.push_back(m.t);
-  if (!tasks.empty()) TRY(serve_round(b->ex, tasks));
+  if (!tasks.empty()) TRY(serve_round(b->ex, tasks, b->round_points.load()));
   int n = 0;
   for (auto& m : b->members) {
     if (m.r && m.active && m.t->done()) m.active = 0;
@@ -872,6 +904,12 @@ extern "C" dgx_status dgx_batch_stats(const dgx_batch* b, double ms[3], int64_t 
 }
 
 extern "C" void* dgx_batch_stream(const dgx_batch* b) { return b ? (void*)b->st : nullptr; }
+
+extern "C" dgx_status dgx_batch_set_round_points(dgx_batch* b, int64_t points) {
+  if (!b || points < 0) return DGX_ERR_ARG;
+  b->round_points = points;
+  return DGX_OK;
+}
 
 extern "C" dgx_status dgx_batch_tuning(const dgx_batch* b, int32_t out[4]) {
   if (!b || !out) return DGX_ERR_ARG;

@@ -190,6 +190,7 @@ extern "C" dgx_status dgx_server_create(int64_t hbm_budget_bytes, int32_t max_ac
   s->cons_block = cons_block;
   dgx_status st = dgx_batch_create(max_active, cons_block, &s->batch);
   if (st != DGX_OK) { delete s; return st; }
+  dgx_batch_set_round_points(s->batch, 4 << 20);
   s->t0 = std::chrono::steady_clock::now();
   s->worker = std::thread([s] { s->run(); });
   *out = s;
@@ -272,6 +273,12 @@ extern "C" dgx_status dgx_server_release(dgx_server* s, int64_t id) {
   if (it->second->state < 2) return DGX_ERR_STATE;
   s->all.erase(it);
   return DGX_OK;
+}
+
+extern "C" dgx_status dgx_server_set_round_points(dgx_server* s, int64_t points) {
+  if (!s || points < 0) return DGX_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);         // the worker reads it between rounds
+  return dgx_batch_set_round_points(s->batch, points);
 }
 
 extern "C" dgx_status dgx_server_stats(dgx_server* s, dgx_server_info* info) {

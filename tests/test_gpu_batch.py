@@ -115,3 +115,19 @@ def test_autotuned_tiles_and_blocks_do_not_change_results(gpu, monkeypatch):
     assert t["tuned_grids"] >= 1 and not t["tuning_block"] and t["cons_block"] in (64, 128, 256)
     _same(batch.records(slot), ref)
     batch.close()
+
+
+def test_round_point_budget_keeps_results(gpu):
+    """With a per-round point cap the smallest remaining work goes first; every member
+    still computes exactly its solo result."""
+    solo = []
+    for c in CASES[:4]:
+        rve, steps = _make(gpu, c, N=3)
+        solo.append(rve.loop_over_loadcase(steps))
+    batch = gpu.Batch(8)
+    batch.set_round_points(5000)        # below the sum of the members' cells
+    slots = [batch.add(*_make(gpu, c, N=3)) for c in CASES[:4]]
+    batch.run()
+    for slot, ref in zip(slots, solo):
+        _same(batch.records(slot), ref)
+    batch.close()
