@@ -292,7 +292,7 @@ dgx_status dgx_server_poll(dgx_server* server, int64_t id, double wait_s, dgx_re
 /* forget a finished request */
 dgx_status dgx_server_release(dgx_server* server, int64_t id);
 dgx_status dgx_server_stats(dgx_server* server, dgx_server_info* info);
-/* the server batch's per-round point cap (dgx_batch_set_round_points); default 4 M cells */
+/* the server batch's per-round point cap (dgx_batch_set_round_points); default 1 M cells */
 dgx_status dgx_server_set_round_points(dgx_server* server, int64_t points);
 
 /* FP64 FMA throughput of the current device (TFLOP/s, best of 5), the

@@ -190,7 +190,7 @@ extern "C" dgx_status dgx_server_create(int64_t hbm_budget_bytes, int32_t max_ac
   s->cons_block = cons_block;
   dgx_status st = dgx_batch_create(max_active, cons_block, &s->batch);
   if (st != DGX_OK) { delete s; return st; }
-  dgx_batch_set_round_points(s->batch, 4 << 20);
+  dgx_batch_set_round_points(s->batch, 1 << 20);
   s->t0 = std::chrono::steady_clock::now();
   s->worker = std::thread([s] { s->run(); });
   *out = s;
