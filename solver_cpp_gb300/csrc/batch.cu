@@ -210,9 +210,12 @@ static GridKey grid_key(const dgx_rve* r) {
                  r->num.derivative, r->num.divergence_correction);
 }
 
-// FFT tile shape of a grid: the tuned one, or (first time, when tuning) the fastest
-// of the default and its halved / doubled x-line, y-tile and z-tile counts, each timed
-// on this group's own convolution (every candidate computes the same result)
+// FFT tile shape of a grid: the tuned one, or (first time, when tuning) chosen per pass.
+// Each pass's time depends only on its own tile (x lines per block, x-frequencies per y
+// block, x-frequencies per z block), so every dimension is scanned with the others at
+// their defaults (x and y: 1/2 .. 8x the default, z: 1/2 .. 2x) and the fastest value of
+// each is kept.  Every candidate is timed on this group's own convolution and computes
+// the same result.
 static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0, const SpecItem* items, int cnt,
                                     const GammaArgs& ga) {
   auto it = e->spec_tuned.find(key);
@@ -222,24 +225,10 @@ static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0
   const bool fp32 = r0->num.precision == 1;
   const size_t cs = fp32 ? sizeof(float2) : sizeof(double2);
   const SpecGeom& g = base.g;
-  std::vector<SpecLaunch> cands{base};
-  const int f[2] = {2, -2};
-  for (int k = 0; k < 2; ++k) {
-    auto sc = [&](int v) { return f[k] > 0 ? v * 2 : std::max(1, v / 2); };
-    cands.push_back(spec_launch_tiles(g.N0, g.N1, g.N2, cs, sc(base.LX), base.TIy, base.TIz));
-    cands.push_back(spec_launch_tiles(g.N0, g.N1, g.N2, cs, base.LX, sc(base.TIy), base.TIz));
-    cands.push_back(spec_launch_tiles(g.N0, g.N1, g.N2, cs, base.LX, base.TIy, sc(base.TIz)));
-  }
-  int best = 0;
-  float best_ms = 1e30f;
-  for (size_t c = 0; c < cands.size(); ++c) {
-    const SpecLaunch& L = cands[c];
-    bool dup = false;
-    for (size_t d = 0; d < c; ++d)
-      dup |= cands[d].LX == L.LX && cands[d].TIy == L.TIy && cands[d].TIz == L.TIz;
-    if (dup || !spec_launch_fits(L)) continue;
+  auto time_of = [&](const SpecLaunch& L) -> float {
+    if (!spec_launch_fits(L)) return 1e30f;
     spec_prepare(L, fp32);
-    float ms = 0.f;
+    float ms = 1e30f;
     for (int rep = 0; rep < 2; ++rep) {
       cudaEventRecord(e->ev[2], e->st);
       spec_convolve_batch(L, fp32, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan, items, cnt, ga, e->st);
@@ -248,9 +237,28 @@ static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0
       cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]);
     }
     e->launches += 10;
-    if (cudaGetLastError() == cudaSuccess && ms < best_ms) { best_ms = ms; best = (int)c; }
+    return cudaGetLastError() == cudaSuccess ? ms : 1e30f;
+  };
+  const int facs[5] = {-2, 2, 4, 8, 1};      // x1/2, x2, x4, x8 (1: the default itself)
+  int best[3] = {base.LX, base.TIy, base.TIz};
+  const float t0 = time_of(base);
+  for (int d = 0; d < 3; ++d) {
+    float bt = t0;
+    const int v0 = d == 0 ? base.LX : d == 1 ? base.TIy : base.TIz;
+    for (int f = 0; f < 4; ++f) {
+      if (d == 2 && facs[f] > 2) continue;
+      const int v = facs[f] < 0 ? v0 / 2 : v0 * facs[f];
+      if (v < 1 || v == v0 || (d > 0 && v > g.N0r) || (d == 0 && v > 9 * g.N1 * g.N2)) continue;
+      int t[3] = {base.LX, base.TIy, base.TIz};
+      t[d] = v;
+      const float ms = time_of(spec_launch_tiles(g.N0, g.N1, g.N2, cs, t[0], t[1], t[2]));
+      if (ms < bt) { bt = ms; best[d] = v; }
+    }
   }
-  return e->spec_tuned.emplace(key, cands[best]).first->second;
+  SpecLaunch L = spec_launch_tiles(g.N0, g.N1, g.N2, cs, best[0], best[1], best[2]);
+  if (!spec_launch_fits(L)) L = base;
+  spec_prepare(L, fp32);
+  return e->spec_tuned.emplace(key, L).first->second;
 }
 
 // residual evaluations R = Gamma * P(X) of every request (form_residual)
