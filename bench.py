@@ -360,6 +360,36 @@ def serve_leg(g, precision, rate, n_requests, seconds, seed=5000):
             "note": "value counts the completed requests' point-updates over the whole window (wall clock)"}
 
 
+def spectral_roofline(cells, precision, ms, fp64_peak):
+    """FFT / Gamma / div-RMS chain of one residual evaluation against both ceilings.
+    bytes: read P and write R (9N FP64 each) plus the spectrum traffic between the five
+    passes (x out, y in/out, z in/out, y in/out, x in: 8 x 9 Nh complex of the spectral
+    precision).  flops: 5 n log2 n per complex line FFT (forward and inverse, x lines
+    as complex), ~230 per frequency for Gamma and the divergence sum."""
+    import math
+    N0, N1, N2 = cells
+    N, N0r = N0 * N1 * N2, N0 // 2 + 1
+    Nh = N0r * N1 * N2
+    cs = 16 if precision == "fp64" else 8
+    bytes_ = 2 * 9 * N * 8 + 8 * 9 * Nh * cs
+    fl = 2 * 5 * 9 * (N1 * N2 * N0 * math.log2(N0) + N0r * N2 * N1 * math.log2(N1) + N0r * N1 * N2 * math.log2(N2))
+    fl += 230 * Nh
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    gbs = bytes_ / (ms * 1e-3) / 1e9
+    tfs = fl / (ms * 1e-3) / 1e12
+    return {"bound": "fp64" if precision == "fp64" else "hbm", "bytes_per_residual": bytes_,
+            "achieved_gbs": gbs, "peak_gbs": hbm, "frac_hbm": gbs / hbm,
+            "peak_source_hbm": "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback",
+            "flops_per_residual": fl, "achieved_tflops": tfs,
+            "frac_fp64": tfs / fp64_peak if fp64_peak else None}
+
+
 def run_increments(rve, step, start, count, n_inc, read_back=False):
     """Run `count` increments starting at global index `start` (load case cycled)."""
     lat = []
@@ -445,6 +475,7 @@ def gpu_arm(a):
                          "peak_source": "measured: dgx_measure_fp64_peak DFMA probe (MEASURED_PEAKS.json has no FP64)"},
             "kernel_time_share": {"constitutive": kms / ms, "spectral": spec_ms / ms,
                                   "spectral_ms_per_residual": spec_ms / max(1, spec_n)},
+            "roofline_spectral": spectral_roofline(cells, a.precision, spec_ms / max(1, spec_n), peak.value),
             "evaluations_per_increment": evals / a.steps,
             "latency": {"p50_increment_ms": 1e3 * statistics.median(lat),
                         "p99_increment_ms": 1e3 * sorted(lat)[min(len(lat) - 1, int(0.99 * len(lat)))]},

@@ -33,16 +33,20 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
 }
 
 
-template <typename R> __device__ __forceinline__ typename cpx<R>::t twid(const AxisPlan& p, long j, int sign) {
+// twiddle exp(sign 2 pi i j / n) for 0 <= j < n
+template <typename R> __device__ __forceinline__ typename cpx<R>::t twid(const AxisPlan& p, int j, int sign) {
   typename cpx<R>::t w;
-  int k = (int)(j % p.n);
-  if constexpr (sizeof(R) == 8) { double2 t = p.tw[k]; w.x = t.x; w.y = sign > 0 ? -t.y : t.y; }
-  else { float2 t = p.twf[k]; w.x = t.x; w.y = sign > 0 ? -t.y : t.y; }
+  if constexpr (sizeof(R) == 8) { double2 t = p.tw[j]; w.x = t.x; w.y = sign > 0 ? -t.y : t.y; }
+  else { float2 t = p.twf[j]; w.x = t.x; w.y = sign > 0 ? -t.y : t.y; }
   return w;
 }
 
+__device__ __forceinline__ int ilog2_or_neg(int v) { return (v & (v - 1)) == 0 ? __ffs(v) - 1 : -1; }
+
 // Stockham FFT of `nl` lines of length p.n, stored contiguously (line l at a + l*n).
 // Returns the buffer that holds the result (a or b).  sign -1 forward, +1 inverse.
+// Index arithmetic uses shifts when the stage sizes are powers of two; the first stage
+// (all twiddles 1) skips the twiddle products, which leaves the results unchanged.
 template <typename R>
 __device__ typename cpx<R>::t* block_fft(typename cpx<R>::t* a, typename cpx<R>::t* b, int nl, const AxisPlan& p, int sign) {
   typedef typename cpx<R>::t C;
@@ -51,22 +55,31 @@ __device__ typename cpx<R>::t* block_fft(typename cpx<R>::t* a, typename cpx<R>:
   for (int s = 0; s < p.nstages; ++s) {
     const int r = p.radix[s], m = n / r;
     const int tot = nl * m;
+    const int mlog = ilog2_or_neg(m), llog = ilog2_or_neg(Ls);
+    const int tws = n / (Ls * r);
+    const bool first = Ls == 1;
     for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-      const int line = t / m, j = t - line * m;
-      const int k = j % Ls;
+      int line, j, k, jl;
+      if (mlog >= 0) { line = t >> mlog; j = t & (m - 1); }
+      else { line = t / m; j = t - line * m; }
+      if (llog >= 0) { k = j & (Ls - 1); jl = j >> llog; }
+      else { jl = j / Ls; k = j - jl * Ls; }
       const C* in = a + (long)line * n;
       C* out = b + (long)line * n;
-      const int od = (j / Ls) * Ls * r + k;
-      const long twstep = (long)(n / (Ls * r)) * k;
+      const int od = jl * Ls * r + k;
+      const int twstep = tws * k;
       if (r == 2) {
-        C v0 = in[j], v1 = cmul(in[j + m], twid<R>(p, twstep, sign));
+        C v0 = in[j], v1 = first ? in[j + m] : cmul(in[j + m], twid<R>(p, twstep, sign));
         C y0, y1; y0.x = v0.x + v1.x; y0.y = v0.y + v1.y; y1.x = v0.x - v1.x; y1.y = v0.y - v1.y;
         out[od] = y0; out[od + Ls] = y1;
       } else if (r == 4) {
-        C v0 = in[j];
-        C v1 = cmul(in[j + m], twid<R>(p, twstep, sign));
-        C v2 = cmul(in[j + 2 * m], twid<R>(p, 2 * twstep, sign));
-        C v3 = cmul(in[j + 3 * m], twid<R>(p, 3 * twstep, sign));
+        C v0 = in[j], v1, v2, v3;
+        if (first) { v1 = in[j + m]; v2 = in[j + 2 * m]; v3 = in[j + 3 * m]; }
+        else {
+          v1 = cmul(in[j + m], twid<R>(p, twstep, sign));
+          v2 = cmul(in[j + 2 * m], twid<R>(p, 2 * twstep, sign));
+          v3 = cmul(in[j + 3 * m], twid<R>(p, 3 * twstep, sign));
+        }
         C s02, d02, s13, d13;
         s02.x = v0.x + v2.x; s02.y = v0.y + v2.y; d02.x = v0.x - v2.x; d02.y = v0.y - v2.y;
         s13.x = v1.x + v3.x; s13.y = v1.y + v3.y; d13.x = v1.x - v3.x; d13.y = v1.y - v3.y;
@@ -80,11 +93,11 @@ __device__ typename cpx<R>::t* block_fft(typename cpx<R>::t* a, typename cpx<R>:
         out[od] = y0; out[od + Ls] = y1; out[od + 2 * Ls] = y2; out[od + 3 * Ls] = y3;
       } else {
         C v[16];
-        for (int q = 0; q < r; ++q) v[q] = cmul(in[j + q * m], twid<R>(p, (long)q * twstep, sign));
+        for (int q = 0; q < r; ++q) v[q] = cmul(in[j + q * m], twid<R>(p, q * twstep, sign));
         for (int s2 = 0; s2 < r; ++s2) {
           C acc; acc.x = v[0].x; acc.y = v[0].y;
           for (int q = 1; q < r; ++q) {
-            C w = twid<R>(p, (long)q * s2 * m, sign);
+            C w = twid<R>(p, (int)(((long)q * s2 * m) % n), sign);
             C t2 = cmul(v[q], w);
             acc.x += t2.x; acc.y += t2.y;
           }
