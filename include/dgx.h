@@ -245,7 +245,8 @@ void* dgx_batch_stream(const dgx_batch* batch);
  * small members without starving large ones; results are unchanged. */
 dgx_status dgx_batch_set_round_points(dgx_batch* batch, int64_t points);
 /* autotuner state: [0] constitutive points per block (0 while still tuning), [1] grids
- * with a chosen FFT tile shape, [2] block size still being tuned, [3] tile tuning on */
+ * with a chosen FFT tile shape, [2] blocks per SM the chosen constitutive variant's
+ * register allocation targets (0 while still tuning), [3] tile tuning on */
 dgx_status dgx_batch_tuning(const dgx_batch* batch, int32_t out[4]);
 
 /* ---- Serving (no counterpart in the reference).  A server owns one worker thread, the

@@ -314,7 +314,8 @@ class Batch:
     def tuning(self):
         a = (C.c_int32 * 4)()
         _d.check(_d.lib().dgx_batch_tuning(self.h, a), "dgx_batch_tuning")
-        return dict(cons_block=a[0], tuned_grids=a[1], tuning_block=bool(a[2]), tuning_tiles=bool(a[3]))
+        return dict(cons_block=a[0], tuned_grids=a[1], blocks_per_sm=a[2], tuning_block=a[0] == 0,
+                    tuning_tiles=bool(a[3]))
 
     @property
     def stream(self):

@@ -115,14 +115,15 @@ struct Executor {
   double* h_mout = nullptr;
   ConsCounters* cnt = nullptr;
   bool own_cnt = false;
-  int cons_block = 128, resident = 0;
-  // autotuner: constitutive points per block, chosen online from the cost per counted
-  // FP64 flop of the first rounds (each candidate twice), and per grid the FFT tile
-  // shape, timed on the first round's own data (results do not depend on either)
+  int cons_variant = 1, resident = 0;          // launch variant (points per block, blocks per SM)
+  // autotuner: the constitutive launch variant (points per block, blocks per SM),
+  // chosen online from the median cost per counted FP64 flop of three interleaved
+  // rounds per variant, and per grid the FFT tile shape, timed on the first round's data
+  // (results do not depend on either)
   bool tune_cons = true, tune_spec = true;
-  int res_by_block[3] = {0, 0, 0};
-  double cons_cost[3] = {0, 0, 0};
-  int cons_trials[3] = {0, 0, 0}, cons_round = 0;
+  int res_by_variant[CONS_VARIANTS] = {0, 0, 0, 0};
+  double cons_cost[CONS_VARIANTS][3] = {};
+  int cons_trials[CONS_VARIANTS] = {0, 0, 0, 0}, cons_round = 0;
   ConsCounters cnt_last{};
   ConsCounters* h_cnt = nullptr;
   std::map<std::tuple<int, int, int, double, double, double, int, int, int>, SpecLaunch> spec_tuned;
@@ -158,7 +159,7 @@ static dgx_status ex_alloc(Executor* e, T** d, T** h, size_t n) {
 dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons_block, Executor** out) {
   Executor* e = new Executor();
   e->st = st; e->cap = cap;
-  e->cons_block = (cons_block == 64 || cons_block == 256) ? cons_block : 128;   // <= 0: autotuned
+  e->cons_variant = cons_block == 64 ? 0 : (cons_block == 256 ? 2 : 1);       // <= 0: autotuned
   dgx_status s = DGX_OK;
 #define EA(d, h, n) do { s = ex_alloc(e, d, h, n); if (s != DGX_OK) { executor_destroy(e); return s; } } while (0)
   EA(&e->d_cons, &e->h_cons, cap);
@@ -175,11 +176,17 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   else { EA(&e->cnt, (ConsCounters**)nullptr, 1); e->own_cnt = true; cudaMemset(e->cnt, 0, sizeof(ConsCounters)); }
 #undef EA
   for (auto& v : e->ev) cudaEventCreate(&v);
-  for (int k = 0; k < 3; ++k) e->res_by_block[k] = constitutive_batch_resident(64 << k);
-  e->resident = constitutive_batch_resident(e->cons_block);
+  for (int k = 0; k < CONS_VARIANTS; ++k) e->res_by_variant[k] = constitutive_batch_resident(k);
+  e->resident = e->res_by_variant[e->cons_variant];
   const char* at = std::getenv("DGX_AUTOTUNE");
   const bool tune = !(at && at[0] == '0');
   e->tune_cons = tune && cons_block <= 0;       // an explicit block size is kept
+  const char* cv = std::getenv("DGX_CONS_VARIANT");   // pin a launch variant (0..3) for measurements
+  if (cv && cv[0] >= '0' && cv[0] < '0' + CONS_VARIANTS && cv[1] == 0) {
+    e->cons_variant = cv[0] - '0';
+    e->resident = e->res_by_variant[e->cons_variant];
+    e->tune_cons = false;
+  }
   e->tune_spec = tune;
   if (cudaMemcpyAsync(&e->cnt_last, e->cnt, sizeof(ConsCounters), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) { executor_destroy(e); set_err("executor: counters"); return DGX_ERR_CUDA; }
@@ -276,11 +283,12 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
   });
   int cand = -1;
   if (e->tune_cons) {
-    cand = e->cons_round % 3;
-    if (e->cons_trials[cand] >= 2) cand = -1;
+    cand = e->cons_round % CONS_VARIANTS;
+    if (e->cons_trials[cand] >= 3) cand = -1;
   }
-  const int BS = cand >= 0 ? (64 << cand) : e->cons_block;
-  const int resident = cand >= 0 ? e->res_by_block[cand] : e->resident;
+  const int variant = cand >= 0 ? cand : e->cons_variant;
+  const int BS = cons_variant_bs(variant);
+  const int resident = e->res_by_variant[variant];
   std::vector<int> slot_of(n);
   for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
   CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, e->st));
@@ -312,7 +320,7 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
     int j1 = g + 1 < groups.size() ? groups[g + 1].first : n;
     long long tiles = groups[g].second;
     int grid = (int)std::min<long long>(tiles, resident);
-    launch_constitutive_batch(q[order[j0]].r->mp, e->d_cons + j0, j1 - j0, tiles, e->d_queue + g, e->cnt, e->st, BS,
+    launch_constitutive_batch(q[order[j0]].r->mp, e->d_cons + j0, j1 - j0, tiles, e->d_queue + g, e->cnt, e->st, variant,
                               std::max(grid, 1));
     e->launches++;
   }
@@ -335,13 +343,21 @@ static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
                      FLOPS_STATE * (double)(c1.state_iters - e->cnt_last.state_iters) +
                      FLOPS_FPI * (double)(c1.fpi_iters - e->cnt_last.fpi_iters);
       e->cnt_last = c1;
-      if (cand >= 0 && flops > 0.0) { e->cons_cost[cand] += ms / flops; e->cons_trials[cand]++; }
+      if (cand >= 0 && flops > 0.0) e->cons_cost[cand][e->cons_trials[cand]++] = ms / flops;
       e->cons_round++;
-      if (e->cons_trials[0] >= 2 && e->cons_trials[1] >= 2 && e->cons_trials[2] >= 2) {
+      bool all = true;
+      for (int k = 0; k < CONS_VARIANTS; ++k) all &= e->cons_trials[k] >= 3;
+      if (all) {
+        // median of three interleaved trials per variant
+        double med[CONS_VARIANTS];
+        for (int k = 0; k < CONS_VARIANTS; ++k) {
+          double* c = e->cons_cost[k];
+          med[k] = std::max(std::min(c[0], c[1]), std::min(std::max(c[0], c[1]), c[2]));
+        }
         int best = 0;
-        for (int k = 1; k < 3; ++k) if (e->cons_cost[k] < e->cons_cost[best]) best = k;
-        e->cons_block = 64 << best;
-        e->resident = e->res_by_block[best];
+        for (int k = 1; k < CONS_VARIANTS; ++k) if (med[k] < med[best]) best = k;
+        e->cons_variant = best;
+        e->resident = e->res_by_variant[best];
         e->tune_cons = false;
       }
     }
@@ -922,9 +938,9 @@ extern "C" dgx_status dgx_batch_set_round_points(dgx_batch* b, int64_t points) {
 extern "C" dgx_status dgx_batch_tuning(const dgx_batch* b, int32_t out[4]) {
   if (!b || !out) return DGX_ERR_ARG;
   const Executor* e = b->ex;
-  out[0] = e->tune_cons ? 0 : e->cons_block;
+  out[0] = e->tune_cons ? 0 : cons_variant_bs(e->cons_variant);
   out[1] = (int32_t)e->spec_tuned.size();
-  out[2] = e->tune_cons ? 1 : 0;
+  out[2] = e->tune_cons ? 0 : cons_variant_minb(e->cons_variant);
   out[3] = e->tune_spec ? 1 : 0;
   return DGX_OK;
 }

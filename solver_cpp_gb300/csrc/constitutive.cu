@@ -594,8 +594,8 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
 // queue (one atomic per tile) so that a few slow tiles do not idle the rest.  Every
 // tile is the same computation as in k_constitutive, so results do not depend on
 // which RVEs share the launch.
-template <int BS>
-__global__ void __launch_bounds__(BS)
+template <int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB)
 k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitems, long long ntiles,
                      unsigned long long* __restrict__ queue, ConsCounters* cnt) {
   __shared__ ConsItem s_it;
@@ -889,18 +889,24 @@ void launch_constitutive(const MatParams& mp, const PointState& ps, const double
 }
 // persistent batched launch: grid = min(tiles, resident blocks); queue must be zero
 void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
-                               unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int block, int grid) {
-  if (block == 64) k_constitutive_batch<64><<<grid, 64, 0, st>>>(mp, items, nitems, ntiles, queue, cnt);
-  else if (block == 256) k_constitutive_batch<256><<<grid, 256, 0, st>>>(mp, items, nitems, ntiles, queue, cnt);
-  else k_constitutive_batch<128><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt);
+                               unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int variant, int grid) {
+  switch (variant) {
+    case 0: k_constitutive_batch<64, 1><<<grid, 64, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
+    case 2: k_constitutive_batch<256, 1><<<grid, 256, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
+    case 3: k_constitutive_batch<128, 3><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
+    default: k_constitutive_batch<128, 1><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
+  }
 }
-int constitutive_batch_resident(int block) {
+int constitutive_batch_resident(int variant) {
   int nb = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (block == 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<64>, 64, 0);
-  else if (block == 256) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<256>, 256, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128>, 128, 0);
+  switch (variant) {
+    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<64, 1>, 64, 0); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<256, 1>, 256, 0); break;
+    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128, 3>, 128, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128, 1>, 128, 0); break;
+  }
   return std::max(1, nb) * std::max(1, sms);
 }
 void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st) {

@@ -92,9 +92,14 @@ struct ConsItem {
 // constitutive.cu launchers
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
                          double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block);
+// launch variants of the batched constitutive kernel: points per block, and the blocks
+// per SM its register allocation targets (more blocks: fewer registers, more spills)
+constexpr int CONS_VARIANTS = 4;
+__host__ __device__ constexpr int cons_variant_bs(int v) { return v == 0 ? 64 : (v == 2 ? 256 : 128); }
+__host__ __device__ constexpr int cons_variant_minb(int v) { return v == 3 ? 3 : 1; }
 void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
-                               unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int block, int grid);
-int constitutive_batch_resident(int block);
+                               unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int variant, int grid);
+int constitutive_batch_resident(int variant);
 void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st);
 void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st);
 void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,
