@@ -8,11 +8,12 @@
 // fused reduction -- and parks the request.  The executor then serves the requests
 // of every task in one batched launch sequence:
 //   residual   one persistent constitutive launch over the points of all RVEs
-//              (offset-indexed tiles), one P_av reduction launch, host BC step,
-//              then per group of equal grids one launch per FFT pass with one
-//              blockIdx.y per RVE (FFT, divergence RMS, Gamma), one RMS launch
+//              (offset-indexed tiles), one P_av reduction launch, one stress-BC
+//              launch, then per group of equal grids one launch per FFT pass with
+//              one blockIdx.y per RVE (FFT, divergence RMS, Gamma), one RMS launch
 //   reduction  one fused multi-dot launch for all RVEs plus one finishing launch
-// and hands the results back.  Per-RVE arithmetic is identical to a batch of one
+//              (after the residuals of the same round when a task asks for both)
+// with a single host synchronisation per round, and hands the results back.  Per-RVE arithmetic is identical to a batch of one
 // (the same tiles, reduction partitions and summation orders), so an RVE's result
 // does not depend on which other RVEs share the batch.  A single-RVE solve is a
 // batch of one.
@@ -93,6 +94,61 @@ __global__ void k_multi_finish_batch(const MultiItem* __restrict__ items) {
   if (threadIdx.x == 0) it.out[k] = s;
 }
 
+// ------------------------------------------------------------------ stress BC step on the device
+// The BC part of form_residual (mech_solver_basic.cpp:321-334) for every RVE of a round,
+// between the P_av reduction and the spectral pass, so that a residual evaluation needs
+// no host round trip.  Rounded operation by operation in the host code's order (no
+// contraction), so F_aim, err_BC and the zero-frequency value are bit-identical to the
+// host computation.
+struct BcItem {
+  BcBlock* bc;
+  double* Pav;        // in: volume average of P; out: in the BC frame when rotated
+  double* aim;        // out: rotated dF_aim (zero frequency of Gamma * P)
+  double* out;        // out: F_aim (9) and err_BC
+};
+
+__device__ void rotate2_exact(const double* R, const double* T, double* out, bool active) {
+  double t[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s = __dadd_rn(s, __dmul_rn(active ? R[k + 3 * i] : R[i + 3 * k], T[k + 3 * j]));
+      t[i + 3 * j] = s;
+    }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s = __dadd_rn(s, __dmul_rn(t[i + 3 * k], active ? R[k + 3 * j] : R[j + 3 * k]));
+      out[i + 3 * j] = s;
+    }
+}
+
+__global__ void k_bc_batch(const BcItem* __restrict__ items) {
+  if (threadIdx.x != 0) return;
+  const BcItem it = items[blockIdx.x];
+  BcBlock* bc = it.bc;
+  double P[9], dF[9], aim[9];
+  for (int k = 0; k < 9; ++k) P[k] = it.Pav[k];
+  if (bc->rotated) {                               // P_av into the BC frame (Spectral::constitutive_response)
+    double t[9];
+    rotate2_exact(bc->R, P, t, false);
+    for (int k = 0; k < 9; ++k) { P[k] = t[k]; it.Pav[k] = t[k]; }
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) s = __dadd_rn(s, __dmul_rn(bc->S[i + 3 * j + 9 * k + 27 * l], P[k + 3 * l]));
+      dF[i + 3 * j] = s;
+    }
+  for (int k = 0; k < 9; ++k) { const double f = __dsub_rn(bc->F_aim[k], dF[k]); bc->F_aim[k] = f; it.out[k] = f; }
+  double err = 0.0;
+  for (int k = 0; k < 9; ++k) if (!bc->mask[k]) err = fmax(err, fabs(__dsub_rn(P[k], bc->P_aim[k])));
+  it.out[9] = err;
+  rotate2_exact(bc->R, dF, aim, true);
+  for (int k = 0; k < 9; ++k) it.aim[k] = aim[k];
+}
+
 // ------------------------------------------------------------------ executor
 struct ResReq { dgx_rve* r; const double* in; double* out; };
 struct MultiReq {
@@ -111,8 +167,10 @@ struct Executor {
   int* d_ill = nullptr; double* d_Pav = nullptr; double* d_aim = nullptr; double* d_rms = nullptr;
   double* d_mout = nullptr; unsigned long long* d_queue = nullptr;
   ConsItem* h_cons = nullptr; SpecItem* h_spec = nullptr; MultiItem* h_multi = nullptr;
-  int* h_ill = nullptr; double* h_Pav = nullptr; double* h_aim = nullptr; double* h_rms = nullptr;
+  int* h_ill = nullptr; double* h_Pav = nullptr; double* h_rms = nullptr;
   double* h_mout = nullptr;
+  BcItem* d_bcitem = nullptr; BcItem* h_bcitem = nullptr;
+  double* d_bcout = nullptr; double* h_bcout = nullptr;
   ConsCounters* cnt = nullptr;
   bool own_cnt = false;
   int cons_variant = 1, resident = 0;          // launch variant (points per block, blocks per SM)
@@ -167,9 +225,11 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   EA(&e->d_multi, &e->h_multi, 2 * cap);
   EA(&e->d_ill, &e->h_ill, cap);
   EA(&e->d_Pav, &e->h_Pav, 9 * cap);
-  EA(&e->d_aim, &e->h_aim, 9 * cap);
+  EA(&e->d_aim, (double**)nullptr, 9 * cap);
   EA(&e->d_rms, &e->h_rms, cap);
   EA(&e->d_mout, &e->h_mout, 64 * 2 * cap);
+  EA(&e->d_bcitem, &e->h_bcitem, cap);
+  EA(&e->d_bcout, &e->h_bcout, 10 * cap);
   EA(&e->d_queue, (unsigned long long**)nullptr, 16);
   EA((ConsCounters**)nullptr, &e->h_cnt, 1);
   if (cnt) e->cnt = cnt;
@@ -268,163 +328,8 @@ static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0
   return e->spec_tuned.emplace(key, L).first->second;
 }
 
-// residual evaluations R = Gamma * P(X) of every request (form_residual)
-static dgx_status ex_residual(Executor* e, std::vector<ResReq>& q) {
-  const int n = (int)q.size();
-  if (n == 0) return DGX_OK;
-  if (n > e->cap) { set_err("executor: %d residual requests exceed capacity %d", n, e->cap); return DGX_ERR_STATE; }
-  // constitutive pass: items grouped by material, largest RVEs first in the tile queue
-  std::vector<int> order(n);
-  for (int i = 0; i < n; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    int c = memcmp(&q[a].r->mp, &q[b].r->mp, sizeof(MatParams));
-    if (c != 0) return c < 0;
-    return q[a].r->N > q[b].r->N;
-  });
-  int cand = -1;
-  if (e->tune_cons) {
-    cand = e->cons_round % CONS_VARIANTS;
-    if (e->cons_trials[cand] >= 3) cand = -1;
-  }
-  const int variant = cand >= 0 ? cand : e->cons_variant;
-  const int BS = cons_variant_bs(variant);
-  const int resident = e->res_by_variant[variant];
-  std::vector<int> slot_of(n);
-  for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
-  CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, e->st));
-  CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * 16, e->st));
-  std::vector<std::pair<int, long long>> groups;    // (first slot, tiles)
-  {
-    long long tiles = 0;
-    int gstart = 0;
-    for (int j = 0; j < n; ++j) {
-      dgx_rve* r = q[order[j]].r;
-      if (j > 0 && memcmp(&r->mp, &q[order[j - 1]].r->mp, sizeof(MatParams)) != 0) {
-        groups.push_back({gstart, tiles}); gstart = j; tiles = 0;
-      }
-      ConsItem& it = e->h_cons[j];
-      it.ps = r->ps; it.F = q[order[j]].in; it.ldF = r->N; it.dt = r->delta_t; it.wgt = r->wgt;
-      it.Ppart = r->d_Ppart; it.ill = e->d_ill + j; it.tile0 = tiles;
-      tiles += (r->N + BS - 1) / BS;
-      r->n_eval++;
-      r->tangent_dt = r->delta_t;
-      e->point_evals += r->N;
-    }
-    groups.push_back({gstart, tiles});
-    if (groups.size() > 16) { set_err("executor: more than 16 materials in one round"); return DGX_ERR_UNSUPPORTED; }
-  }
-  TRY(ex_h2d(e, e->d_cons, e->h_cons, sizeof(ConsItem) * n));
-  CK(cudaEventRecord(e->ev[0], e->st));
-  for (size_t g = 0; g < groups.size(); ++g) {
-    int j0 = groups[g].first;
-    int j1 = g + 1 < groups.size() ? groups[g + 1].first : n;
-    long long tiles = groups[g].second;
-    int grid = (int)std::min<long long>(tiles, resident);
-    launch_constitutive_batch(q[order[j0]].r->mp, e->d_cons + j0, j1 - j0, tiles, e->d_queue + g, e->cnt, e->st, variant,
-                              std::max(grid, 1));
-    e->launches++;
-  }
-  CK(cudaEventRecord(e->ev[1], e->st));
-  launch_pav_finish_batch(e->d_cons, n, e->d_Pav, e->st);
-  e->launches++;
-  TRY(ex_d2h(e, e->h_Pav, e->d_Pav, sizeof(double) * 9 * n));
-  TRY(ex_d2h(e, e->h_ill, e->d_ill, sizeof(int) * n));
-  if (e->tune_cons) TRY(ex_d2h(e, e->h_cnt, e->cnt, sizeof(ConsCounters)));
-  CK(cudaStreamSynchronize(e->st));
-  CK(cudaGetLastError());
-  {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[0] += ms; e->t_n[0]++;
-    if (e->tune_cons) {
-      // cost per counted flop (the constitutive roofline's own flop model)
-      const ConsCounters& c1 = *e->h_cnt;
-      double flops = FLOPS_LP * (double)(c1.lp_iters - e->cnt_last.lp_iters) +
-                     FLOPS_JAC * (double)(c1.jac_iters - e->cnt_last.jac_iters) +
-                     FLOPS_STATE * (double)(c1.state_iters - e->cnt_last.state_iters) +
-                     FLOPS_FPI * (double)(c1.fpi_iters - e->cnt_last.fpi_iters);
-      e->cnt_last = c1;
-      if (cand >= 0 && flops > 0.0) e->cons_cost[cand][e->cons_trials[cand]++] = ms / flops;
-      e->cons_round++;
-      bool all = true;
-      for (int k = 0; k < CONS_VARIANTS; ++k) all &= e->cons_trials[k] >= 3;
-      if (all) {
-        // median of three interleaved trials per variant
-        double med[CONS_VARIANTS];
-        for (int k = 0; k < CONS_VARIANTS; ++k) {
-          double* c = e->cons_cost[k];
-          med[k] = std::max(std::min(c[0], c[1]), std::min(std::max(c[0], c[1]), c[2]));
-        }
-        int best = 0;
-        for (int k = 1; k < CONS_VARIANTS; ++k) if (med[k] < med[best]) best = k;
-        e->cons_variant = best;
-        e->resident = e->res_by_variant[best];
-        e->tune_cons = false;
-      }
-    }
-  }
-  // host BC step of every RVE
-  for (int i = 0; i < n; ++i) {
-    dgx_rve* r = q[i].r;
-    const int j = slot_of[i];
-    memcpy(r->P_av, e->h_Pav + 9 * j, 9 * sizeof(double));
-    TRY(post_constitutive(r, e->h_ill[j], !r->num.lazy_tangent));
-    residual_bc(r, e->h_aim + 9 * i);
-  }
-  // spectral pass: one launch chain per grid group
-  std::map<GridKey, std::vector<int>> gg;
-  for (int i = 0; i < n; ++i) gg[grid_key(q[i].r)].push_back(i);
-  int off = 0;
-  std::vector<std::pair<int, int>> spans;
-  for (auto& kv : gg) {
-    spans.push_back({off, (int)kv.second.size()});
-    for (int i : kv.second) {
-      dgx_rve* r = q[i].r;
-      SpecItem& it = e->h_spec[off++];
-      it.in = r->ps.P; it.out = q[i].out; it.spec = r->spec; it.C_ref = r->d_Cref; it.aim = e->d_aim + 9 * i;
-      it.div_part = r->d_divpart; it.rms = e->d_rms + i;
-    }
-  }
-  TRY(ex_h2d(e, e->d_aim, e->h_aim, sizeof(double) * 9 * n));
-  TRY(ex_h2d(e, e->d_spec, e->h_spec, sizeof(SpecItem) * n));
-  // tile shapes first (a grid seen for the first time is tuned on its own data)
-  std::vector<const SpecLaunch*> Ls;
-  std::vector<GammaArgs> gas;
-  {
-    size_t gi = 0;
-    for (auto& kv : gg) {
-      dgx_rve* r0 = q[kv.second[0]].r;
-      gas.push_back(gamma_args(r0, true, true));
-      Ls.push_back(&spec_tiles(e, kv.first, r0, e->d_spec + spans[gi].first, spans[gi].second, gas.back()));
-      ++gi;
-    }
-  }
-  CK(cudaEventRecord(e->ev[2], e->st));
-  {
-    size_t gi = 0;
-    for (auto& kv : gg) {
-      dgx_rve* r0 = q[kv.second[0]].r;
-      const int o = spans[gi].first, cnt = spans[gi].second;
-      spec_convolve_batch(*Ls[gi], r0->num.precision == 1, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan,
-                          e->d_spec + o, cnt, gas[gi], e->st);
-      spec_div_finish_batch(e->d_spec + o, cnt, r0->sl.ndiv, r0->wgt, r0->cells[0], e->st);
-      e->launches += 6;
-      ++gi;
-    }
-  }
-  CK(cudaEventRecord(e->ev[3], e->st));
-  TRY(ex_d2h(e, e->h_rms, e->d_rms, sizeof(double) * n));
-  CK(cudaStreamSynchronize(e->st));
-  CK(cudaGetLastError());
-  {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[1] += ms; e->t_n[1]++;
-  }
-  for (int i = 0; i < n; ++i) q[i].r->err_div = e->h_rms[i];
-  return DGX_OK;
-}
-
-// fused reductions of every request
-static dgx_status ex_multi(Executor* e, std::vector<MultiReq>& q) {
+// fused reductions of every request: launches only (results after the round's sync)
+static dgx_status ex_multi_launch(Executor* e, std::vector<MultiReq>& q) {
   const int n = (int)q.size();
   if (n == 0) return DGX_OK;
   if (n > 2 * e->cap) { set_err("executor: %d reductions exceed capacity", n); return DGX_ERR_STATE; }
@@ -444,16 +349,179 @@ static dgx_status ex_multi(Executor* e, std::vector<MultiReq>& q) {
   k_multi_finish_batch<<<dim3(64, n), 32, 0, e->st>>>(e->d_multi);
   e->launches += 2;
   TRY(ex_d2h(e, e->h_mout, e->d_mout, sizeof(double) * 64 * n));
+  return DGX_OK;
+}
+
+// One round of device work with a single host synchronisation: the residual
+// evaluations R = Gamma * P(X) of every request (form_residual: constitutive pass,
+// P_av, stress BC step, spectral pass, divergence RMS), then the fused reductions
+// (which may read the residuals of this round).
+static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<MultiReq>& mq) {
+  const int n = (int)q.size();
+  if (n > e->cap) { set_err("executor: %d residual requests exceed capacity %d", n, e->cap); return DGX_ERR_STATE; }
+  int cand = -1;
+  std::vector<int> slot_of(n);
+  if (n > 0) {
+    // constitutive pass: items grouped by material, largest RVEs first in the tile queue
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      int c = memcmp(&q[a].r->mp, &q[b].r->mp, sizeof(MatParams));
+      if (c != 0) return c < 0;
+      return q[a].r->N > q[b].r->N;
+    });
+    if (e->tune_cons) {
+      cand = e->cons_round % CONS_VARIANTS;
+      if (e->cons_trials[cand] >= 3) cand = -1;
+    }
+    const int variant = cand >= 0 ? cand : e->cons_variant;
+    const int BS = cons_variant_bs(variant);
+    const int resident = e->res_by_variant[variant];
+    for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
+    CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, e->st));
+    CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * 16, e->st));
+    std::vector<std::pair<int, long long>> groups;    // (first slot, tiles)
+    {
+      long long tiles = 0;
+      int gstart = 0;
+      for (int j = 0; j < n; ++j) {
+        dgx_rve* r = q[order[j]].r;
+        if (j > 0 && memcmp(&r->mp, &q[order[j - 1]].r->mp, sizeof(MatParams)) != 0) {
+          groups.push_back({gstart, tiles}); gstart = j; tiles = 0;
+        }
+        ConsItem& it = e->h_cons[j];
+        it.ps = r->ps; it.F = q[order[j]].in; it.ldF = r->N; it.dt = r->delta_t; it.wgt = r->wgt;
+        it.Ppart = r->d_Ppart; it.ill = e->d_ill + j; it.tile0 = tiles;
+        tiles += (r->N + BS - 1) / BS;
+        r->n_eval++;
+        r->tangent_dt = r->delta_t;
+        e->point_evals += r->N;
+      }
+      groups.push_back({gstart, tiles});
+      if (groups.size() > 16) { set_err("executor: more than 16 materials in one round"); return DGX_ERR_UNSUPPORTED; }
+    }
+    for (int i = 0; i < n; ++i)
+      e->h_bcitem[i] = BcItem{q[i].r->d_bc, e->d_Pav + 9 * slot_of[i], e->d_aim + 9 * i, e->d_bcout + 10 * i};
+    // spectral items per grid group
+    std::map<GridKey, std::vector<int>> gg;
+    for (int i = 0; i < n; ++i) gg[grid_key(q[i].r)].push_back(i);
+    int off = 0;
+    std::vector<std::pair<int, int>> spans;
+    for (auto& kv : gg) {
+      spans.push_back({off, (int)kv.second.size()});
+      for (int i : kv.second) {
+        dgx_rve* r = q[i].r;
+        SpecItem& it = e->h_spec[off++];
+        it.in = r->ps.P; it.out = q[i].out; it.spec = r->spec; it.C_ref = r->d_Cref; it.aim = e->d_aim + 9 * i;
+        it.div_part = r->d_divpart; it.rms = e->d_rms + i;
+      }
+    }
+    TRY(ex_h2d(e, e->d_cons, e->h_cons, sizeof(ConsItem) * n));
+    TRY(ex_h2d(e, e->d_bcitem, e->h_bcitem, sizeof(BcItem) * n));
+    TRY(ex_h2d(e, e->d_spec, e->h_spec, sizeof(SpecItem) * n));
+    CK(cudaEventRecord(e->ev[0], e->st));
+    for (size_t g = 0; g < groups.size(); ++g) {
+      int j0 = groups[g].first;
+      int j1 = g + 1 < groups.size() ? groups[g + 1].first : n;
+      long long tiles = groups[g].second;
+      int grid = (int)std::min<long long>(tiles, resident);
+      launch_constitutive_batch(q[order[j0]].r->mp, e->d_cons + j0, j1 - j0, tiles, e->d_queue + g, e->cnt, e->st,
+                                variant, std::max(grid, 1));
+      e->launches++;
+    }
+    CK(cudaEventRecord(e->ev[1], e->st));
+    launch_pav_finish_batch(e->d_cons, n, e->d_Pav, e->st);
+    k_bc_batch<<<n, 32, 0, e->st>>>(e->d_bcitem);
+    e->launches += 2;
+    // tile shapes (a grid seen for the first time is tuned on its own data)
+    std::vector<const SpecLaunch*> Ls;
+    std::vector<GammaArgs> gas;
+    {
+      size_t gi = 0;
+      for (auto& kv : gg) {
+        dgx_rve* r0 = q[kv.second[0]].r;
+        gas.push_back(gamma_args(r0, true, true));
+        Ls.push_back(&spec_tiles(e, kv.first, r0, e->d_spec + spans[gi].first, spans[gi].second, gas.back()));
+        ++gi;
+      }
+    }
+    CK(cudaEventRecord(e->ev[2], e->st));
+    {
+      size_t gi = 0;
+      for (auto& kv : gg) {
+        dgx_rve* r0 = q[kv.second[0]].r;
+        const int o = spans[gi].first, cnt = spans[gi].second;
+        spec_convolve_batch(*Ls[gi], r0->num.precision == 1, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan,
+                            e->d_spec + o, cnt, gas[gi], e->st);
+        spec_div_finish_batch(e->d_spec + o, cnt, r0->sl.ndiv, r0->wgt, r0->cells[0], e->st);
+        e->launches += 6;
+        ++gi;
+      }
+    }
+    CK(cudaEventRecord(e->ev[3], e->st));
+    TRY(ex_d2h(e, e->h_Pav, e->d_Pav, sizeof(double) * 9 * n));
+    TRY(ex_d2h(e, e->h_ill, e->d_ill, sizeof(int) * n));
+    TRY(ex_d2h(e, e->h_rms, e->d_rms, sizeof(double) * n));
+    TRY(ex_d2h(e, e->h_bcout, e->d_bcout, sizeof(double) * 10 * n));
+    if (e->tune_cons) TRY(ex_d2h(e, e->h_cnt, e->cnt, sizeof(ConsCounters)));
+  }
+  TRY(ex_multi_launch(e, mq));
   CK(cudaStreamSynchronize(e->st));
   CK(cudaGetLastError());
-  for (int i = 0; i < n; ++i) memcpy(q[i].out, e->h_mout + 64 * i, sizeof(double) * (q[i].K + q[i].K2));
+  e->rounds++;
+  if (n > 0) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[0] += ms; e->t_n[0]++;
+    const float cons_ms = ms;
+    cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[1] += ms; e->t_n[1]++;
+    if (e->tune_cons) {
+      // cost per counted flop (the constitutive roofline's own flop model)
+      const ConsCounters& c1 = *e->h_cnt;
+      double flops = FLOPS_LP * (double)(c1.lp_iters - e->cnt_last.lp_iters) +
+                     FLOPS_JAC * (double)(c1.jac_iters - e->cnt_last.jac_iters) +
+                     FLOPS_STATE * (double)(c1.state_iters - e->cnt_last.state_iters) +
+                     FLOPS_FPI * (double)(c1.fpi_iters - e->cnt_last.fpi_iters);
+      e->cnt_last = c1;
+      if (cand >= 0 && flops > 0.0) e->cons_cost[cand][e->cons_trials[cand]++] = cons_ms / flops;
+      e->cons_round++;
+      bool all = true;
+      for (int k = 0; k < CONS_VARIANTS; ++k) all &= e->cons_trials[k] >= 3;
+      if (all) {
+        // median of three interleaved trials per variant
+        double med[CONS_VARIANTS];
+        for (int k = 0; k < CONS_VARIANTS; ++k) {
+          double* c = e->cons_cost[k];
+          med[k] = std::max(std::min(c[0], c[1]), std::min(std::max(c[0], c[1]), c[2]));
+        }
+        int best = 0;
+        for (int k = 1; k < CONS_VARIANTS; ++k) if (med[k] < med[best]) best = k;
+        e->cons_variant = best;
+        e->resident = e->res_by_variant[best];
+        e->tune_cons = false;
+      }
+    }
+    // host mirrors of the device BC step and the convergence inputs
+    for (int i = 0; i < n; ++i) {
+      dgx_rve* r = q[i].r;
+      const int j = slot_of[i];
+      memcpy(r->P_av, e->h_Pav + 9 * j, 9 * sizeof(double));
+      memcpy(r->F_aim, e->h_bcout + 10 * i, 9 * sizeof(double));
+      r->err_BC = e->h_bcout[10 * i + 9];
+      r->err_div = e->h_rms[i];
+      r->tangent_fresh = false;
+      if (e->h_ill[j]) r->terminally_ill = 1;
+      if (!r->num.lazy_tangent) TRY(ensure_tangent(r));
+    }
+  }
+  for (size_t i = 0; i < mq.size(); ++i)
+    memcpy(mq[i].out, e->h_mout + 64 * i, sizeof(double) * (mq[i].K + mq[i].K2));
   return DGX_OK;
 }
 
 // ------------------------------------------------------------------ solver state machine
 enum TState {
-  T_LC_BEGIN, T_INC_BEGIN, T_SUB_CHECK, T_SOLVE_BEGIN, T_N_INIT1, T_N_INIT2, T_FP_ITER, T_FP_NORM, T_FP_CHECK,
-  T_N_ITER, T_N_M1, T_N_LSQ, T_N_A1, T_N_DECIDE, T_SOLVE_END, T_SUB_AFTER, T_INC_END, T_DONE
+  T_LC_BEGIN, T_INC_BEGIN, T_SUB_CHECK, T_SOLVE_BEGIN, T_N_INIT2, T_FP_ITER, T_FP_CHECK,
+  T_N_ITER, T_N_LSQ, T_N_DECIDE, T_SOLVE_END, T_SUB_AFTER, T_INC_END, T_DONE
 };
 
 struct Task {
@@ -468,7 +536,8 @@ struct Task {
   int32_t conv = 0, sit = 0, sill = 0;
   TState pc = T_LC_BEGIN;
   dgx_status err = DGX_OK;
-  // pending device request: 0 none, 1 residual, 2 reductions
+  // pending device work: bit 0 a residual evaluation, bit 1 fused reductions (run after
+  // the residual of the same round when both are requested)
   int want = 0;
   const double* rin = nullptr;
   double* rout = nullptr;
@@ -488,14 +557,14 @@ struct Task {
   const dgx_loadstep* cur_step() const { return mode == 2 ? &steps[l] : steps; }
 };
 
-static void req_residual(Task& t, const double* in, double* out) { t.want = 1; t.rin = in; t.rout = out; }
+static void req_residual(Task& t, const double* in, double* out) { t.want |= 1; t.rin = in; t.rout = out; }
 static void req_multi(Task& t, int mode, const double* a, const double* b, const std::vector<const double*>& vs, int K2,
                       double* out) {
   MultiReq& m = t.mq[t.nmq];
   m.r = t.r; m.mode = mode; m.a = a; m.b = b; m.K = (int)vs.size(); m.K2 = K2; m.slot = t.nmq; m.out = out;
   for (int k = 0; k < m.K; ++k) m.v[k] = vs[k];
   t.nmq++;
-  t.want = 2;
+  t.want |= 2;
 }
 static dgx_status d2d9(dgx_rve* r, double* dst, const double* src) {
   CK(cudaMemcpyAsync(dst, src, sizeof(double) * 9 * r->N, cudaMemcpyDeviceToDevice, r->st));
@@ -544,10 +613,7 @@ static dgx_status advance(Task& t) {
         t.tmp.assign(2 * 32 + 2, 0.0);
         t.tmpA.assign(2, 0.0);
         req_residual(t, t.X, t.F);
-        t.pc = T_N_INIT1;
-        return DGX_OK;
-      case T_N_INIT1:
-        req_multi(t, 0, t.F, nullptr, {t.F}, 0, t.tmp.data());
+        req_multi(t, 0, t.F, nullptr, {t.F}, 0, t.tmp.data());      // |F|^2 in the same round
         t.pc = T_N_INIT2;
         return DGX_OK;
       case T_N_INIT2: {
@@ -572,9 +638,6 @@ static dgx_status advance(Task& t) {
         r->n_launch++;
         r->total_iter = t.k;
         req_residual(t, t.X, t.F);
-        t.pc = T_FP_NORM;
-        return DGX_OK;
-      case T_FP_NORM:
         req_multi(t, 0, t.F, nullptr, {t.F}, 0, t.tmp.data());
         t.pc = T_FP_CHECK;
         return DGX_OK;
@@ -594,17 +657,15 @@ static dgx_status advance(Task& t) {
         r->n_launch++;
         r->total_iter = t.k;
         req_residual(t, r->XM, r->FM);
-        t.pc = T_N_M1;
-        return DGX_OK;
-      case T_N_M1: {
-        // |FM|^2, <FM, Fdot_i>, <Fdot_ivec, Fdot_i> in one pass
-        std::vector<const double*> vs;
-        for (int i = 0; i < t.lh; ++i) vs.push_back(r->Fdot[i]);
-        vs.push_back(r->FM);
-        req_multi(t, 0, r->FM, r->Fdot[t.ivec], vs, t.lh, t.tmp.data());
+        {
+          // |FM|^2, <FM, Fdot_i>, <Fdot_ivec, Fdot_i> in one pass, after the residual
+          std::vector<const double*> vs;
+          for (int i = 0; i < t.lh; ++i) vs.push_back(r->Fdot[i]);
+          vs.push_back(r->FM);
+          req_multi(t, 0, r->FM, r->Fdot[t.ivec], vs, t.lh, t.tmp.data());
+        }
         t.pc = T_N_LSQ;
         return DGX_OK;
-      }
       case T_N_LSQ: {
         const int m = r->num.ngmres_m, l = t.lh;
         t.fMnorm = std::sqrt(t.tmp[l]);
@@ -627,13 +688,9 @@ static dgx_status advance(Task& t) {
         CK(h2d(r, r->d_beta, t.beta.data(), sizeof(double) * l));
         launch_combine(r->XA, r->XM, xl, l, 1.0 - alph, r->d_beta, n9, r->nb_red, r->st);
         r->n_launch++;
-        req_residual(t, r->XA, r->FA);
-        t.pc = T_N_A1;
-        return DGX_OK;
-      }
-      case T_N_A1: {
         if (t.fminnorm > t.fMnorm) t.fminnorm = t.fMnorm;
-        // |FA|^2 ; |XA - XM|^2, |XA - Xdot_i|^2
+        req_residual(t, r->XA, r->FA);
+        // |FA|^2 ; |XA - XM|^2, |XA - Xdot_i|^2 after the residual
         req_multi(t, 0, r->FA, nullptr, {r->FA}, 0, t.tmpA.data());
         std::vector<const double*> ds;
         ds.push_back(r->XM);
@@ -737,19 +794,18 @@ static double remaining_work(const Task& t) {
   return (double)t.r->N * std::max(1.0, inc);
 }
 
-// One round: serve the parked requests, then advance the tasks that were served.  With
-// a point budget, residual evaluations are served least remaining work first until the
-// budget is filled (at least one per round); a task passed over gains priority each
-// round it waits (its work counts half per skipped round), so none starves.  Fused
-// reductions are cheap and always served.  A task that fails is finished with its
-// error; the others go on.
+// One round: serve the parked requests (one host synchronisation), then advance the
+// tasks that were served.  With a point budget, residual evaluations are served least
+// remaining work first until the budget is filled (at least one per round); a task
+// passed over gains priority each round it waits (its work counts half per skipped
+// round), so none starves.  Requests of reductions alone are cheap and always served.
+// A task that fails is finished with its error; the others go on.
 static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks, int64_t point_budget) {
   std::vector<Task*> res_tasks, served;
-  std::vector<MultiReq> mq;
   for (Task* t : tasks) {
     if (t->done() || t->want == 0) continue;
-    if (t->want == 1) res_tasks.push_back(t);
-    else { for (int i = 0; i < t->nmq; ++i) mq.push_back(t->mq[i]); served.push_back(t); }
+    if (t->want & 1) res_tasks.push_back(t);
+    else served.push_back(t);                         // reductions only
   }
   int64_t total = 0;
   for (Task* t : res_tasks) total += t->r->N;
@@ -767,9 +823,9 @@ static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks, int64_t po
   }
   std::vector<ResReq> rq;
   for (Task* t : res_tasks) { rq.push_back({t->r, t->rin, t->rout}); t->skips = 0; served.push_back(t); }
-  TRY(ex_residual(e, rq));
-  TRY(ex_multi(e, mq));
-  e->rounds++;
+  std::vector<MultiReq> mq;
+  for (Task* t : served) for (int i = 0; i < t->nmq; ++i) mq.push_back(t->mq[i]);
+  TRY(ex_round(e, rq, mq));
   for (Task* t : served) {
     t->want = 0; t->nmq = 0;
     dgx_status s = advance(*t);

@@ -77,6 +77,17 @@ struct ConsCounters {
 // hardening from the slip rates of the last Lp iteration, damper, state update).
 constexpr double FLOPS_LP = 537.0, FLOPS_JAC = 1184.0, FLOPS_STATE = 1028.0, FLOPS_FPI = 815.0;
 
+// Stress boundary condition of one RVE's solve, resident on the device so that the
+// BC step of a residual evaluation (form_residual) needs no host round trip.
+struct BcBlock {
+  double S[81];              // masked compliance (rotated frame)
+  double F_aim[9];           // in / out: updated by every residual evaluation
+  double P_aim[9];
+  double R[9];               // rotation matrix of the BC frame, column-major
+  int mask[9];               // 1: stress component not prescribed
+  int rotated;               // the BC frame is not the identity
+};
+
 // One RVE of a batched constitutive launch (device table, ordered by tile0).
 struct ConsItem {
   PointState ps;

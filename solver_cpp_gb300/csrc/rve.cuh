@@ -37,6 +37,7 @@ struct dgx_rve {
   double *d_xi_x = nullptr, *d_xi_y = nullptr, *d_xi_z = nullptr;
   double* d_dPdF = nullptr;        // optional (81 planes) for the boundary call
   double *d_un = nullptr, *d_up = nullptr, *d_Favg = nullptr;   // optional: coordinate update
+  dgx::BcBlock* d_bc = nullptr;    // stress BC of the current solve (device copy)
   int32_t* d_mat = nullptr;
   double* d_Rm = nullptr;
   int n_materials = 0;
@@ -105,6 +106,7 @@ struct VecList { const double* v[32]; };
 
 // solver.cu: host steps of MechSolverBasic / DamaskGrid shared by every execution mode
 void rotate2(const double* q, const double* T, double* out, bool active);
+void qu2om(const double* q, double* om);
 void lsq_svd(int l, const double* H, double* b);
 int converged(dgx_rve* r);
 double forward_time(const dgx_loadstep* ls, int inc, int sub_step_factor, int cut_back_level);
@@ -112,9 +114,8 @@ dgx_status commit(dgx_rve* r);
 dgx_status ensure_tangent(dgx_rve* r);
 // after the constitutive pass of a residual evaluation (P_av, ill on the host)
 dgx_status post_constitutive(dgx_rve* r, int ill, bool want_tangent);
-// stress boundary condition step of form_residual: F_aim, err_BC, rotated dF_aim
-void residual_bc(dgx_rve* r, double aim[9]);
-// MechSolverBasic::calculate_solution before and after SNESSolve
+// MechSolverBasic::calculate_solution before and after SNESSolve; the prologue also
+// uploads the solve's stress BC (BcBlock) to the device
 dgx_status solve_prologue(dgx_rve* r);
 void solve_epilogue(dgx_rve* r, int reason, int32_t* conv, int32_t* iterations, int32_t* ill_out);
 // volume average of F (the record of an increment)

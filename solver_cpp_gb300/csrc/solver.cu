@@ -470,22 +470,6 @@ GammaArgs gamma_args(dgx_rve* r, bool gamma, bool div) {
   return ga;
 }
 
-// stress-BC part of form_residual (mech_solver_basic.cpp:321-334): dF_aim = S : P_av,
-// F_aim -= dF_aim, err_BC; the rotated dF_aim is the zero-frequency value of Gamma * P
-void residual_bc(dgx_rve* r, double aim[9]) {
-  double dF[9];
-  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) {
-    double s = 0.0;
-    for (int k = 0; k < 3; ++k) for (int l = 0; l < 3; ++l) s += r->S[i + 3 * j + 9 * k + 27 * l] * r->P_av[k + 3 * l];
-    dF[i + 3 * j] = s;
-  }
-  for (int k = 0; k < 9; ++k) r->F_aim[k] -= dF[k];
-  double err = 0.0;
-  for (int k = 0; k < 9; ++k) if (!r->stress_mask[k]) err = std::max(err, std::fabs(r->P_av[k] - r->P_aim[k]));
-  r->err_BC = err;
-  rotate2(r->rot_q, dF, aim, true);
-}
-
 int converged(dgx_rve* r) {
   double mx = -1.7976931348623157e308;
   for (int k = 0; k < 9; ++k) mx = std::max(mx, r->P_av[k]);
@@ -504,6 +488,16 @@ dgx_status solve_prologue(dgx_rve* r) {
     for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
     CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
   }
+  // the BC state the device updates during the solve (same values as the host copy)
+  BcBlock bc;
+  memcpy(bc.S, r->S, sizeof(bc.S));
+  memcpy(bc.F_aim, r->F_aim, sizeof(bc.F_aim));
+  memcpy(bc.P_aim, r->P_aim, sizeof(bc.P_aim));
+  qu2om(r->rot_q, bc.R);
+  memcpy(bc.mask, r->stress_mask, sizeof(bc.mask));
+  bc.rotated = !(r->rot_q[0] == 1.0 && r->rot_q[1] == 0.0 && r->rot_q[2] == 0.0 && r->rot_q[3] == 0.0);
+  CK(h2d(r, r->d_bc, &bc, sizeof(bc)));
+  CK(cudaStreamSynchronize(r->st));       // bc is a stack copy
   return DGX_OK;
 }
 
@@ -644,6 +638,7 @@ static dgx_status allocate_buffers(dgx_rve* r, const int32_t cells[3], const dgx
   AL(&r->d_divpart, r->sl.ndiv);
   AL(&r->d_redpart, 128 * (int64_t)r->nb_red);   // two concurrent fused reductions of up to 64 sums
   AL(&r->d_redout, 128); AL(&r->d_beta, 32);
+  AL(&r->d_bc, 1);
   AL(&r->d_Pav, 9); AL(&r->d_Cvol, 81); AL(&r->d_Cmm, 81); AL(&r->d_Cref, 81); AL(&r->d_aim, 9); AL(&r->d_rms, 1);
   AL(&r->d_ill, 1); AL(&r->d_cnt, 1);
   AL(&r->d_xi_x, cells[0] / 2 + 1); AL(&r->d_xi_y, cells[1]); AL(&r->d_xi_z, cells[2]);
