@@ -191,7 +191,7 @@ dgx_status dgx_get(dgx_rve* rve, const char* name, double* out);
  * integrations (sub-steps), [2] Lp Newton iterations, [3] tangent evaluations,
  * [4] kernel launches issued by the library, [5] Lp Jacobian factorisations,
  * [6] host-to-device bytes, [7] device-to-host bytes copied by the library,
- * [8] fixed-point state iterations, [9] reserved. */
+ * [8] fixed-point state iterations, [9] rounds issued as CUDA graph replays. */
 dgx_status dgx_counters(const dgx_rve* rve, int64_t out[10]);
 /* FP64 flops per counted unit of the constitutive kernel (FMA = 2): [0] Lp iteration,
  * [1] Jacobian, [2] state integration, [3] fixed-point iteration.  No reference
@@ -213,8 +213,8 @@ void* dgx_rve_stream(const dgx_rve* rve);
  * rounds (continuous batching); an RVE in a batch may not be driven by the
  * single-RVE calls until it is removed. */
 typedef struct dgx_batch dgx_batch;
-/* capacity: most members at once; cons_block: points per constitutive block (64,
- * 128 or 256), or 0 to let the batch's autotuner pick it from the first rounds (it
+/* capacity: most members at once; cons_block: points per constitutive block (32,
+ * 64, 128 or 256), or 0 to let the batch's autotuner pick it from the first rounds (it
  * also picks each grid's FFT tile shape; DGX_AUTOTUNE=0 turns both off).  Results do
  * not depend on these choices. */
 dgx_status dgx_batch_create(int32_t capacity, int32_t cons_block, dgx_batch** out);
@@ -236,7 +236,9 @@ dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
 /* ms: CUDA-event time of [0] constitutive launches, [1] spectral chains, [2] unused;
  * out: [0] point evaluations, [1] state integrations, [2] Lp iterations, [3] rounds,
  * [4] launches of the batched kernels, [5] Jacobian factorisations, [6] h2d bytes,
- * [7] d2h bytes of the executor, [8] fixed-point iterations, [9] reserved. */
+ * [7] d2h bytes of the executor, [8] fixed-point iterations, [9] rounds issued as a
+ * CUDA graph replay (a round's launch sequence is captured once its launch parameters
+ * repeat; DGX_GRAPHS=0 in the environment at creation launches every round directly). */
 dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[10]);
 void* dgx_batch_stream(const dgx_batch* batch);
 /* Cap the residual evaluations served per round at `points` cells (0: no cap).  Above

@@ -24,8 +24,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
+#include <cstddef>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -160,6 +163,15 @@ struct MultiReq {
   double* out;               // host, K + K2 values
 };
 
+struct IssueCount { int64_t launches = 0, h2d = 0, d2h = 0; };
+struct GraphEntry {
+  std::string sig;
+  cudaGraphExec_t exec;
+  IssueCount count;
+  int64_t last_use;
+};
+constexpr size_t GRAPH_CACHE = 16;
+
 struct Executor {
   cudaStream_t st = nullptr;
   int cap = 0;                               // residual items per round; 2 cap reductions
@@ -179,9 +191,9 @@ struct Executor {
   // rounds per variant, and per grid the FFT tile shape, timed on the first round's data
   // (results do not depend on either)
   bool tune_cons = true, tune_spec = true;
-  int res_by_variant[CONS_VARIANTS] = {0, 0, 0, 0};
+  int res_by_variant[CONS_VARIANTS] = {};
   double cons_cost[CONS_VARIANTS][3] = {};
-  int cons_trials[CONS_VARIANTS] = {0, 0, 0, 0}, cons_round = 0;
+  int cons_trials[CONS_VARIANTS] = {}, cons_round = 0;
   ConsCounters cnt_last{};
   ConsCounters* h_cnt = nullptr;
   std::map<std::tuple<int, int, int, double, double, double, int, int, int>, SpecLaunch> spec_tuned;
@@ -189,11 +201,18 @@ struct Executor {
   double t_ms[3] = {0, 0, 0};
   int64_t t_n[3] = {0, 0, 0};
   int64_t launches = 0, bytes_h2d = 0, bytes_d2h = 0, point_evals = 0, rounds = 0;
+  // CUDA graphs of rounds (see ex_issue_round)
+  bool use_graphs = true;
+  std::vector<GraphEntry> graphs;
+  std::vector<size_t> seen = std::vector<size_t>(64, 0);   // signature hashes of recent direct rounds
+  size_t seen_pos = 0;
+  int64_t graph_clock = 0, graph_rounds = 0, graph_captures = 0;
   std::vector<void*> dev, host;
 };
 
 void executor_destroy(Executor* e) {
   if (!e) return;
+  for (GraphEntry& g : e->graphs) cudaGraphExecDestroy(g.exec);
   for (void* p : e->dev) cudaFree(p);
   for (void* p : e->host) cudaFreeHost(p);
   for (auto& v : e->ev) if (v) cudaEventDestroy(v);
@@ -217,7 +236,7 @@ static dgx_status ex_alloc(Executor* e, T** d, T** h, size_t n) {
 dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons_block, Executor** out) {
   Executor* e = new Executor();
   e->st = st; e->cap = cap;
-  e->cons_variant = cons_block == 64 ? 0 : (cons_block == 256 ? 2 : 1);       // <= 0: autotuned
+  e->cons_variant = cons_block == 64 ? 0 : cons_block == 256 ? 2 : cons_block == 32 ? 4 : 1;   // <= 0: autotuned
   dgx_status s = DGX_OK;
 #define EA(d, h, n) do { s = ex_alloc(e, d, h, n); if (s != DGX_OK) { executor_destroy(e); return s; } } while (0)
   EA(&e->d_cons, &e->h_cons, cap);
@@ -241,33 +260,26 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   const char* at = std::getenv("DGX_AUTOTUNE");
   const bool tune = !(at && at[0] == '0');
   e->tune_cons = tune && cons_block <= 0;       // an explicit block size is kept
-  const char* cv = std::getenv("DGX_CONS_VARIANT");   // pin a launch variant (0..3) for measurements
+  const char* cv = std::getenv("DGX_CONS_VARIANT");   // pin a launch variant (0..4) for measurements
   if (cv && cv[0] >= '0' && cv[0] < '0' + CONS_VARIANTS && cv[1] == 0) {
     e->cons_variant = cv[0] - '0';
     e->resident = e->res_by_variant[e->cons_variant];
     e->tune_cons = false;
   }
   e->tune_spec = tune;
+  const char* gr = std::getenv("DGX_GRAPHS");          // 0: launch every round directly
+  e->use_graphs = !(gr && gr[0] == '0');
   if (cudaMemcpyAsync(&e->cnt_last, e->cnt, sizeof(ConsCounters), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) { executor_destroy(e); set_err("executor: counters"); return DGX_ERR_CUDA; }
   *out = e;
   return DGX_OK;
 }
 
-void executor_stats(const Executor* e, double ms[3], int64_t n[3], int64_t* launches, int64_t* h2d_b, int64_t* d2h_b) {
+void executor_stats(const Executor* e, double ms[3], int64_t n[3], int64_t* launches, int64_t* h2d_b, int64_t* d2h_b,
+                    int64_t* graph_rounds) {
   for (int i = 0; i < 3; ++i) { ms[i] += e->t_ms[i]; n[i] += e->t_n[i]; }
   *launches += e->launches; *h2d_b += e->bytes_h2d; *d2h_b += e->bytes_d2h;
-}
-
-static dgx_status ex_h2d(Executor* e, void* d, const void* h, size_t b) {
-  e->bytes_h2d += (int64_t)b;
-  CK(cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, e->st));
-  return DGX_OK;
-}
-static dgx_status ex_d2h(Executor* e, void* h, const void* d, size_t b) {
-  e->bytes_d2h += (int64_t)b;
-  CK(cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, e->st));
-  return DGX_OK;
+  if (graph_rounds) *graph_rounds += e->graph_rounds;
 }
 
 // equal grids (and spectral precision, derivative, geometry) share a launch
@@ -328,10 +340,62 @@ static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0
   return e->spec_tuned.emplace(key, L).first->second;
 }
 
-// fused reductions of every request: launches only (results after the round's sync)
-static dgx_status ex_multi_launch(Executor* e, std::vector<MultiReq>& q) {
+// ------------------------------------------------------------------ round plan, issue and graph
+// A round is planned on the host (tables staged in pinned memory, every launch
+// parameter fixed) and then issued: directly, or as a CUDA graph captured from the
+// same issue code.  The graph's copy nodes read the staged tables from the same
+// pinned buffers at every replay, so a graph depends only on the launch parameters:
+// the plan's signature lists every value a launch takes (counts, grid sizes, the
+// material parameters, the FFT plans with their twiddle pointers, the Gamma
+// arguments), and a graph is replayed only for a round whose signature is identical.
+struct ConsGroup { int j0, cnt, grid; long long tiles; const MatParams* mp; };
+struct SpecGroup {
+  GridKey key;
+  dgx_rve* r0;
+  const SpecLaunch* L;      // null: not tuned yet (tuned while the round is issued directly)
+  GammaArgs ga;
+  int o, cnt;
+};
+struct RoundPlan {
+  int n = 0, nm = 0, maxnb = 1, variant = 1;
+  bool cnt_d2h = false;
+  std::vector<ConsGroup> cons;
+  std::vector<SpecGroup> spec;
+};
+
+struct Sig {
+  std::string b;
+  void raw(const void* p, size_t n) { b.append(reinterpret_cast<const char*>(p), n); }
+  template <typename T> void put(const T& v) { raw(&v, sizeof(T)); }
+};
+// MatParams without its tail padding (the bytes the kernel parameter carries)
+constexpr size_t MATPARAMS_BYTES = offsetof(MatParams, a_quarters) + sizeof(int);
+
+static std::string plan_signature(const RoundPlan& p) {
+  Sig s;
+  s.put(p.n); s.put(p.nm); s.put(p.maxnb); s.put(p.variant); s.put(p.cnt_d2h);
+  for (const ConsGroup& c : p.cons) { s.put(c.j0); s.put(c.cnt); s.put(c.grid); s.put(c.tiles); s.raw(c.mp, MATPARAMS_BYTES); }
+  for (const SpecGroup& g : p.spec) {
+    const SpecLaunch& L = *g.L;
+    s.put(L.g.N0); s.put(L.g.N1); s.put(L.g.N2); s.put(L.g.N0r); s.put(L.g.N); s.put(L.g.Nh);
+    s.put(L.LX); s.put(L.TIy); s.put(L.TIz); s.put(L.smx); s.put(L.smy); s.put(L.smz);
+    s.put(L.nbx); s.put(L.nby); s.put(L.nbz); s.put(L.ndiv);
+    const GammaArgs& a = g.ga;
+    s.put(a.xi_x); s.put(a.xi_y); s.put(a.xi_z); s.raw(a.resc, sizeof(a.resc)); s.put(a.C_ref); s.put(a.aim);
+    s.put(a.do_gamma); s.put(a.do_div); s.put(a.store_fwd); s.put(a.zsign); s.put(a.div_part);
+    for (int k = 0; k < 3; ++k) {
+      const AxisPlan& ap = g.r0->ax[k].plan;
+      s.put(ap.n); s.put(ap.nstages); s.raw(ap.radix, sizeof(ap.radix)); s.put(ap.tw); s.put(ap.twf);
+    }
+    s.put(g.r0->num.precision); s.put(g.r0->sl.ndiv); s.put(g.r0->wgt); s.put(g.r0->cells[0]);
+    s.put(g.o); s.put(g.cnt);
+  }
+  return s.b;
+}
+
+// stage the fused reductions of every request (results after the round's sync)
+static dgx_status ex_multi_stage(Executor* e, std::vector<MultiReq>& q, RoundPlan& p) {
   const int n = (int)q.size();
-  if (n == 0) return DGX_OK;
   if (n > 2 * e->cap) { set_err("executor: %d reductions exceed capacity", n); return DGX_ERR_STATE; }
   int maxnb = 1;
   for (int i = 0; i < n; ++i) {
@@ -344,11 +408,129 @@ static dgx_status ex_multi_launch(Executor* e, std::vector<MultiReq>& q) {
     it.out = e->d_mout + 64 * i;
     maxnb = std::max(maxnb, r->nb_red);
   }
-  TRY(ex_h2d(e, e->d_multi, e->h_multi, sizeof(MultiItem) * n));
-  k_multi_batch<<<dim3(maxnb, n), RB, 0, e->st>>>(e->d_multi);
-  k_multi_finish_batch<<<dim3(64, n), 32, 0, e->st>>>(e->d_multi);
-  e->launches += 2;
-  TRY(ex_d2h(e, e->h_mout, e->d_mout, sizeof(double) * 64 * n));
+  p.nm = n; p.maxnb = maxnb;
+  return DGX_OK;
+}
+
+// The device work of a planned round, in stream order: constitutive pass, P_av, stress
+// BC step, spectral pass with the divergence RMS, then the fused reductions, and the
+// copies of the results to the pinned host buffers.  capture: recorded into a graph
+// (event records become event nodes; nothing runs until the graph is launched).
+static dgx_status ex_issue(Executor* e, RoundPlan& p, bool capture, IssueCount& c) {
+  cudaStream_t st = e->st;
+  auto rec = [&](int k) {
+    return capture ? cudaEventRecordWithFlags(e->ev[k], st, cudaEventRecordExternal) : cudaEventRecord(e->ev[k], st);
+  };
+  auto h2d = [&](void* d, const void* h, size_t b) { c.h2d += (int64_t)b; return cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, st); };
+  auto d2h = [&](void* h, const void* d, size_t b) { c.d2h += (int64_t)b; return cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, st); };
+  const int n = p.n;
+  if (n > 0) {
+    CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, st));
+    CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * 16, st));
+    CK(h2d(e->d_cons, e->h_cons, sizeof(ConsItem) * n));
+    CK(h2d(e->d_bcitem, e->h_bcitem, sizeof(BcItem) * n));
+    CK(h2d(e->d_spec, e->h_spec, sizeof(SpecItem) * n));
+    CK(rec(0));
+    for (size_t g = 0; g < p.cons.size(); ++g) {
+      const ConsGroup& cg = p.cons[g];
+      launch_constitutive_batch(*cg.mp, e->d_cons + cg.j0, cg.cnt, cg.tiles, e->d_queue + g, e->cnt, st, p.variant,
+                                cg.grid);
+      c.launches++;
+    }
+    CK(rec(1));
+    launch_pav_finish_batch(e->d_cons, n, e->d_Pav, st);
+    k_bc_batch<<<n, 32, 0, st>>>(e->d_bcitem);
+    c.launches += 2;
+    // a grid seen for the first time is tuned here, on this round's own data (direct issue only)
+    for (SpecGroup& g : p.spec)
+      if (!g.L) g.L = &spec_tiles(e, g.key, g.r0, e->d_spec + g.o, g.cnt, g.ga);
+    CK(rec(2));
+    for (const SpecGroup& g : p.spec) {
+      dgx_rve* r0 = g.r0;
+      spec_convolve_batch(*g.L, r0->num.precision == 1, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan,
+                          e->d_spec + g.o, g.cnt, g.ga, st);
+      spec_div_finish_batch(e->d_spec + g.o, g.cnt, r0->sl.ndiv, r0->wgt, r0->cells[0], st);
+      c.launches += 6;
+    }
+    CK(rec(3));
+    CK(d2h(e->h_Pav, e->d_Pav, sizeof(double) * 9 * n));
+    CK(d2h(e->h_ill, e->d_ill, sizeof(int) * n));
+    CK(d2h(e->h_rms, e->d_rms, sizeof(double) * n));
+    CK(d2h(e->h_bcout, e->d_bcout, sizeof(double) * 10 * n));
+    if (p.cnt_d2h) CK(d2h(e->h_cnt, e->cnt, sizeof(ConsCounters)));
+  }
+  if (p.nm > 0) {
+    CK(h2d(e->d_multi, e->h_multi, sizeof(MultiItem) * p.nm));
+    k_multi_batch<<<dim3(p.maxnb, p.nm), RB, 0, st>>>(e->d_multi);
+    k_multi_finish_batch<<<dim3(64, p.nm), 32, 0, st>>>(e->d_multi);
+    c.launches += 2;
+    CK(d2h(e->h_mout, e->d_mout, sizeof(double) * 64 * p.nm));
+  }
+  CK(cudaGetLastError());
+  return DGX_OK;
+}
+
+static void ex_count(Executor* e, const IssueCount& c) {
+  e->launches += c.launches; e->bytes_h2d += c.h2d; e->bytes_d2h += c.d2h;
+}
+
+// Issue a planned round: replay the graph of an identical earlier round, capture one
+// for a signature seen for the second time, else launch directly.  Graphs are kept
+// per executor (least recently used out beyond GRAPH_CACHE).
+static dgx_status ex_issue_round(Executor* e, RoundPlan& p) {
+  bool graphable = e->use_graphs && !p.cnt_d2h && (p.n > 0 || p.nm > 0);
+  for (const SpecGroup& g : p.spec) graphable &= g.L != nullptr;
+  IssueCount c;
+  if (!graphable) {
+    TRY(ex_issue(e, p, false, c));
+    ex_count(e, c);
+    return DGX_OK;
+  }
+  std::string sig = plan_signature(p);
+  for (GraphEntry& g : e->graphs)
+    if (g.sig == sig) {
+      g.last_use = ++e->graph_clock;
+      CK(cudaGraphLaunch(g.exec, e->st));
+      ex_count(e, g.count);
+      e->graph_rounds++;
+      return DGX_OK;
+    }
+  const size_t h = std::hash<std::string>{}(sig);
+  bool seen = false;
+  for (size_t v : e->seen) seen |= v == h;
+  if (!seen) {
+    e->seen[e->seen_pos++ % e->seen.size()] = h;
+    TRY(ex_issue(e, p, false, c));
+    ex_count(e, c);
+    return DGX_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeRelaxed));
+  dgx_status s = ex_issue(e, p, true, c);
+  cudaError_t ce = cudaStreamEndCapture(e->st, &graph);
+  if (s == DGX_OK && ce == cudaSuccess && graph) ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (s != DGX_OK || ce != cudaSuccess || !exec) {
+    // capture refused: this executor launches directly from now on
+    (void)cudaGetLastError();
+    e->use_graphs = false;
+    IssueCount d;
+    TRY(ex_issue(e, p, false, d));
+    ex_count(e, d);
+    return DGX_OK;
+  }
+  if (e->graphs.size() >= GRAPH_CACHE) {
+    auto lru = std::min_element(e->graphs.begin(), e->graphs.end(),
+                                [](const GraphEntry& a, const GraphEntry& b) { return a.last_use < b.last_use; });
+    cudaGraphExecDestroy(lru->exec);
+    e->graphs.erase(lru);
+  }
+  e->graphs.push_back(GraphEntry{std::move(sig), exec, c, ++e->graph_clock});
+  e->graph_captures++;
+  CK(cudaGraphLaunch(exec, e->st));
+  ex_count(e, c);
+  e->graph_rounds++;
   return DGX_OK;
 }
 
@@ -361,6 +543,8 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
   if (n > e->cap) { set_err("executor: %d residual requests exceed capacity %d", n, e->cap); return DGX_ERR_STATE; }
   int cand = -1;
   std::vector<int> slot_of(n);
+  RoundPlan p;
+  p.n = n;
   if (n > 0) {
     // constitutive pass: items grouped by material, largest RVEs first in the tile queue
     std::vector<int> order(n);
@@ -374,20 +558,21 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
       cand = e->cons_round % CONS_VARIANTS;
       if (e->cons_trials[cand] >= 3) cand = -1;
     }
-    const int variant = cand >= 0 ? cand : e->cons_variant;
-    const int BS = cons_variant_bs(variant);
-    const int resident = e->res_by_variant[variant];
+    p.variant = cand >= 0 ? cand : e->cons_variant;
+    const int BS = cons_variant_bs(p.variant);
+    const int resident = e->res_by_variant[p.variant];
     for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
-    CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, e->st));
-    CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * 16, e->st));
-    std::vector<std::pair<int, long long>> groups;    // (first slot, tiles)
     {
       long long tiles = 0;
       int gstart = 0;
+      auto close_group = [&](int jend) {
+        const int grid = (int)std::max<long long>(1, std::min<long long>(tiles, resident));
+        p.cons.push_back(ConsGroup{gstart, jend - gstart, grid, tiles, &q[order[gstart]].r->mp});
+      };
       for (int j = 0; j < n; ++j) {
         dgx_rve* r = q[order[j]].r;
         if (j > 0 && memcmp(&r->mp, &q[order[j - 1]].r->mp, sizeof(MatParams)) != 0) {
-          groups.push_back({gstart, tiles}); gstart = j; tiles = 0;
+          close_group(j); gstart = j; tiles = 0;
         }
         ConsItem& it = e->h_cons[j];
         it.ps = r->ps; it.F = q[order[j]].in; it.ldF = r->N; it.dt = r->delta_t; it.wgt = r->wgt;
@@ -397,8 +582,8 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
         r->tangent_dt = r->delta_t;
         e->point_evals += r->N;
       }
-      groups.push_back({gstart, tiles});
-      if (groups.size() > 16) { set_err("executor: more than 16 materials in one round"); return DGX_ERR_UNSUPPORTED; }
+      close_group(n);
+      if (p.cons.size() > 16) { set_err("executor: more than 16 materials in one round"); return DGX_ERR_UNSUPPORTED; }
     }
     for (int i = 0; i < n; ++i)
       e->h_bcitem[i] = BcItem{q[i].r->d_bc, e->d_Pav + 9 * slot_of[i], e->d_aim + 9 * i, e->d_bcout + 10 * i};
@@ -406,9 +591,11 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
     std::map<GridKey, std::vector<int>> gg;
     for (int i = 0; i < n; ++i) gg[grid_key(q[i].r)].push_back(i);
     int off = 0;
-    std::vector<std::pair<int, int>> spans;
     for (auto& kv : gg) {
-      spans.push_back({off, (int)kv.second.size()});
+      dgx_rve* r0 = q[kv.second[0]].r;
+      auto t = e->spec_tuned.find(kv.first);
+      p.spec.push_back(SpecGroup{kv.first, r0, t == e->spec_tuned.end() ? nullptr : &t->second,
+                                 gamma_args(r0, true, true), off, (int)kv.second.size()});
       for (int i : kv.second) {
         dgx_rve* r = q[i].r;
         SpecItem& it = e->h_spec[off++];
@@ -416,56 +603,10 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
         it.div_part = r->d_divpart; it.rms = e->d_rms + i;
       }
     }
-    TRY(ex_h2d(e, e->d_cons, e->h_cons, sizeof(ConsItem) * n));
-    TRY(ex_h2d(e, e->d_bcitem, e->h_bcitem, sizeof(BcItem) * n));
-    TRY(ex_h2d(e, e->d_spec, e->h_spec, sizeof(SpecItem) * n));
-    CK(cudaEventRecord(e->ev[0], e->st));
-    for (size_t g = 0; g < groups.size(); ++g) {
-      int j0 = groups[g].first;
-      int j1 = g + 1 < groups.size() ? groups[g + 1].first : n;
-      long long tiles = groups[g].second;
-      int grid = (int)std::min<long long>(tiles, resident);
-      launch_constitutive_batch(q[order[j0]].r->mp, e->d_cons + j0, j1 - j0, tiles, e->d_queue + g, e->cnt, e->st,
-                                variant, std::max(grid, 1));
-      e->launches++;
-    }
-    CK(cudaEventRecord(e->ev[1], e->st));
-    launch_pav_finish_batch(e->d_cons, n, e->d_Pav, e->st);
-    k_bc_batch<<<n, 32, 0, e->st>>>(e->d_bcitem);
-    e->launches += 2;
-    // tile shapes (a grid seen for the first time is tuned on its own data)
-    std::vector<const SpecLaunch*> Ls;
-    std::vector<GammaArgs> gas;
-    {
-      size_t gi = 0;
-      for (auto& kv : gg) {
-        dgx_rve* r0 = q[kv.second[0]].r;
-        gas.push_back(gamma_args(r0, true, true));
-        Ls.push_back(&spec_tiles(e, kv.first, r0, e->d_spec + spans[gi].first, spans[gi].second, gas.back()));
-        ++gi;
-      }
-    }
-    CK(cudaEventRecord(e->ev[2], e->st));
-    {
-      size_t gi = 0;
-      for (auto& kv : gg) {
-        dgx_rve* r0 = q[kv.second[0]].r;
-        const int o = spans[gi].first, cnt = spans[gi].second;
-        spec_convolve_batch(*Ls[gi], r0->num.precision == 1, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan,
-                            e->d_spec + o, cnt, gas[gi], e->st);
-        spec_div_finish_batch(e->d_spec + o, cnt, r0->sl.ndiv, r0->wgt, r0->cells[0], e->st);
-        e->launches += 6;
-        ++gi;
-      }
-    }
-    CK(cudaEventRecord(e->ev[3], e->st));
-    TRY(ex_d2h(e, e->h_Pav, e->d_Pav, sizeof(double) * 9 * n));
-    TRY(ex_d2h(e, e->h_ill, e->d_ill, sizeof(int) * n));
-    TRY(ex_d2h(e, e->h_rms, e->d_rms, sizeof(double) * n));
-    TRY(ex_d2h(e, e->h_bcout, e->d_bcout, sizeof(double) * 10 * n));
-    if (e->tune_cons) TRY(ex_d2h(e, e->h_cnt, e->cnt, sizeof(ConsCounters)));
+    p.cnt_d2h = e->tune_cons;
   }
-  TRY(ex_multi_launch(e, mq));
+  TRY(ex_multi_stage(e, mq, p));
+  TRY(ex_issue_round(e, p));
   CK(cudaStreamSynchronize(e->st));
   CK(cudaGetLastError());
   e->rounds++;
@@ -978,7 +1119,7 @@ extern "C" dgx_status dgx_batch_stats(const dgx_batch* b, double ms[3], int64_t 
     CK(cudaMemcpy(&c, e->cnt, sizeof(c), cudaMemcpyDeviceToHost));
     out[0] = e->point_evals; out[1] = (int64_t)c.state_iters; out[2] = (int64_t)c.lp_iters; out[3] = e->rounds;
     out[4] = e->launches; out[5] = (int64_t)c.jac_iters; out[6] = e->bytes_h2d; out[7] = e->bytes_d2h;
-    out[8] = (int64_t)c.fpi_iters; out[9] = 0;
+    out[8] = (int64_t)c.fpi_iters; out[9] = e->graph_rounds;
   }
   return DGX_OK;
 }

@@ -471,7 +471,8 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 __device__ __forceinline__ double ldp(const double* p, int64_t ld, int c, int64_t e) { return p[c * ld + e]; }
 
 // Per-point constitutive response (restore, cut-back driver, FPI, P) of one tile of
-// BS points plus the partial sums of P (per 64 points) for P_av.  One thread per point.
+// BS points plus the partial sums of P (per 32 points, one warp) for P_av.  One thread
+// per point.
 template <int BS>
 __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState& ps, const double* __restrict__ Fin,
                                           int64_t ldF, double dt, double* __restrict__ Ppart, int* __restrict__ ill,
@@ -547,22 +548,14 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
 #pragma unroll
     for (int k = 0; k < 9; ++k) P[k] = 0.0;
   }
-  // deterministic reduction of P per group of 64 cells (fixed tree, independent of BS)
-  __shared__ double red[9][BS];
+  // deterministic reduction of P per group of 32 cells: one warp, fixed tree
+  // (v_i += v_{i+s}, s = 16 .. 1), independent of BS
 #pragma unroll
-  for (int k = 0; k < 9; ++k) red[k][threadIdx.x] = P[k];
-  __syncthreads();
-  for (int s = 32; s > 0; s >>= 1) {
-    if ((threadIdx.x & 63) < s)
+  for (int k = 0; k < 9; ++k) {
+    double v = P[k];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
-    __syncthreads();
-  }
-  if ((threadIdx.x & 63) == 0) {
-    const int64_t g = (tile * BS + threadIdx.x) >> 6;
-    if (g * 64 < ps.n)
-#pragma unroll
-      for (int k = 0; k < 9; ++k) Ppart[g * 9 + k] = red[k][threadIdx.x];
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+    if ((threadIdx.x & 31) == 0 && e < ps.n) Ppart[(e >> 5) * 9 + k] = v;
   }
   if (cnt) {
     // per-warp aggregation of the work counters
@@ -624,7 +617,7 @@ __global__ void k_pav_finish_batch(const ConsItem* __restrict__ items, double* _
   const ConsItem& it = items[blockIdx.x];
   int c = threadIdx.x >> 5;
   if (c >= 9) return;
-  const int nblocks = (int)((it.ps.n + 63) / 64);
+  const int nblocks = (int)((it.ps.n + 31) / 32);
   const double* base = it.Ppart + c;
   double s = 0.0;
   for (int b = threadIdx.x & 31; b < nblocks; b += 32) s += base[(long)b * 9];
@@ -875,11 +868,13 @@ __global__ void k_pav_finish(const double* __restrict__ part, int nblocks, doubl
 
 // ------------------------------------------------------------------ host launchers
 namespace dgx {
-// block size of the constitutive launch (64, 128 or 256 threads); P_av partials are
-// per 64 cells whatever the block size: ceil(n / 64) x 9 doubles
+// block size of the constitutive launch (32, 64, 128 or 256 threads); P_av partials are
+// per 32 cells whatever the block size: ceil(n / 32) x 9 doubles
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
                          double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block) {
-  if (block == 64) {
+  if (block == 32) {
+    k_constitutive<32><<<(int)((ps.n + 31) / 32), 32, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+  } else if (block == 64) {
     k_constitutive<64><<<(int)((ps.n + 63) / 64), 64, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
   } else if (block == 256) {
     k_constitutive<256><<<(int)((ps.n + 255) / 256), 256, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
@@ -894,6 +889,7 @@ void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int n
     case 0: k_constitutive_batch<64, 1><<<grid, 64, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
     case 2: k_constitutive_batch<256, 1><<<grid, 256, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
     case 3: k_constitutive_batch<128, 3><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
+    case 4: k_constitutive_batch<32, 1><<<grid, 32, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
     default: k_constitutive_batch<128, 1><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
   }
 }
@@ -905,6 +901,7 @@ int constitutive_batch_resident(int variant) {
     case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<64, 1>, 64, 0); break;
     case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<256, 1>, 256, 0); break;
     case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128, 3>, 128, 0); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<32, 1>, 32, 0); break;
     default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128, 1>, 128, 0); break;
   }
   return std::max(1, nb) * std::max(1, sms);

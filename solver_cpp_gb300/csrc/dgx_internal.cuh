@@ -95,7 +95,7 @@ struct ConsItem {
   int64_t ldF;
   double dt;
   double wgt;                // 1 / N
-  double* Ppart;             // ceil(n / 64) x 9 partial sums of P
+  double* Ppart;             // ceil(n / 32) x 9 partial sums of P
   int* ill;                  // terminally-ill flag of this RVE
   long long tile0;           // first tile of this item in the launch
 };
@@ -103,10 +103,12 @@ struct ConsItem {
 // constitutive.cu launchers
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
                          double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block);
-// launch variants of the batched constitutive kernel: points per block, and the blocks
-// per SM its register allocation targets (more blocks: fewer registers, more spills)
-constexpr int CONS_VARIANTS = 4;
-__host__ __device__ constexpr int cons_variant_bs(int v) { return v == 0 ? 64 : (v == 2 ? 256 : 128); }
+// launch variants of the batched constitutive kernel: points per block (64, 128, 256,
+// 128, 32), and the blocks per SM its register allocation targets (more blocks: fewer
+// registers, more spills).  32 points per block spreads a small RVE over the most SMs
+// (one warp each), which matters because one SM's FP64 unit is the scarce resource.
+constexpr int CONS_VARIANTS = 5;
+__host__ __device__ constexpr int cons_variant_bs(int v) { return v == 0 ? 64 : v == 2 ? 256 : v == 4 ? 32 : 128; }
 __host__ __device__ constexpr int cons_variant_minb(int v) { return v == 3 ? 3 : 1; }
 void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
                                unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int variant, int grid);

@@ -130,7 +130,8 @@ void launch_combine(double* XA, const double* XM, const VecList& Xd, int l, doub
 dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons_block, Executor** out);
 void executor_destroy(Executor* e);
 // adds the executor's timers (ms, launches per timer), launches and copied bytes
-void executor_stats(const Executor* e, double ms[3], int64_t n[3], int64_t* launches, int64_t* h2d_b, int64_t* d2h_b);
+void executor_stats(const Executor* e, double ms[3], int64_t n[3], int64_t* launches, int64_t* h2d_b, int64_t* d2h_b,
+                    int64_t* graph_rounds);
 // a solve (mode 0), one increment (mode 1: steps = that step, n_or_index = its index)
 // or a load case (mode 2: n_or_index = number of steps) of one RVE, as a batch of one
 // result / restart output of a load case (increment 0 at the start, then every

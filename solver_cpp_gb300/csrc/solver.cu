@@ -624,11 +624,11 @@ static dgx_status allocate_buffers(dgx_rve* r, const int32_t cells[3], const dgx
     AL(&sp, (fp32 ? 1 : 2) * 9 * r->sl.g.Nh);
     r->spec = sp;
   }
-  r->nb_cons = (int)((N + 63) / 64);            // P_av partials: one per 64 cells
+  r->nb_cons = (int)((N + 31) / 32);            // P_av partials: one per 32 cells
   {
     const char* env = std::getenv("DGX_CONS_BLOCK");
     int b = env ? std::atoi(env) : 128;
-    r->cons_block = (b == 64 || b == 256) ? b : 128;
+    r->cons_block = (b == 32 || b == 64 || b == 256) ? b : 128;
     r->cons_block_forced = env != nullptr;
   }
   r->nb_tan = (int)((N + 63) / 64);
@@ -1029,7 +1029,7 @@ extern "C" dgx_status dgx_timers(const dgx_rve* r, double ms[3], int64_t launche
   if (!r || !ms) return DGX_ERR_ARG;
   int64_t n[3] = {0, 0, 0}, l = 0, hb = 0, db = 0;
   for (int i = 0; i < 3; ++i) { ms[i] = r->t_ms[i]; n[i] = r->t_n[i]; }
-  if (r->ex) executor_stats(r->ex, ms, n, &l, &hb, &db);
+  if (r->ex) executor_stats(r->ex, ms, n, &l, &hb, &db, nullptr);
   if (launches) for (int i = 0; i < 3; ++i) launches[i] = n[i];
   return DGX_OK;
 }
@@ -1039,11 +1039,11 @@ extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[10]) {
   ConsCounters c{};
   CK(cudaMemcpy(&c, r->d_cnt, sizeof(c), cudaMemcpyDeviceToHost));
   double ms[3] = {0, 0, 0};
-  int64_t n[3] = {0, 0, 0}, l = 0, hb = 0, db = 0;
-  if (r->ex) executor_stats(r->ex, ms, n, &l, &hb, &db);
+  int64_t n[3] = {0, 0, 0}, l = 0, hb = 0, db = 0, gr = 0;
+  if (r->ex) executor_stats(r->ex, ms, n, &l, &hb, &db, &gr);
   out[0] = r->n_eval; out[1] = (int64_t)c.state_iters; out[2] = (int64_t)c.lp_iters; out[3] = r->n_tangent;
   out[4] = r->n_launch + l; out[5] = (int64_t)c.jac_iters; out[6] = r->bytes_h2d + hb; out[7] = r->bytes_d2h + db;
-  out[8] = (int64_t)c.fpi_iters; out[9] = 0;
+  out[8] = (int64_t)c.fpi_iters; out[9] = gr;
   return DGX_OK;
 }
 

@@ -112,7 +112,7 @@ def test_autotuned_tiles_and_blocks_do_not_change_results(gpu, monkeypatch):
     slot = batch.add(tuned, steps2)
     batch.run()
     t = batch.tuning()
-    assert t["tuned_grids"] >= 1 and not t["tuning_block"] and t["cons_block"] in (64, 128, 256)
+    assert t["tuned_grids"] >= 1 and not t["tuning_block"] and t["cons_block"] in (32, 64, 128, 256)
     _same(batch.records(slot), ref)
     batch.close()
 
@@ -131,3 +131,34 @@ def test_round_point_budget_keeps_results(gpu):
     for slot, ref in zip(slots, solo):
         _same(batch.records(slot), ref)
     batch.close()
+
+
+def test_graph_replay_is_bitwise_identical(gpu, monkeypatch):
+    """Rounds whose launch parameters repeat are replayed as captured CUDA graphs; the
+    records equal those of a batch that launches every round directly (DGX_GRAPHS=0)."""
+    monkeypatch.setenv("DGX_GRAPHS", "0")
+    direct = gpu.Batch(4)
+    m0 = [_make(gpu, c, N=4) for c in CASES[:3]]
+    s0 = [direct.add(r, s) for r, s in m0]
+    direct.run()
+    assert direct.stats()["graph_rounds"] == 0
+    monkeypatch.delenv("DGX_GRAPHS")
+    graphed = gpu.Batch(4)
+    m1 = [_make(gpu, c, N=4) for c in CASES[:3]]
+    s1 = [graphed.add(r, s) for r, s in m1]
+    graphed.run()
+    st = graphed.stats()
+    assert st["graph_rounds"] > st["rounds"] // 4
+    for a, b, (ra, _), (rb, _) in zip(s0, s1, m0, m1):
+        _same(direct.records(a), graphed.records(b))
+        direct.remove(a); graphed.remove(b)
+        assert np.array_equal(ra.get("P"), rb.get("P"))
+    direct.close()
+    graphed.close()
+
+
+def test_single_rve_uses_graphs(gpu):
+    """A single-RVE load case is a batch of one: its repeated rounds replay graphs too."""
+    rve, steps = _make(gpu, CASES[0], N=3)
+    rve.loop_over_loadcase(steps)
+    assert rve.counters()["graph_rounds"] > 0
