@@ -302,6 +302,12 @@ dgx_status dgx_server_set_round_points(dgx_server* server, int64_t points);
  * denominator of the constitutive kernel's roofline.  No reference counterpart. */
 dgx_status dgx_measure_fp64_peak(double* tflops, double* ms);
 
+/* The constitutive kernel's own device math on n host values (validation against the
+ * CUDA library functions; no reference counterpart): fn 0 the Newton-Raphson
+ * reciprocal 1/x, fn 1 x^(9/4) (slip-resistance saturation, a = 2.25), fn 2 x^19
+ * (the power law's x^(n-1), n = 20). */
+dgx_status dgx_device_math(int32_t fn, int64_t n, const double* x, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,7 @@
 // which are algebraically identical to the reference's contractions.
 #include <algorithm>
 
+#include "../../include/dgx.h"
 #include "dgx_internal.cuh"
 
 namespace dgx {
@@ -44,18 +45,40 @@ __device__ __forceinline__ void mmt(const double* __restrict__ A, const double* 
     for (int i = 0; i < 3; ++i)
       C[i + 3 * j] = A[i] * B[j] + A[i + 3] * B[j + 3] + A[i + 6] * B[j + 6];
 }
+// Magnitude order of doubles through their bit patterns: for non-NaN x, y,
+// |x| <= |y|  <=>  absbits(x) <= absbits(y).  Integer compares keep the tests off the
+// FP64 pipe (the scarce unit on this part).
+__device__ __forceinline__ long long absbits(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
+__device__ __forceinline__ bool nan_bits(double x) { return absbits(x) > 0x7ff0000000000000LL; }
+constexpr long long TINY_BITS = 0x0010000000000000LL;    // 2.2250738585072014e-307 (smallest normal)
+
+// 1 / x by Newton-Raphson (r <- r + r (1 - x r), quadratic convergence) from the
+// hardware reciprocal estimate rcp.approx.ftz.f64 (about 20 correct bits): two steps
+// reach full double precision (within one ulp of the rounded quotient; tested against
+// 1.0 / x).  Zero, subnormal, huge, infinite and NaN arguments take 1.0 / x.
+__device__ __forceinline__ double rcp(double x) {
+  const unsigned ex = (unsigned)(__double_as_longlong(x) >> 52) & 0x7ffu;
+  if (ex - 24u > 2000u) return 1.0 / x;
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
 __device__ __forceinline__ bool inv33(const double* __restrict__ A, double* __restrict__ I, double* det = nullptr) {
   double c0 = A[4] * A[8] - A[7] * A[5];
   double c1 = -A[1] * A[8] + A[7] * A[2];
   double c2 = A[1] * A[5] - A[4] * A[2];
   double D = A[0] * c0 + A[3] * c1 + A[6] * c2;
   if (det) *det = D;
-  if (fabs(D) <= 2.2250738585072014e-307) {
+  if (absbits(D) <= TINY_BITS) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) I[k] = 0.0;
     return false;
   }
-  double r = 1.0 / D;
+  double r = rcp(D);
   I[0] = c0 * r; I[1] = c1 * r; I[2] = c2 * r;
   I[3] = (-A[3] * A[8] + A[6] * A[5]) * r;
   I[4] = (A[0] * A[8] - A[6] * A[2]) * r;
@@ -137,32 +160,48 @@ __device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, d
 }
 
 // resolved shear, slip rates and |d gdot / d tau| on the 12 systems (Mp = S).
-// Division free: with r = |tau|/xi, gdot = gdot0 r^n and |dgdot/dtau| = n gdot0 r^(n-1) / xi.
-__device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, const double* rxi,
+// tau = S : P_a = pval t with t the signed sum of S's components of the system's sign
+// pattern (compile time; S symmetric).  Division free: with prxi = pval / xi and
+// r = |tau| / xi = |t| prxi, gdot = gdot0 r^n sign(tau) and
+// |dgdot/dtau| = n gdot0 r^(n-1) / xi = (n gdot0 / pval) prxi r^(n-1).
+// Accumulators start at -0.0 (the additive identity) so the first term is free.
+__device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, const double* prxi,
                                          double* gdot, double* dg) {
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
-    double tau = mp.Psym[a][0] * S[0] + mp.Psym[a][1] * S[4] + mp.Psym[a][2] * S[8]
-               + mp.Psym[a][3] * S[5] + mp.Psym[a][4] * S[2] + mp.Psym[a][5] * S[1];
-    double r = fabs(tau) * rxi[a];
-    double p = pow_nm1(r, mp);               // r^(n-1)
-    double g = mp.gdot0 * (r * p);
-    gdot[a] = tau > 0.0 ? g : -g;
-    if (dg) dg[a] = (g > 2.2250738585072014e-307) ? mp.ngdot0 * (rxi[a] * p) : 0.0;
+    double t = -0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (fcc_s(a, k, k) > 0) t += S[4 * k];
+      else if (fcc_s(a, k, k) < 0) t -= S[4 * k];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {             // pairs (1,2), (0,2), (0,1)
+      const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
+      const int sg = fcc_s(a, r, q) + fcc_s(a, q, r);
+      if (sg == 1) t += S[r + 3 * q];
+      else if (sg == -1) t -= S[r + 3 * q];
+      else if (sg == 2) t = fma(2.0, S[r + 3 * q], t);
+      else if (sg == -2) t = fma(-2.0, S[r + 3 * q], t);
+    }
+    const double r = fabs(t) * prxi[a];
+    const double p = pow_nm1(r, mp);         // r^(n-1)
+    gdot[a] = copysign(mp.gdot0 * (r * p), t);
+    if (dg) dg[a] = mp.ngdot0_p * (prxi[a] * p);
   }
 }
 
 // phenopowerlaw dotState: [dot xi (12), |gdot| (12)]
 // gdot: the slip rates of S if already known (the last Lp iteration evaluated them
 // for the same S and xi), else null
-__device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, const double* rxi,
+__device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, const double* prxi,
                                           double* dot, const double* gdot = nullptr) {
   double g[NSLIP];
   if (gdot) {
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) g[a] = gdot[a];
   } else {
-    kinetics(mp, S, rxi, g, nullptr);
+    kinetics(mp, S, prxi, g, nullptr);
   }
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) g[a] = fabs(g[a]);
@@ -186,16 +225,16 @@ __device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
   double rp[N];                                  // reciprocal pivots: one division per pivot
   for (int k = 0; k < N; ++k) {
     int p = k;
-    double mx = fabs(M[N * k + k]);
+    long long mx = absbits(M[N * k + k]);
     for (int i = k + 1; i < N; ++i) {
-      double v = fabs(M[N * i + k]);
+      const long long v = absbits(M[N * i + k]);
       if (v > mx) { mx = v; p = i; }
     }
     piv[k] = p;
-    if (M[N * p + k] == 0.0) return false;
+    if (mx == 0) return false;
     if (p != k)
       for (int j = 0; j < N; ++j) { double t = M[N * k + j]; M[N * k + j] = M[N * p + j]; M[N * p + j] = t; }
-    double r = 1.0 / M[N * k + k];
+    double r = rcp(M[N * k + k]);
     rp[k] = r;
     for (int i = k + 1; i < N; ++i) {
       double l = M[N * i + k] * r;
@@ -219,16 +258,16 @@ __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) 
   double rp[9];
   for (int k = 0; k < 9; ++k) {
     int p = k;
-    double mx = fabs(M[9 * k + k]);
+    long long mx = absbits(M[9 * k + k]);
     for (int i = k + 1; i < 9; ++i) {
-      double v = fabs(M[9 * i + k]);
+      const long long v = absbits(M[9 * i + k]);
       if (v > mx) { mx = v; p = i; }
     }
     piv[k] = p;
-    if (M[9 * p + k] == 0.0) return false;
+    if (mx == 0) return false;
     if (p != k)
       for (int j = 0; j < 9; ++j) { double t = M[9 * k + j]; M[9 * k + j] = M[9 * p + j]; M[9 * p + j] = t; }
-    double r = 1.0 / M[9 * k + k];
+    double r = rcp(M[9 * k + k]);
     rp[k] = r;
     for (int i = k + 1; i < 9; ++i) {
       double l = M[9 * i + k] * r;
@@ -250,14 +289,15 @@ __device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) 
 }
 
 // integrateStress with Fi = I for fixed F and Fp0 (A = F Fp0^-1) and slip resistances
-// xi (rxi = 1 / xi): the Lp Newton iteration.  Returns true if broken.  On success
+// xi (prxi = pval / xi): the Lp Newton iteration.  Returns true if broken.  On success
 // writes S, Lp and the slip rates of S; Fp, Fe and P follow from stress_outputs().
-__device__ bool integrate_stress(const MatParams& mp, const double* A, double dt, const double* rxi, double* Lp,
+__device__ bool integrate_stress(const MatParams& mp, const double* A, double dt, const double* prxi, double* Lp,
                                  double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters) {
   double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
-  double res_old_n = 0.0, step = 1.0;
+  long long res_old_n = 0;
+  double step = 1.0;
   int jaco = 0;
   for (int it = 1;; ++it) {
     if (it > mp.N_iter_Lp_max) return true;
@@ -267,14 +307,14 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     mm(A, B, Fe_);
     hooke_S(mp, Fe_, S);
     double gdot[NSLIP], dg[NSLIP];
-    kinetics(mp, S, rxi, gdot, dg);
+    kinetics(mp, S, prxi, gdot, dg);
     // Lp = sum_a gdot_a P_a with the cF sparsity folded at compile time
     double Lpc[9];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
       for (int l = 0; l < 3; ++l) {
-        double s = 0.0;
+        double s = -0.0;
 #pragma unroll
         for (int a = 0; a < NSLIP; ++a) {
           if (fcc_s(a, k, l) > 0) s += gdot[a];
@@ -285,21 +325,24 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     double res[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) res[k] = Lpg[k] - Lpc[k];
-    // convergence tests on squared norms (no square roots)
+    // convergence tests on squared norms (no square roots); the norms are non-negative
+    // and, past the NaN test, not NaN, so they compare exactly as integers
     double nLg2 = 0.0, nLc2 = 0.0, nr2 = 0.0;
 #pragma unroll
     for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nLc2 = fma(Lpc[k], Lpc[k], nLc2); nr2 = fma(res[k], res[k], nr2); }
-    double atol2 = fmax(mp.eps_rel_Lp2 * fmax(nLg2, nLc2), mp.eps_abs_Lp2);
-    if (isnan(nr2)) return true;
-    if (nr2 < atol2) {
+    if (nan_bits(nr2)) return true;
+    const long long nr2b = absbits(nr2);
+    const long long atol2 = max(absbits(mp.eps_rel_Lp2 * __longlong_as_double(max(absbits(nLg2), absbits(nLc2)))),
+                                absbits(mp.eps_abs_Lp2));
+    if (nr2b < atol2) {
 #pragma unroll
       for (int a = 0; a < NSLIP; ++a) gdot_out[a] = gdot[a];   // slip rates of the final S
 #pragma unroll
       for (int k = 0; k < 9; ++k) Lp[k] = Lpg[k];
       return false;
     }
-    if (it == 1 || nr2 < res_old_n) {
-      res_old_n = nr2;
+    if (it == 1 || nr2b < res_old_n) {
+      res_old_n = nr2b;
 #pragma unroll
       for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
       step = 1.0;
@@ -330,7 +373,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
 #pragma unroll
       for (int kl = 0; kl < 8; ++kl) {
         const int k = kl / 3, l = kl % 3;
-        double Td[3] = {0.0, 0.0, 0.0}, To[3] = {0.0, 0.0, 0.0};   // T(r, r); T of the pairs (1,2), (0,2), (0,1)
+        double Td[3] = {-0.0, -0.0, -0.0}, To[3] = {-0.0, -0.0, -0.0};   // T(r, r); T of the pairs (1,2), (0,2), (0,1)
 #pragma unroll
         for (int a = 0; a < NSLIP; ++a) {
           if (fcc_s(a, k, l) == 0) continue;
@@ -411,7 +454,7 @@ __device__ __forceinline__ double damper(const double* o0, const double* o1, con
     double a = o0[i] - o1[i], b = o1[i] - o2[i];
     d12 = fma(a, b, d12); d22 = fma(b, b, d22); d01 = fma(o0[i], o1[i], d01);
   }
-  if (fmin(d01, d12) < 0.0 && d22 > 0.0) return 0.75 + 0.25 * tanh(2.0 + 4.0 * d12 / d22);
+  if (fmin(d01, d12) < 0.0 && d22 > 0.0) return 0.75 + 0.25 * tanh(2.0 + 4.0 * d12 * rcp(d22));
   return 1.0;
 }
 
@@ -422,17 +465,19 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
                                 double dt, double* state, double* Lp, double* S, double* P, double* Fp,
                                 double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
                                 unsigned* fpi_iters) {
-  double dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP], rxi[NSLIP], gdot[NSLIP];
+  double dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP], prxi[NSLIP], gdot[NSLIP];
   (*st_iters)++;
   double invFp0[9], A[9];
   if (!inv33(Fp0, invFp0)) return true;
   mm(F, invFp0, A);
 #pragma unroll
-  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / state[a];
-  dot_state(mp, S, state, rxi, dot);
+  for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
+  dot_state(mp, S, state, prxi, dot);
+  {
+    bool nan = false;
 #pragma unroll
-  for (int i = 0; i < 2 * NSLIP; ++i) {
-    if (isnan(dot[i])) return true;
+    for (int i = 0; i < 2 * NSLIP; ++i) nan |= nan_bits(dot[i]);
+    if (nan) return true;
   }
 #pragma unroll
   for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(dot[i], dt, state0[i]);
@@ -441,14 +486,14 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) { last2[i] = it > 1 ? last1[i] : 0.0; last1[i] = dot[i]; }
 #pragma unroll
-    for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / state[a];
+    for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
     (*fpi_iters)++;
-    broken = integrate_stress(mp, A, dt, rxi, Lp, S, gdot, lp_iters, jac_iters);
+    broken = integrate_stress(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters);
     if (broken) break;
-    dot_state(mp, S, state, rxi, dot, gdot);
+    dot_state(mp, S, state, prxi, dot, gdot);
     bool nan = false;
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) nan |= isnan(dot[i]);
+    for (int i = 0; i < 2 * NSLIP; ++i) nan |= nan_bits(dot[i]);
     if (nan) break;
     double z = damper(dot, last1, last2);
     bool conv = true;
@@ -457,8 +502,10 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
       double d = dot[i] * z + last1[i] * (1.0 - z);
       double r = state[i] - state0[i] - d * dt;
       state[i] = state[i] - r;
-      double atol = i < NSLIP ? mp.atol_xi : mp.atol_gamma;
-      conv &= fabs(r) <= fmax(atol, mp.eps_rel_state * fabs(state[i]));
+      // |r| <= max(atol, eps |state|), compared exactly as integers (r and state are
+      // not NaN here: a NaN dot state ended the iteration above)
+      const long long atol = absbits(i < NSLIP ? mp.atol_xi : mp.atol_gamma);
+      conv &= absbits(r) <= max(atol, absbits(mp.eps_rel_state * state[i]));
       dot[i] = d;
     }
     if (conv) { broken = false; break; }
@@ -631,10 +678,10 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
   double invFp[9], invFp0[9];
   inv33(Fp, invFp);
   inv33(Fp0, invFp0);
-  double rxi[NSLIP], gdot[NSLIP], d[NSLIP];
+  double prxi[NSLIP], gdot[NSLIP], d[NSLIP];
 #pragma unroll
-  for (int a = 0; a < NSLIP; ++a) rxi[a] = 1.0 / xi[a];
-  kinetics(mp, S, rxi, gdot, d);
+  for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(xi[a]);
+  kinetics(mp, S, prxi, gdot, d);
   double t2[9], Y[9];
   mm(F, invFp0, t2);
   mtm(Fe, t2, Y);                          // Fe^T (F Fp0^-1)
@@ -744,11 +791,8 @@ __global__ void __launch_bounds__(64)
 k_tangent(MatParams mp, PointState ps, double dt, double* __restrict__ dPdF_out, int64_t ld_out,
           TangentPartial* __restrict__ part) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  __shared__ double s_sum[81];
   __shared__ double s_nmax[64], s_nmin[64];
   __shared__ long long s_imax[64], s_imin[64];
-  if (threadIdx.x < 81) s_sum[threadIdx.x] = 0.0;
-  if (threadIdx.x + 64 < 81) s_sum[threadIdx.x + 64] = 0.0;
   double dPdF[81];
   double nrm = 0.0;
   bool valid = e < ps.n;
@@ -921,4 +965,31 @@ void launch_tangent_finish(const TangentPartial* part, int nblocks, double wgt, 
                            cudaStream_t st) {
   k_tangent_finish<<<82, 32, 0, st>>>(part, nblocks, wgt, Cvol, Cmm);
 }
+
+// device math helpers of the constitutive kernel on n values (validation entry point)
+__global__ void k_device_math(int fn, int64_t n, const double* __restrict__ x, double* __restrict__ out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  MatParams mp{};
+  mp.n = 20.0; mp.n_int = 20; mp.a = 2.25; mp.a_quarters = 9;
+  const double v = x[i];
+  out[i] = fn == 0 ? rcp(v) : fn == 1 ? pow_a(v, mp) : pow_nm1(v, mp);
+}
 }  // namespace dgx
+
+extern "C" dgx_status dgx_device_math(int32_t fn, int64_t n, const double* x, double* out) {
+  if (fn < 0 || fn > 2 || n < 0 || (n > 0 && (!x || !out))) return DGX_ERR_ARG;
+  if (n == 0) return DGX_OK;
+  double* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(double) * (size_t)n) != cudaSuccess) return DGX_ERR_NOMEM;
+  dgx_status s = DGX_OK;
+  if (cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess) s = DGX_ERR_CUDA;
+  if (s == DGX_OK) {
+    dgx::k_device_math<<<(unsigned)((n + 255) / 256), 256>>>(fn, n, d, d + n);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpy(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess) s = DGX_ERR_CUDA;
+  }
+  cudaFree(d);
+  return s;
+}
+

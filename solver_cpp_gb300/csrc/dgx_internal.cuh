@@ -26,6 +26,7 @@ struct MatParams {
   double C11mC12, C12, C44x2;  // cubic stiffness: C11 - C12, C12, 2 C44
   double C44;
   double ngdot0, rxi_inf;      // n * gdot0, 1 / xi_inf
+  double ngdot0_p;             // n * gdot0 / pval
   double pval;                 // magnitude of the non-zero Schmid entries (1/sqrt2 * 1/sqrt3)
   double atol_xi, atol_gamma;
   double r_cutback_min, r_cutback, r_increase, eps_rel_state;

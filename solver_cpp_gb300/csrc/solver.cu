@@ -377,6 +377,7 @@ MatParams make_params(const dgx_material& m) {
   p.C11mC12 = m.C11 - m.C12; p.C12 = m.C12; p.C44x2 = 2.0 * m.C44; p.C44 = m.C44;
   p.ngdot0 = m.n * m.dot_gamma_0; p.rxi_inf = 1.0 / m.xi_inf;
   p.pval = std::fabs(p.P[0][1]);                       // (1/sqrt2)(1/sqrt3), as the host computed P
+  p.ngdot0_p = p.ngdot0 / p.pval;
   p.eps_rel_Lp2 = m.eps_rel_Lp * m.eps_rel_Lp; p.eps_abs_Lp2 = m.eps_abs_Lp * m.eps_abs_Lp;
   double aq = 4.0 * m.a;
   p.a_quarters = (aq == std::floor(aq) && aq >= 1 && aq <= 256) ? (int)aq : -1;

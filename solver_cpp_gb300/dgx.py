@@ -76,7 +76,7 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_server_submit", "dgx_server_poll", "dgx_server_release", "dgx_server_stats",
            "dgx_update_coords", "dgx_result_open", "dgx_result_add_setup", "dgx_result_write_increment",
            "dgx_result_close", "dgx_restart_write", "dgx_restart_read", "dgx_run_loadcase_output", "dgx_batch_tuning", "dgx_flop_model", "dgx_batch_set_round_points",
-           "dgx_server_set_round_points"]
+           "dgx_server_set_round_points", "dgx_device_math"]
 
 
 class DgxError(RuntimeError):
@@ -123,6 +123,7 @@ def lib():
     L.dgx_rve_stream.argtypes = [vp]
     L.dgx_rve_stream.restype = vp
     L.dgx_measure_fp64_peak.argtypes = [dp, dp]
+    L.dgx_device_math.argtypes = [C.c_int32, C.c_int64, dp, dp]
     L.dgx_batch_create.argtypes = [C.c_int32, C.c_int32, C.POINTER(vp)]
     L.dgx_batch_destroy.argtypes = [vp]
     L.dgx_batch_destroy.restype = None

@@ -1,0 +1,55 @@
+"""The constitutive kernel's own device math (dgx_device_math) against IEEE results:
+the Newton-Raphson reciprocal within one ulp of the correctly rounded 1/x (exact where
+it falls back to the division), x^(9/4) and x^19 within a few ulps of numpy's power."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dm():
+    from solver_cpp_gb300 import build, dgx
+    build.build()
+    L = dgx.lib()
+
+    def run(fn, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.empty_like(x)
+        dp = C.POINTER(C.c_double)
+        dgx.check(L.dgx_device_math(fn, x.size, x.ctypes.data_as(dp), out.ctypes.data_as(dp)), "dgx_device_math")
+        return out
+    return run
+
+
+def ulps(a, b):
+    ia = a.view(np.int64).astype(object)
+    ib = b.view(np.int64).astype(object)
+    return np.array([abs(p - q) for p, q in zip(ia, ib)])
+
+
+def test_reciprocal(dm):
+    rng = np.random.default_rng(5)
+    x = np.concatenate([rng.uniform(0.5, 2.0, 20000), 10.0 ** rng.uniform(-290, 290, 20000),
+                        -(10.0 ** rng.uniform(-30, 30, 5000)), 2.0 ** np.arange(-990, 990, 7.0),
+                        np.nextafter(2.0 ** np.arange(-60, 60.0), 0.0), [1.0, -1.0, 3.0, 7.0, 1e8, 2.5e7]])
+    r = dm(0, x)
+    assert ulps(r, 1.0 / x).max() <= 1
+    edge = np.array([0.0, -0.0, 1e-310, -5e-320, 1e305, -1e308, np.inf, -np.inf, np.nan])
+    re = dm(0, edge)
+    with np.errstate(divide="ignore", over="ignore"):
+        ref = 1.0 / edge
+    assert np.array_equal(re[:-1], ref[:-1]) and np.isnan(re[-1])
+    assert np.signbit(re[1]) and not np.signbit(re[0])
+
+
+def test_powers(dm):
+    rng = np.random.default_rng(6)
+    y = np.concatenate([rng.uniform(1e-6, 1.0, 20000), 10.0 ** rng.uniform(-25, 0, 5000)])
+    assert np.max(np.abs(dm(1, y) / y ** 2.25 - 1.0)) < 1e-12
+    x = rng.uniform(0.0, 1.5, 20000)
+    p = dm(2, x)
+    ref = x ** 19
+    assert np.max(np.abs(p - ref) / np.maximum(ref, 1e-300)) < 1e-14
