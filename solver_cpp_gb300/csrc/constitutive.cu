@@ -355,68 +355,91 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     if (jaco % mp.f_update_jacobi_Lp == 0) {
       ++jaco;
       (*jac_iters)++;
-      // Jacobian of R(Lp) = Lp - sum_a gdot_a(tau_a(Lp)) P_a:
-      //   J(kl, pq) = delta + sum_r W(p, r) T(kl; r, q),  W = A^T Fe,
-      //   T(kl; r, q) = sum_a dt |dg_a| P_a(k, l) (C : P_a)(r, q).
+      // Jacobian of R(Lp) = Lp - sum_a gdot_a(tau_a(Lp)) P_a, rows and columns in the
+      // order kl = 3k + l:
+      //   J(kl, pq) = delta + sum_r W(p, r) T_kl(r, q),  W = A^T Fe,
+      //   T_kl(r, q) = sum_a dt |dg_a| P_a(k, l) (C : P_a)(r, q)   (symmetric in r, q).
       // With P_a = pval s_a (signs in {-1, 0, 1}, compile-time) and the cubic C : P_a
-      // (= (C11 - C12) P_a on the diagonal, C44 (P_a + P_a^T) off it, P_a traceless), T is
-      // a signed sum of c_a = dt pval^2 |dg_a| times C11 - C12 or C44.  Lp and the
-      // residual are traceless, so component (2, 2) is eliminated (x22 = -x00 - x11):
-      // 8 equations (rows kl = 3k + l < 8) in 8 unknowns.
+      // (= (C11 - C12) P_a on the diagonal, C44 (P_a + P_a^T) off it), T_kl is a signed
+      // sum of cd_a = dt pval^2 (C11 - C12) |dg_a| (diagonal) and co_a = dt pval^2 C44
+      // |dg_a| (off-diagonal entries).  In the basis of symmetric matrices
+      // (00, 11, 22, 12, 02, 01) J = I + T^ B^ with T^ (9 x 6) the components of the T_kl
+      // and B^(s, pq) the coefficient of component s in (W T)(p, q).  J has rank-6
+      // structure, so the Newton step solves (Woodbury)
+      //   x = b - T^ u,  (I6 + B^ T^) u = B^ b,
+      // a 6 x 6 system instead of the 9 x 9 one; algebraically identical.
       double W[9];
       mtm(A, Fe_, W);
-      double c[NSLIP];
-      const double cdt = dt * mp.pval * mp.pval;
+      double cd[NSLIP], co[NSLIP];
+      {
+        const double sd = dt * mp.pval * mp.pval * mp.C11mC12, so = dt * mp.pval * mp.pval * mp.C44;
 #pragma unroll
-      for (int a = 0; a < NSLIP; ++a) c[a] = cdt * dg[a];
-      double J[64];
+        for (int a = 0; a < NSLIP; ++a) { cd[a] = sd * dg[a]; co[a] = so * dg[a]; }
+      }
+      double T[9][6];
 #pragma unroll
       for (int kl = 0; kl < 8; ++kl) {
         const int k = kl / 3, l = kl % 3;
-        double Td[3] = {-0.0, -0.0, -0.0}, To[3] = {-0.0, -0.0, -0.0};   // T(r, r); T of the pairs (1,2), (0,2), (0,1)
+#pragma unroll
+        for (int sl = 0; sl < 6; ++sl) T[kl][sl] = -0.0;
 #pragma unroll
         for (int a = 0; a < NSLIP; ++a) {
           if (fcc_s(a, k, l) == 0) continue;
-          const double v = fcc_s(a, k, l) > 0 ? c[a] : -c[a];
+          const bool pos = fcc_s(a, k, l) > 0;
 #pragma unroll
           for (int r = 0; r < 3; ++r) {
-            if (fcc_s(a, r, r) > 0) Td[r] += v;
-            else if (fcc_s(a, r, r) < 0) Td[r] -= v;
+            const int sg = fcc_s(a, r, r) * (pos ? 1 : -1);
+            if (sg > 0) T[kl][r] += cd[a];
+            else if (sg < 0) T[kl][r] -= cd[a];
           }
 #pragma unroll
           for (int m = 0; m < 3; ++m) {
             const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
-            const int sg = fcc_s(a, r, q) + fcc_s(a, q, r);
-            if (sg == 1) To[m] += v;
-            else if (sg == -1) To[m] -= v;
-            else if (sg == 2) To[m] = fma(2.0, v, To[m]);
-            else if (sg == -2) To[m] = fma(-2.0, v, To[m]);
+            const int sg = (fcc_s(a, r, q) + fcc_s(a, q, r)) * (pos ? 1 : -1);
+            if (sg > 0) T[kl][3 + m] += co[a];
+            else if (sg < 0) T[kl][3 + m] -= co[a];
           }
         }
-#pragma unroll
-        for (int r = 0; r < 3; ++r) { Td[r] *= mp.C11mC12; To[r] *= mp.C44; }
-        // T as a symmetric 3x3: T(r, r) = Td[r], T(1,2) = To[0], T(0,2) = To[1], T(0,1) = To[2]
-        const double T[9] = {Td[0], To[2], To[1], To[2], Td[1], To[0], To[1], To[0], Td[2]};
-        double M[9];
-        mm(W, T, M);                               // M(p, q) = sum_r W(p, r) T(r, q)
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            const int col = 3 * p + q;
-            if (col == 8) continue;
-            double v = M[p + 3 * q];
-            if (col == 0 || col == 4) v -= M[8];   // x22 = -x00 - x11
-            J[8 * kl + col] = (col == kl ? 1.0 : 0.0) + v;
-          }
       }
-      double x[8];
 #pragma unroll
-      for (int kl = 0; kl < 8; ++kl) x[kl] = res[kl / 3 + 3 * (kl % 3)];
-      if (!lu_solve<8>(J, x)) return true;
+      for (int sl = 0; sl < 6; ++sl) T[8][sl] = -T[0][sl] - T[4][sl];   // s_a(2,2) = -s_a(0,0) - s_a(1,1)
+      // B^ v for a vector v over pq (v(p, q) = v[3p + q]): component s of sum_pq B^(s, pq) v(p, q)
+      auto bhat = [&](const double* v, double* y) {
 #pragma unroll
-      for (int kl = 0; kl < 8; ++kl) dLp[kl / 3 + 3 * (kl % 3)] = -x[kl];
-      dLp[8] = x[0] + x[4];
+        for (int r = 0; r < 3; ++r) y[r] = W[3 * r] * v[r] + W[1 + 3 * r] * v[3 + r] + W[2 + 3 * r] * v[6 + r];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
+          double t = W[3 * r] * v[q];
+          t = fma(W[1 + 3 * r], v[3 + q], t);
+          t = fma(W[2 + 3 * r], v[6 + q], t);
+          t = fma(W[3 * q], v[r], t);
+          t = fma(W[1 + 3 * q], v[3 + r], t);
+          y[3 + m] = fma(W[2 + 3 * q], v[6 + r], t);
+        }
+      };
+      double b9[9], u[6], G[36];
+#pragma unroll
+      for (int kl = 0; kl < 9; ++kl) b9[kl] = res[kl / 3 + 3 * (kl % 3)];
+      bhat(b9, u);
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        double v[9], g[6];
+#pragma unroll
+        for (int kl = 0; kl < 9; ++kl) v[kl] = T[kl][t];
+        bhat(v, g);
+#pragma unroll
+        for (int sl = 0; sl < 6; ++sl) G[6 * sl + t] = sl == t ? 1.0 + g[sl] : g[sl];
+      }
+      if (!lu_solve<6>(G, u)) return true;
+#pragma unroll
+      for (int kl = 0; kl < 8; ++kl) {
+        double x = b9[kl];
+#pragma unroll
+        for (int t = 0; t < 6; ++t) x = fma(-T[kl][t], u[t], x);
+        dLp[kl / 3 + 3 * (kl % 3)] = -x;
+      }
+      dLp[8] = -dLp[0] - dLp[4];
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg[k]);

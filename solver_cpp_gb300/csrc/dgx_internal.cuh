@@ -69,14 +69,16 @@ struct ConsCounters {
   unsigned long long state_iters, lp_iters, jac_iters, points, fpi_iters;
 };
 
-// Algorithmic FP64 flops of the constitutive kernel per counted unit (FMA = 2, division
-// and square root = 1), counted from its arithmetic: one Lp Newton iteration (B, Fe,
-// Hooke, 12-system kinetics with derivatives, Lp, residual and norms), one Jacobian
-// (W, signed-sum T, W T for 8 rows, 8x8 LU with one right-hand side), one state
-// integration call (Fp0^-1, F Fp0^-1, 1/xi, first dot state, predictor, and once the
-// iteration ends Fp^-1, P, det and Fp scaling) and one fixed-point iteration (1/xi,
-// hardening from the slip rates of the last Lp iteration, damper, state update).
-constexpr double FLOPS_LP = 537.0, FLOPS_JAC = 1184.0, FLOPS_STATE = 1028.0, FLOPS_FPI = 815.0;
+// Algorithmic FP64 flops of the constitutive kernel per counted unit (FMA = 2, division,
+// reciprocal and square root = 1), counted from its arithmetic: one Lp Newton iteration
+// (B, Fe, Hooke, 12-system kinetics with derivatives, Lp, residual and norms: 432), one
+// Jacobian step (W, the signed sums T^ scaled by the cubic moduli, B^ b and the 6 x 6
+// matrix I + B^ T^, its LU with one right-hand side, the step b - T^ u: 923), one state
+// integration call (Fp0^-1, F Fp0^-1, pval/xi, first dot state, predictor, and once
+// the iteration ends Fp^-1, P, det and Fp scaling: 944) and one fixed-point iteration
+// (pval/xi, hardening from the slip rates of the last Lp iteration, damper, state
+// update: 827).
+constexpr double FLOPS_LP = 432.0, FLOPS_JAC = 923.0, FLOPS_STATE = 944.0, FLOPS_FPI = 827.0;
 
 // Stress boundary condition of one RVE's solve, resident on the device so that the
 // BC step of a residual evaluation (form_residual) needs no host round trip.
