@@ -141,22 +141,30 @@ __device__ __forceinline__ double pow_a(double y, const MatParams& mp) {
 __host__ __device__ constexpr int fcc_d(int a, int k) { return "120012201100212021102010221122210001"[3 * a + k] - '1'; }
 __host__ __device__ constexpr int fcc_n(int a, int l) { return "222222222002002002200200200020020020"[3 * a + l] - '1'; }
 __host__ __device__ constexpr int fcc_s(int a, int k, int l) { return fcc_d(a, k) * fcc_n(a, l); }
+// sign pattern of C : s_a in the symmetric basis (00, 11, 22, 12, 02, 01): the diagonal
+// entries of s_a, and s_a(r, q) + s_a(q, r) off the diagonal (both in {-1, 0, 1} for cF)
+__host__ __device__ constexpr int fcc_q(int a, int sl) {
+  return sl < 3 ? fcc_s(a, sl, sl)
+                : fcc_s(a, sl == 3 ? 1 : 0, sl == 5 ? 1 : 2) + fcc_s(a, sl == 5 ? 1 : 2, sl == 3 ? 1 : 0);
+}
 
-// Hooke for the cubic stiffness: S = C : E(Fe), E = (Fe^T Fe - I)/2 (symmetric)
+// Hooke for the cubic stiffness: S = C : E(Fe), E = (Fe^T Fe - I)/2 (symmetric), formed
+// from 2E with the halved moduli: S_ii = (C11 - C12)/2 (2E)_ii + C12/2 tr(2E),
+// S_ij = C44 (2E)_ij
 __device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, double* S) {
-  double E00 = 0.5 * (Fe[0] * Fe[0] + Fe[1] * Fe[1] + Fe[2] * Fe[2] - 1.0);
-  double E11 = 0.5 * (Fe[3] * Fe[3] + Fe[4] * Fe[4] + Fe[5] * Fe[5] - 1.0);
-  double E22 = 0.5 * (Fe[6] * Fe[6] + Fe[7] * Fe[7] + Fe[8] * Fe[8] - 1.0);
-  double E12 = 0.5 * (Fe[3] * Fe[6] + Fe[4] * Fe[7] + Fe[5] * Fe[8]);
-  double E02 = 0.5 * (Fe[0] * Fe[6] + Fe[1] * Fe[7] + Fe[2] * Fe[8]);
-  double E01 = 0.5 * (Fe[0] * Fe[3] + Fe[1] * Fe[4] + Fe[2] * Fe[5]);
-  double tr = E00 + E11 + E22;
-  S[0] = fma(mp.C11mC12, E00, mp.C12 * tr);
-  S[4] = fma(mp.C11mC12, E11, mp.C12 * tr);
-  S[8] = fma(mp.C11mC12, E22, mp.C12 * tr);
-  S[5] = S[7] = mp.C44x2 * E12;
-  S[2] = S[6] = mp.C44x2 * E02;
-  S[1] = S[3] = mp.C44x2 * E01;
+  const double E00 = fma(Fe[0], Fe[0], fma(Fe[1], Fe[1], fma(Fe[2], Fe[2], -1.0)));
+  const double E11 = fma(Fe[3], Fe[3], fma(Fe[4], Fe[4], fma(Fe[5], Fe[5], -1.0)));
+  const double E22 = fma(Fe[6], Fe[6], fma(Fe[7], Fe[7], fma(Fe[8], Fe[8], -1.0)));
+  const double E12 = Fe[3] * Fe[6] + Fe[4] * Fe[7] + Fe[5] * Fe[8];
+  const double E02 = Fe[0] * Fe[6] + Fe[1] * Fe[7] + Fe[2] * Fe[8];
+  const double E01 = Fe[0] * Fe[3] + Fe[1] * Fe[4] + Fe[2] * Fe[5];
+  const double ct = mp.hC12 * (E00 + E11 + E22);
+  S[0] = fma(mp.hC11mC12, E00, ct);
+  S[4] = fma(mp.hC11mC12, E11, ct);
+  S[8] = fma(mp.hC11mC12, E22, ct);
+  S[5] = S[7] = mp.C44 * E12;
+  S[2] = S[6] = mp.C44 * E02;
+  S[1] = S[3] = mp.C44 * E01;
 }
 
 // resolved shear, slip rates and |d gdot / d tau| on the 12 systems (Mp = S).
@@ -209,10 +217,17 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
   for (int a = 0; a < NSLIP; ++a) {
     double x = 1.0 - xi[a] * mp.rxi_inf;
     double left = copysign(pow_a(fabs(x), mp), x);
-    double hs = 0.0;
+    // h0 sum_b h_ab |gdot_b| with h_ab one of seven values: the slip rates are summed
+    // per interaction type (compile-time grouping), then weighted by h0 h_t
+    double gt[7];
 #pragma unroll
-    for (int b = 0; b < NSLIP; ++b) hs = fma(mp.h[a][b], g[b], hs);
-    dot[a] = mp.h0 * left * hs;
+    for (int t = 0; t < 7; ++t) gt[t] = -0.0;
+#pragma unroll
+    for (int b = 0; b < NSLIP; ++b) gt[cf_interaction(a, b) - 1] += g[b];
+    double hs = mp.h0h[0] * gt[0];
+#pragma unroll
+    for (int t = 1; t < 7; ++t) hs = fma(mp.h0h[t], gt[t], hs);
+    dot[a] = left * hs;
     dot[NSLIP + a] = g[a];
   }
 }
@@ -308,7 +323,21 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     hooke_S(mp, Fe_, S);
     double gdot[NSLIP], dg[NSLIP];
     kinetics(mp, S, prxi, gdot, dg);
-    // Lp = sum_a gdot_a P_a with the cF sparsity folded at compile time
+    // Lp = pval sum_a gdot_a d_a (x) n_a with the cF signs folded at compile time: the
+    // three systems of a slip plane share n, so the plane sums Y_p = sum_a gdot_a d_a
+    // come first, then Lp(k, l) = pval sum_p n_p(l) Y_p(k)
+    double Y[4][3];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        Y[p][k] = -0.0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (fcc_d(3 * p + j, k) > 0) Y[p][k] += gdot[3 * p + j];
+          else if (fcc_d(3 * p + j, k) < 0) Y[p][k] -= gdot[3 * p + j];
+        }
+      }
     double Lpc[9];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -316,9 +345,9 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       for (int l = 0; l < 3; ++l) {
         double s = -0.0;
 #pragma unroll
-        for (int a = 0; a < NSLIP; ++a) {
-          if (fcc_s(a, k, l) > 0) s += gdot[a];
-          else if (fcc_s(a, k, l) < 0) s -= gdot[a];
+        for (int p = 0; p < 4; ++p) {
+          if (fcc_n(3 * p, l) > 0) s += Y[p][k];
+          else s -= Y[p][k];
         }
         Lpc[k + 3 * l] = mp.pval * s;
       }

@@ -14,17 +14,24 @@ namespace dgx {
 
 constexpr int NSLIP = 12;
 
+// cF slip-slip interaction type (1..7, the index into h_sl-sl) of reacting system r and
+// acting system b, the reference's interaction table (crystal.f90, FCC_INTERACTIONSLIPSLIP)
+// as digits so that unrolled device loops fold it into constants.
+__host__ __device__ constexpr int cf_interaction(int r, int b) {
+  return "122475355467212745647535221553674764476122467355746212535647553221"
+         "764674355467122476647535212746674764221553467355476122535647746212764674553221"[12 * r + b] - '0';
+}
+
 // Constitutive parameters of one phenopowerlaw cF phase, passed by value as a
 // kernel parameter (constant bank, broadcast to all threads).
 struct MatParams {
   double C66[36];            // column-major 6x6, Voigt 11,22,33,23,13,12
   double P[NSLIP][9];        // Schmid matrices d (x) n, column-major 3x3
-  double Psym[NSLIP][6];     // P11, P22, P33, P23+P32, P13+P31, P12+P21
-  double Q[NSLIP][9];        // C : P_alpha  (column-major 3x3)
-  double h[NSLIP][NSLIP];    // slip-slip interaction, h[reacting][acting]
+  double h0h[7];             // h0 times the seven cF slip-slip interaction values (h_sl-sl)
   double xi_inf, h0, n, gdot0, a, c1, c2;
   double C11mC12, C12, C44x2;  // cubic stiffness: C11 - C12, C12, 2 C44
   double C44;
+  double hC11mC12, hC12;       // (C11 - C12) / 2, C12 / 2
   double ngdot0, rxi_inf;      // n * gdot0, 1 / xi_inf
   double ngdot0_p;             // n * gdot0 / pval
   double pval;                 // magnitude of the non-zero Schmid entries (1/sqrt2 * 1/sqrt3)
@@ -71,14 +78,14 @@ struct ConsCounters {
 
 // Algorithmic FP64 flops of the constitutive kernel per counted unit (FMA = 2, division,
 // reciprocal and square root = 1), counted from its arithmetic: one Lp Newton iteration
-// (B, Fe, Hooke, 12-system kinetics with derivatives, Lp, residual and norms: 432), one
+// (B, Fe, Hooke, 12-system kinetics with derivatives, Lp, residual and norms: 402), one
 // Jacobian step (W, the signed sums T^ scaled by the cubic moduli, B^ b and the 6 x 6
 // matrix I + B^ T^, its LU with one right-hand side, the step b - T^ u: 923), one state
 // integration call (Fp0^-1, F Fp0^-1, pval/xi, first dot state, predictor, and once
-// the iteration ends Fp^-1, P, det and Fp scaling: 944) and one fixed-point iteration
-// (pval/xi, hardening from the slip rates of the last Lp iteration, damper, state
-// update: 827).
-constexpr double FLOPS_LP = 432.0, FLOPS_JAC = 923.0, FLOPS_STATE = 944.0, FLOPS_FPI = 827.0;
+// the iteration ends Fp^-1, P, det and Fp scaling: 860) and one fixed-point iteration
+// (pval/xi, hardening from the slip rates of the last Lp iteration summed per
+// interaction type, damper, state update: 743).
+constexpr double FLOPS_LP = 402.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS_FPI = 743.0;
 
 // Stress boundary condition of one RVE's solve, resident on the device so that the
 // BC step of a residual evaluation (form_residual) needs no host round trip.

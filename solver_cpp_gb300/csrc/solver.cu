@@ -326,11 +326,6 @@ const int CF_SLIP[12][6] = {
   { 0,-1,-1, -1,-1, 1}, { 1, 0, 1, -1,-1, 1}, {-1, 1, 0, -1,-1, 1},
   { 0,-1, 1,  1,-1,-1}, {-1, 0,-1,  1,-1,-1}, { 1, 1, 0,  1,-1,-1},
   { 0, 1, 1, -1, 1,-1}, { 1, 0,-1, -1, 1,-1}, {-1,-1, 0, -1, 1,-1}};
-const int CF_INTERACT[12][12] = {
-  {1,2,2,4,7,5,3,5,5,4,6,7}, {2,1,2,7,4,5,6,4,7,5,3,5}, {2,2,1,5,5,3,6,7,4,7,6,4},
-  {4,7,6,1,2,2,4,6,7,3,5,5}, {7,4,6,2,1,2,5,3,5,6,4,7}, {5,5,3,2,2,1,7,6,4,6,7,4},
-  {3,5,5,4,6,7,1,2,2,4,7,6}, {6,4,7,5,3,5,2,1,2,7,4,6}, {6,7,4,7,6,4,2,2,1,5,5,3},
-  {4,6,7,3,5,5,4,7,6,1,2,2}, {5,3,5,6,4,7,7,4,6,2,1,2}, {7,6,4,6,7,4,5,5,3,2,2,1}};
 
 MatParams make_params(const dgx_material& m) {
   MatParams p;
@@ -341,31 +336,16 @@ MatParams make_params(const dgx_material& m) {
   C66[21] = C66[28] = C66[35] = m.C44;
   for (int i = 0; i < 6; ++i) for (int j = i + 1; j < 6; ++j) C66[j + 6 * i] = C66[i + 6 * j];
   memcpy(p.C66, C66, sizeof(C66));
-  const int VO[6][2] = {{0, 0}, {1, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}};
-  double C[81] = {0};
-  for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) {
-    int a = VO[i][0], b = VO[i][1], c = VO[j][0], d = VO[j][1];
-    double v = C66[i + 6 * j];
-    C[a + 3 * b + 9 * c + 27 * d] = C[b + 3 * a + 9 * c + 27 * d] = C[a + 3 * b + 9 * d + 27 * c] = C[b + 3 * a + 9 * d + 27 * c] = v;
-  }
   for (int s = 0; s < 12; ++s) {
     double d[3], n[3], ld = 0, ln = 0;
     for (int i = 0; i < 3; ++i) { d[i] = CF_SLIP[s][i]; n[i] = CF_SLIP[s][3 + i]; ld += d[i] * d[i]; ln += n[i] * n[i]; }
     ld = std::sqrt(ld); ln = std::sqrt(ln);
     for (int i = 0; i < 3; ++i) { d[i] /= ld; n[i] /= ln; }
     for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) p.P[s][i + 3 * j] = d[i] * n[j];
-    const double* P = p.P[s];
-    p.Psym[s][0] = P[0]; p.Psym[s][1] = P[4]; p.Psym[s][2] = P[8];
-    p.Psym[s][3] = P[7] + P[5]; p.Psym[s][4] = P[6] + P[2]; p.Psym[s][5] = P[3] + P[1];
-    for (int mm = 0; mm < 3; ++mm) for (int q = 0; q < 3; ++q) {
-      double v = 0.0;
-      for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) v += P[i + 3 * j] * C[i + 3 * j + 9 * mm + 27 * q];
-      p.Q[s][mm + 3 * q] = v;
-    }
   }
-  for (int r = 0; r < 12; ++r) for (int a = 0; a < 12; ++a) p.h[r][a] = m.h_sl_sl[CF_INTERACT[r][a] - 1];
   p.xi_inf = m.xi_inf;
   p.h0 = m.h_0 * (1.0 + m.c_1 * std::pow(0.0, m.c_2));     // no twins: sum f = 0
+  for (int t = 0; t < 7; ++t) p.h0h[t] = p.h0 * m.h_sl_sl[t];
   p.n = m.n; p.gdot0 = m.dot_gamma_0; p.a = m.a; p.c1 = m.c_1; p.c2 = m.c_2;
   p.atol_xi = m.atol_xi; p.atol_gamma = m.atol_gamma;
   p.r_cutback_min = m.r_cutback_min; p.r_cutback = m.r_cutback; p.r_increase = m.r_increase;
@@ -375,6 +355,7 @@ MatParams make_params(const dgx_material& m) {
   p.f_update_jacobi_Lp = m.f_update_jacobi_Lp < 1 ? 1 : m.f_update_jacobi_Lp;
   p.n_int = (m.n == std::floor(m.n) && m.n >= 1 && m.n <= 64) ? (int)m.n : -1;
   p.C11mC12 = m.C11 - m.C12; p.C12 = m.C12; p.C44x2 = 2.0 * m.C44; p.C44 = m.C44;
+  p.hC11mC12 = 0.5 * p.C11mC12; p.hC12 = 0.5 * m.C12;
   p.ngdot0 = m.n * m.dot_gamma_0; p.rxi_inf = 1.0 / m.xi_inf;
   p.pval = std::fabs(p.P[0][1]);                       // (1/sqrt2)(1/sqrt3), as the host computed P
   p.ngdot0_p = p.ngdot0 / p.pval;
