@@ -39,10 +39,10 @@ METRIC = "point-updates/s, mixed vs FP64 GPU at ≤1e-5 rel. P error; p50/p99 RV
 UNIT = "point-updates/s"
 SEED = 42
 
-# DRAM traffic of one constitutive launch per cell, from the ncu capture summarised in
-# profiles/constitutive_64cube.md (dram__bytes_read.sum + dram__bytes_write.sum of one
-# launch / 262,144 cells; mostly register-spill write-back)
-TRAFFIC_BYTES_PER_CELL = 6466.0
+# DRAM traffic of one constitutive launch per cell, from an ncu capture of this
+# workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch / 262,144 cells:
+# 0.372 GB read + 0.980 GB written; mostly register-spill write-back)
+TRAFFIC_BYTES_PER_CELL = 5157.0
 
 
 def args_():
