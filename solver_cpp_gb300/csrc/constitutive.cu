@@ -712,16 +712,33 @@ k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitem
 }
 
 // P_av of every item: block i, warp c sums component c (same order as k_pav_finish)
-__global__ void k_pav_finish_batch(const ConsItem* __restrict__ items, double* __restrict__ Pav) {
-  const ConsItem& it = items[blockIdx.x];
-  int c = threadIdx.x >> 5;
-  if (c >= 9) return;
-  const int nblocks = (int)((it.ps.n + 31) / 32);
-  const double* base = it.Ppart + c;
-  double s = 0.0;
-  for (int b = threadIdx.x & 31; b < nblocks; b += 32) s += base[(long)b * 9];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) Pav[9 * blockIdx.x + c] = s * it.wgt;
+// Sum of one component of the P partials (stride 9) by a block of 256 threads in a
+// fixed order: thread t takes partials t, t + 256, ... into four independent
+// accumulators (four loads in flight), then a fixed tree over the block.
+__device__ __forceinline__ double pav_block_sum(const double* __restrict__ base, int nblocks) {
+  __shared__ double red[256];
+  const int t = threadIdx.x;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int b = t;
+  for (; b + 768 < nblocks; b += 1024) {
+    s0 += base[(long)b * 9]; s1 += base[(long)(b + 256) * 9];
+    s2 += base[(long)(b + 512) * 9]; s3 += base[(long)(b + 768) * 9];
+  }
+  for (; b < nblocks; b += 256) s0 += base[(long)b * 9];
+  red[t] = (s0 + s1) + (s2 + s3);
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (t < o) red[t] += red[t + o];
+    __syncthreads();
+  }
+  return red[0];
+}
+
+// P_av of every item: block (c, item) sums component c (the same order as k_pav_finish)
+__global__ void __launch_bounds__(256) k_pav_finish_batch(const ConsItem* __restrict__ items, double* __restrict__ Pav) {
+  const ConsItem& it = items[blockIdx.y];
+  const double s = pav_block_sum(it.Ppart + blockIdx.x, (int)((it.ps.n + 31) / 32));
+  if (threadIdx.x == 0) Pav[9 * blockIdx.y + blockIdx.x] = s * it.wgt;
 }
 
 // Analytic consistent tangent (Fi = I) for one point; writes dPdF (col-major 3333).
@@ -737,25 +754,43 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
   double t2[9], Y[9];
   mm(F, invFp0, t2);
   mtm(Fe, t2, Y);                          // Fe^T (F Fp0^-1)
-  // M = I + dt sum_a d_a vec(C:U_a) vec(P_a)^T, rows (p,o) cols (p',o'), MAPPLAIN order
+  // M = I + dt sum_a d_a vec(C:U_a) vec(P_a)^T, rows (p,o) cols (q,r), MAPPLAIN order.
+  // With P_a = pval d_a (x) n_a (signs compile-time): U_a = Y P_a = pval (Y d_a) (x) n_a,
+  // C : U_a in the cubic closed form, and the outer product with P_a is a signed add.
   double M[81];
 #pragma unroll
   for (int k = 0; k < 81; ++k) M[k] = (k % 10) == 0 ? 1.0 : 0.0;
+  const double cp2 = dt * mp.pval * mp.pval;
+#pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
-    double c = dt * d[a];
-    if (c == 0.0) continue;
-    double U[9];
-    mm(Y, mp.P[a], U);
-    double e6[6] = {U[0], U[4], U[8], U[5] + U[7], U[2] + U[6], U[1] + U[3]};
+    const double c = cp2 * d[a];
+    double y[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      y[i] = -0.0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (fcc_d(a, k) > 0) y[i] += Y[i + 3 * k];
+        else if (fcc_d(a, k) < 0) y[i] -= Y[i + 3 * k];
+      }
+    }
+    // Voigt strain (engineering shear) of y (x) n_a
+    double e[6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) e[i] = fcc_n(a, i) > 0 ? y[i] : -y[i];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;       // pairs (1,2), (0,2), (0,1)
+      const double t1 = fcc_n(a, q) > 0 ? y[r] : -y[r];
+      e[3 + m] = fcc_n(a, r) > 0 ? t1 + y[q] : t1 - y[q];
+    }
+    const double ct = mp.C12 * (e[0] + e[1] + e[2]);
     double s6[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      double s = 0.0;
+    for (int i = 0; i < 3; ++i) s6[i] = c * fma(mp.C11mC12, e[i], ct);
 #pragma unroll
-      for (int j = 0; j < 6; ++j) s = fma(mp.C66[i + 6 * j], e6[j], s);
-      s6[i] = c * s;
-    }
-    double CU[9] = {s6[0], s6[5], s6[4], s6[5], s6[1], s6[3], s6[4], s6[3], s6[2]};
+    for (int m = 0; m < 3; ++m) s6[3 + m] = c * (mp.C44 * e[3 + m]);
+    const double CU[9] = {s6[0], s6[5], s6[4], s6[5], s6[1], s6[3], s6[4], s6[3], s6[2]};
 #pragma unroll
     for (int p = 0; p < 3; ++p)
 #pragma unroll
@@ -763,37 +798,34 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
 #pragma unroll
         for (int q = 0; q < 3; ++q)
 #pragma unroll
-          for (int r = 0; r < 3; ++r)
-            M[9 * (3 * p + o) + 3 * q + r] = fma(CU[p + 3 * o], mp.P[a][q + 3 * r], M[9 * (3 * p + o) + 3 * q + r]);
+          for (int r = 0; r < 3; ++r) {
+            if (fcc_s(a, q, r) > 0) M[9 * (3 * p + o) + 3 * q + r] += CU[p + 3 * o];
+            else if (fcc_s(a, q, r) < 0) M[9 * (3 * p + o) + 3 * q + r] -= CU[p + 3 * o];
+          }
   }
-  // rhs(p,o,k,l) = (Fe C_po invFp^T)(k,l); stored B[(3k+l)*9 + (3p+o)] (9 rhs columns)
+  // rhs(p,o,k,l) = (Fe C_po invFp^T)(k,l); stored B[(3k+l)*9 + (3p+o)] (9 rhs columns).
+  // Cubic C_pomn = C12 d_po d_mn + C44 (d_pm d_on + d_pn d_om) + (C11 - C12 - 2 C44) d_pomn:
+  //   p == o: C12 (Fe invFp^T)(k,l) + (C11 - C12) Fe(k,p) invFp(l,p)
+  //   p != o: C44 (Fe(k,p) invFp(l,o) + Fe(k,o) invFp(l,p))
   double Bm[81];
   {
-    double C3[81];   // full stiffness from Voigt
-    const int vi[3][3] = {{0, 5, 4}, {5, 1, 3}, {4, 3, 2}};
+    double H[9];
+    mmt(Fe, invFp, H);
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-#pragma unroll
-          for (int l = 0; l < 3; ++l) C3[i + 3 * j + 9 * k + 27 * l] = mp.C66[vi[i][j] + 6 * vi[k][l]];
     for (int p = 0; p < 3; ++p)
-      for (int o = 0; o < 3; ++o) {
-        double Cpo[9], T[9], R[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Cpo[k] = C3[p + 3 * o + 9 * k];
-        mm(Fe, Cpo, T);
-        mmt(T, invFp, R);
+      for (int o = 0; o < 3; ++o)
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
-          for (int l = 0; l < 3; ++l) Bm[(3 * k + l) * 9 + 3 * p + o] = R[k + 3 * l];
-      }
+          for (int l = 0; l < 3; ++l) {
+            double v;
+            if (p == o) v = fma(mp.C11mC12, Fe[k + 3 * p] * invFp[l + 3 * p], mp.C12 * H[k + 3 * l]);
+            else v = mp.C44 * fma(Fe[k + 3 * p], invFp[l + 3 * o], Fe[k + 3 * o] * invFp[l + 3 * p]);
+            Bm[(3 * k + l) * 9 + 3 * p + o] = v;
+          }
   }
   lu_solve9(M, Bm, 9);   // Bm <- dSdF: Bm[(3k+l)*9 + 3p+o] = dS_po/dF_kl
-  // R_a = invFp0 P_a
   double u1[9], u2[9], u3[9], w[9];
   mmt(S, invFp, u1);                      // S invFp^T
   mm(F, invFp, u2);
@@ -807,6 +839,9 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
     for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int l = 0; l < 3; ++l) dPdF[p + 3 * j + 9 * p + 27 * l] = w[l + 3 * j];
+  double mdd[NSLIP];                      // -dt pval^2 d_a
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) mdd[a] = -cp2 * d[a];
   for (int kk = 0; kk < 3; ++kk)
     for (int ll = 0; ll < 3; ++ll) {
       const double* dS = Bm + (3 * kk + ll) * 9;    // dS(p,o) at row 3p+o
@@ -815,18 +850,53 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
       for (int p = 0; p < 3; ++p)
 #pragma unroll
         for (int o = 0; o < 3; ++o) dSm[p + 3 * o] = dS[3 * p + o];
-      // D = -dt sum_a d_a (P_a : dS) invFp0 P_a
+      // G = -dt sum_a d_a (P_a : dS) P_a = pval^2 sum_a mdd_a (d_a . dS n_a) d_a (x) n_a,
+      // through the slip planes' normals: v_p = dS n_p, then per-plane sums of d_a
+      double Gs[4][3];
+#pragma unroll
+      for (int pl = 0; pl < 4; ++pl) {
+        double v[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          v[q] = -0.0;
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            if (fcc_n(3 * pl, r) > 0) v[q] += dSm[q + 3 * r];
+            else v[q] -= dSm[q + 3 * r];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) Gs[pl][k] = -0.0;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int a = 3 * pl + j;
+          double wa = -0.0;
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            if (fcc_d(a, q) > 0) wa += v[q];
+            else if (fcc_d(a, q) < 0) wa -= v[q];
+          }
+          const double ca = mdd[a] * wa;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            if (fcc_d(a, k) > 0) Gs[pl][k] += ca;
+            else if (fcc_d(a, k) < 0) Gs[pl][k] -= ca;
+          }
+        }
+      }
       double G[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) G[k] = 0.0;
-      for (int a = 0; a < NSLIP; ++a) {
-        double wa = mp.P[a][0] * dSm[0];
+      for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int k = 1; k < 9; ++k) wa = fma(mp.P[a][k], dSm[k], wa);
-        double c = -dt * d[a] * wa;
+        for (int l = 0; l < 3; ++l) {
+          double g = -0.0;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) G[k] = fma(c, mp.P[a][k], G[k]);
-      }
+          for (int pl = 0; pl < 4; ++pl) {
+            if (fcc_n(3 * pl, l) > 0) g += Gs[pl][k];
+            else g -= Gs[pl][k];
+          }
+          G[k + 3 * l] = g;
+        }
       double D[9], X[9], Xa[9], Yb[9], Yc[9], Z[9];
       mm(invFp0, G, D);
       mm(F, D, X); mm(X, u1, Xa);
@@ -950,14 +1020,10 @@ __global__ void k_tangent_finish(const TangentPartial* __restrict__ part, int nb
 }
 
 // P_av from block partials: warp c sums component c (fixed order)
-__global__ void k_pav_finish(const double* __restrict__ part, int nblocks, double wgt, double* __restrict__ Pav) {
-  int c = threadIdx.x >> 5;
-  if (c >= 9) return;
-  const double* base = part + c;
-  double s = 0.0;
-  for (int b = threadIdx.x & 31; b < nblocks; b += 32) s += base[(long)b * 9];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) Pav[c] = s * wgt;
+__global__ void __launch_bounds__(256) k_pav_finish(const double* __restrict__ part, int nblocks, double wgt,
+                                                    double* __restrict__ Pav) {
+  const double s = pav_block_sum(part + blockIdx.x, nblocks);
+  if (threadIdx.x == 0) Pav[blockIdx.x] = s * wgt;
 }
 
 }  // namespace dgx
@@ -1003,10 +1069,10 @@ int constitutive_batch_resident(int variant) {
   return std::max(1, nb) * std::max(1, sms);
 }
 void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st) {
-  k_pav_finish_batch<<<nitems, 9 * 32, 0, st>>>(items, Pav);
+  k_pav_finish_batch<<<dim3(9, nitems), 256, 0, st>>>(items, Pav);
 }
 void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st) {
-  k_pav_finish<<<1, 9 * 32, 0, st>>>(Ppart, nblocks, wgt, Pav);
+  k_pav_finish<<<9, 256, 0, st>>>(Ppart, nblocks, wgt, Pav);
 }
 void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,
                     TangentPartial* part, cudaStream_t st) {
