@@ -364,16 +364,17 @@ def spectral_roofline(cells, precision, ms, fp64_peak):
     """FFT / Gamma / div-RMS chain of one residual evaluation against both ceilings.
     bytes: read P and write R (9N FP64 each) plus the spectrum traffic between the five
     passes (x out, y in/out, z in/out, y in/out, x in: 8 x 9 Nh complex of the spectral
-    precision).  flops: 5 n log2 n per complex line FFT (forward and inverse, x lines
-    as complex), ~230 per frequency for Gamma and the divergence sum."""
+    precision).  flops: 5 n log2 n per complex line FFT (forward and inverse; along x
+    two real lines share one complex FFT), ~230 per frequency for Gamma and the
+    divergence sum, ~8 per frequency to separate and join the packed x lines."""
     import math
     N0, N1, N2 = cells
     N, N0r = N0 * N1 * N2, N0 // 2 + 1
     Nh = N0r * N1 * N2
     cs = 16 if precision == "fp64" else 8
     bytes_ = 2 * 9 * N * 8 + 8 * 9 * Nh * cs
-    fl = 2 * 5 * 9 * (N1 * N2 * N0 * math.log2(N0) + N0r * N2 * N1 * math.log2(N1) + N0r * N1 * N2 * math.log2(N2))
-    fl += 230 * Nh
+    fl = 2 * 5 * 9 * (N1 * N2 * N0 * math.log2(N0) / 2 + N0r * N2 * N1 * math.log2(N1) + N0r * N1 * N2 * math.log2(N2))
+    fl += 230 * Nh + 8 * 9 * Nh
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:

@@ -121,59 +121,88 @@ __global__ void k_xfwd(SpecGeom g, AxisPlan px, const Rin* __restrict__ field, l
   typedef typename cpx<R>::t C;
   if (items) { field = (const Rin*)items[blockIdx.y].in; spec = (C*)items[blockIdx.y].spec; }
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
-  C* b = a + (long)LX * g.N0;
   const long long nlines = 9LL * g.N1 * g.N2;
   const long long l0 = (long long)blockIdx.x * LX;
   const int nl = (int)min((long long)LX, nlines - l0);
-  for (int t = threadIdx.x; t < nl * g.N0; t += blockDim.x) {
-    int l = t / g.N0, x = t - l * g.N0;
-    long long L = l0 + l;
-    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
-    C v; v.x = (R)field[c * ld_in + yz * g.N0 + x]; v.y = 0;
+  const int np = (nl + 1) >> 1;          // complex lines: real lines 2j and 2j+1 as z = a + i b (LX even)
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + (long)np * g.N0;
+  const long long nyz = (long long)g.N1 * g.N2;
+  for (int t = threadIdx.x; t < np * g.N0; t += blockDim.x) {
+    const int j = t / g.N0, x = t - j * g.N0;
+    const long long L = l0 + 2 * j;
+    const long long c = L / nyz, yz = L - c * nyz;
+    C v;
+    v.x = (R)field[c * ld_in + yz * g.N0 + x];
+    if (2 * j + 1 < nl) {
+      const long long L1 = L + 1, c1 = L1 / nyz, yz1 = L1 - c1 * nyz;
+      v.y = (R)field[c1 * ld_in + yz1 * g.N0 + x];
+    } else {
+      v.y = 0;
+    }
     a[t] = v;
   }
   __syncthreads();
-  C* res = block_fft<R>(a, b, nl, px, -1);
+  C* res = block_fft<R>(a, b, np, px, -1);
+  // separate the two real lines' spectra: with Z = FFT(a + i b) and W_i = Z_(N0-i),
+  // A_i = (Z_i + conj W_i) / 2, B_i = (Z_i - conj W_i) / 2i
   for (int t = threadIdx.x; t < nl * g.N0r; t += blockDim.x) {
-    int l = t / g.N0r, i = t - l * g.N0r;
-    long long L = l0 + l;
-    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
-    spec[c * g.Nh + yz * g.N0r + i] = res[(long)l * g.N0 + i];
+    const int l = t / g.N0r, i = t - l * g.N0r;
+    const int j = l >> 1;
+    const C z = res[(long)j * g.N0 + i], w = res[(long)j * g.N0 + (i == 0 ? 0 : g.N0 - i)];
+    C v;
+    if ((l & 1) == 0) { v.x = (R)0.5 * (z.x + w.x); v.y = (R)0.5 * (z.y - w.y); }
+    else { v.x = (R)0.5 * (z.y + w.y); v.y = (R)0.5 * (w.x - z.x); }
+    const long long L = l0 + l;
+    const long long c = L / nyz, yz = L - c * nyz;
+    spec[c * g.Nh + yz * g.N0r + i] = v;
   }
 }
 
-// inverse: spectrum -> real planes (ld_out), c2r by Hermitian extension.
-// If `accumulate`, out += scale * result (FP64 accumulation of an update).
+// inverse: spectrum -> real planes (ld_out), c2r by Hermitian extension; the half
+// spectra A, B of real lines 2j, 2j+1 are transformed together as z = A + i B (both
+// Hermitian-extended), whose inverse is a + i b.
 template <typename R, typename Rout>
 __global__ void k_xinv(SpecGeom g, AxisPlan px, const typename cpx<R>::t* __restrict__ spec, Rout* __restrict__ field,
                        long long ld_out, int LX, const SpecItem* __restrict__ items) {
   typedef typename cpx<R>::t C;
   if (items) { spec = (const C*)items[blockIdx.y].spec; field = (Rout*)items[blockIdx.y].out; }
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
-  C* b = a + (long)LX * g.N0;
   const long long nlines = 9LL * g.N1 * g.N2;
   const long long l0 = (long long)blockIdx.x * LX;
   const int nl = (int)min((long long)LX, nlines - l0);
+  const int np = (nl + 1) >> 1;
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + (long)np * g.N0;
+  C* hs = b + (long)np * g.N0;           // the nl half spectra (2 np N0 + nl N0r <= 2 LX N0)
+  const long long nyz = (long long)g.N1 * g.N2;
   for (int t = threadIdx.x; t < nl * g.N0r; t += blockDim.x) {
-    int l = t / g.N0r, i = t - l * g.N0r;
-    long long L = l0 + l;
-    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
-    a[(long)l * g.N0 + i] = spec[c * g.Nh + yz * g.N0r + i];
+    const int l = t / g.N0r, i = t - l * g.N0r;
+    const long long L = l0 + l;
+    const long long c = L / nyz, yz = L - c * nyz;
+    hs[t] = spec[c * g.Nh + yz * g.N0r + i];
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nl * g.N0; t += blockDim.x) {
-    int l = t / g.N0, i = t - l * g.N0;
-    if (i >= g.N0r) { C v = a[(long)l * g.N0 + (g.N0 - i)]; v.y = -v.y; a[(long)l * g.N0 + i] = v; }
+  for (int t = threadIdx.x; t < np * g.N0; t += blockDim.x) {
+    const int j = t / g.N0, k = t - j * g.N0;
+    const bool hi = k >= g.N0r;
+    const int kk = hi ? g.N0 - k : k;
+    C A = hs[(long)(2 * j) * g.N0r + kk], B;
+    if (2 * j + 1 < nl) B = hs[(long)(2 * j + 1) * g.N0r + kk];
+    else { B.x = 0; B.y = 0; }
+    if (hi) { A.y = -A.y; B.y = -B.y; }
+    C v;
+    v.x = A.x - B.y; v.y = A.y + B.x;
+    a[t] = v;
   }
   __syncthreads();
-  C* res = block_fft<R>(a, b, nl, px, +1);
+  C* res = block_fft<R>(a, b, np, px, +1);
   for (int t = threadIdx.x; t < nl * g.N0; t += blockDim.x) {
-    int l = t / g.N0, x = t - l * g.N0;
-    long long L = l0 + l;
-    long long c = L / ((long long)g.N1 * g.N2), yz = L - c * g.N1 * g.N2;
-    field[c * ld_out + yz * g.N0 + x] = (Rout)res[t].x;
+    const int l = t / g.N0, x = t - l * g.N0;
+    const C v = res[(long)(l >> 1) * g.N0 + x];
+    const long long L = l0 + l;
+    const long long c = L / nyz, yz = L - c * nyz;
+    field[c * ld_out + yz * g.N0 + x] = (Rout)((l & 1) ? v.y : v.x);
   }
 }
 
@@ -519,10 +548,15 @@ SpecLaunch spec_launch_tiles(int N0, int N1, int N2, size_t csize, int LX, int T
   L.g.N0 = N0; L.g.N1 = N1; L.g.N2 = N2; L.g.N0r = N0 / 2 + 1;
   L.g.N = (long long)N0 * N1 * N2;
   L.g.Nh = (long long)L.g.N0r * N1 * N2;
-  L.LX = std::max(1, LX);
+  // x lines are transformed in pairs (2m, 2m + 1) of the global line index; an even
+  // number of lines per block keeps every pair inside one block for any tile choice, so
+  // the results do not depend on LX
+  L.LX = std::max(2, LX + (LX & 1));
   L.TIy = std::max(1, std::min(TIy, L.g.N0r));
   L.TIz = std::max(1, std::min(TIz, L.g.N0r));
-  L.smx = 2 * (size_t)L.LX * N0 * csize;
+  // x passes: two real lines per complex line (np = ceil(LX / 2)): ping-pong buffers of
+  // np lines, plus the inverse pass's staging of the LX half spectra
+  L.smx = (2 * (size_t)((L.LX + 1) / 2) * N0 + (size_t)L.LX * L.g.N0r) * csize;
   L.smy = 2 * (size_t)L.TIy * N1 * csize;
   L.smz = 2 * 9 * (size_t)L.TIz * N2 * csize + (size_t)L.TIz * N2 * sizeof(double);
   long long nlines = 9LL * N1 * N2;
