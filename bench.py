@@ -477,7 +477,10 @@ def gpu_arm(a):
                          "ms_per_launch": kms / max(1, launches),
                          "peak_source": "measured: dgx_measure_fp64_peak DFMA probe (MEASURED_PEAKS.json has no FP64)"},
             "kernel_time_share": {"constitutive": kms / ms, "spectral": spec_ms / ms,
-                                  "spectral_ms_per_residual": spec_ms / max(1, spec_n)},
+                                  "tangent": (t1["tangent_ms"] - t0["tangent_ms"]) / ms,
+                                  "spectral_ms_per_residual": spec_ms / max(1, spec_n),
+                                  "tangent_ms_per_launch": (t1["tangent_ms"] - t0["tangent_ms"]) /
+                                                           max(1, t1["tangent_launches"] - t0["tangent_launches"])},
             "roofline_spectral": spectral_roofline(cells, a.precision, spec_ms / max(1, spec_n), peak.value),
             "evaluations_per_increment": evals / a.steps,
             "latency": {"p50_increment_ms": 1e3 * statistics.median(lat),

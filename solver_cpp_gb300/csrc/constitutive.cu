@@ -232,12 +232,11 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
   }
 }
 
-// LU with partial pivoting of an NxN row-major matrix M[r][c], solving M x = b in place
-// (one right-hand side).  Returns false for an exactly singular pivot.
+// LU factorisation with partial pivoting of an NxN row-major matrix M[r][c] in place
+// (unit lower factor below the diagonal, reciprocal pivots in rp).  Returns false for
+// an exactly singular pivot.
 template <int N>
-__device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
-  int piv[N];
-  double rp[N];                                  // reciprocal pivots: one division per pivot
+__device__ __forceinline__ bool lu_factor(double (&M)[N * N], int (&piv)[N], double (&rp)[N]) {
   for (int k = 0; k < N; ++k) {
     int p = k;
     long long mx = absbits(M[N * k + k]);
@@ -249,7 +248,7 @@ __device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
     if (mx == 0) return false;
     if (p != k)
       for (int j = 0; j < N; ++j) { double t = M[N * k + j]; M[N * k + j] = M[N * p + j]; M[N * p + j] = t; }
-    double r = rcp(M[N * k + k]);
+    double r = rcp(M[N * k + k]);                  // reciprocal pivots: one reciprocal per pivot
     rp[k] = r;
     for (int i = k + 1; i < N; ++i) {
       double l = M[N * i + k] * r;
@@ -257,6 +256,11 @@ __device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
       for (int j = k + 1; j < N; ++j) M[N * i + j] = fma(-l, M[N * k + j], M[N * i + j]);
     }
   }
+  return true;
+}
+// x <- M^-1 x with the factors of lu_factor
+template <int N>
+__device__ __forceinline__ void lu_apply(const double (&M)[N * N], const int (&piv)[N], const double (&rp)[N], double* x) {
   for (int k = 0; k < N; ++k) { int p = piv[k]; if (p != k) { double t = x[k]; x[k] = x[p]; x[p] = t; } }
   for (int i = 1; i < N; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s = fma(-M[N * i + j], x[j], s); x[i] = s; }
   for (int i = N - 1; i >= 0; --i) {
@@ -264,42 +268,15 @@ __device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
     for (int j = i + 1; j < N; ++j) s = fma(-M[N * i + j], x[j], s);
     x[i] = s * rp[i];
   }
-  return true;
 }
-
-// multi-right-hand-side 9x9 form used by the tangent
-__device__ __forceinline__ bool lu_solve9(double (&M)[81], double* B, int nrhs) {
-  int piv[9];
-  double rp[9];
-  for (int k = 0; k < 9; ++k) {
-    int p = k;
-    long long mx = absbits(M[9 * k + k]);
-    for (int i = k + 1; i < 9; ++i) {
-      const long long v = absbits(M[9 * i + k]);
-      if (v > mx) { mx = v; p = i; }
-    }
-    piv[k] = p;
-    if (mx == 0) return false;
-    if (p != k)
-      for (int j = 0; j < 9; ++j) { double t = M[9 * k + j]; M[9 * k + j] = M[9 * p + j]; M[9 * p + j] = t; }
-    double r = rcp(M[9 * k + k]);
-    rp[k] = r;
-    for (int i = k + 1; i < 9; ++i) {
-      double l = M[9 * i + k] * r;
-      M[9 * i + k] = l;
-      for (int j = k + 1; j < 9; ++j) M[9 * i + j] = fma(-l, M[9 * k + j], M[9 * i + j]);
-    }
-  }
-  for (int c = 0; c < nrhs; ++c) {
-    double* x = B + 9 * c;
-    for (int k = 0; k < 9; ++k) { int p = piv[k]; if (p != k) { double t = x[k]; x[k] = x[p]; x[p] = t; } }
-    for (int i = 1; i < 9; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s = fma(-M[9 * i + j], x[j], s); x[i] = s; }
-    for (int i = 8; i >= 0; --i) {
-      double s = x[i];
-      for (int j = i + 1; j < 9; ++j) s = fma(-M[9 * i + j], x[j], s);
-      x[i] = s * rp[i];
-    }
-  }
+// LU with partial pivoting of an NxN row-major matrix M[r][c], solving M x = b in place
+// (one right-hand side).  Returns false for an exactly singular pivot.
+template <int N>
+__device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
+  int piv[N];
+  double rp[N];
+  if (!lu_factor<N>(M, piv, rp)) return false;
+  lu_apply<N>(M, piv, rp, x);
   return true;
 }
 
@@ -754,12 +731,19 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
   double t2[9], Y[9];
   mm(F, invFp0, t2);
   mtm(Fe, t2, Y);                          // Fe^T (F Fp0^-1)
-  // M = I + dt sum_a d_a vec(C:U_a) vec(P_a)^T, rows (p,o) cols (q,r), MAPPLAIN order.
-  // With P_a = pval d_a (x) n_a (signs compile-time): U_a = Y P_a = pval (Y d_a) (x) n_a,
-  // C : U_a in the cubic closed form, and the outer product with P_a is a signed add.
-  double M[81];
+  // dS/dF from the linearised stress integration M dS = rhs, with
+  //   M = I + dt sum_a d_a vec(C:U_a) vec(P_a)^T   (rows (p,o), columns (q,r)),
+  //   rhs(p,o; k,l) = (Fe C_po invFp^T)(k,l).
+  // C:U_a is symmetric, so M = I + E K with E (9 x 6) placing symmetric components in
+  // rows (p,o) and (o,p); the rhs is symmetric in (p,o) too (rhs = E B~).  Hence
+  // dS = E Y with (I6 + K E) Y = B~: a 6 x 6 system for the 9 right-hand sides,
+  // algebraically identical to the 9 x 9 one.  (K E)(s, t) = sum_a (C:U_a)_s q_a(t), q_a
+  // the pattern of s_a in the symmetric basis (00, 11, 22, 12, 02, 01).
+  // With P_a = pval d_a (x) n_a (signs compile-time): U_a = Y P_a = pval (Y d_a) (x) n_a
+  // and C : U_a in the cubic closed form.
+  double G6[36];
 #pragma unroll
-  for (int k = 0; k < 81; ++k) M[k] = (k % 10) == 0 ? 1.0 : 0.0;
+  for (int k = 0; k < 36; ++k) G6[k] = (k % 7) == 0 ? 1.0 : 0.0;
   const double cp2 = dt * mp.pval * mp.pval;
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
@@ -785,47 +769,47 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
       e[3 + m] = fcc_n(a, r) > 0 ? t1 + y[q] : t1 - y[q];
     }
     const double ct = mp.C12 * (e[0] + e[1] + e[2]);
-    double s6[6];
+    double s6[6];                                             // C : U_a (times dt d_a pval^2)
 #pragma unroll
     for (int i = 0; i < 3; ++i) s6[i] = c * fma(mp.C11mC12, e[i], ct);
 #pragma unroll
     for (int m = 0; m < 3; ++m) s6[3 + m] = c * (mp.C44 * e[3 + m]);
-    const double CU[9] = {s6[0], s6[5], s6[4], s6[5], s6[1], s6[3], s6[4], s6[3], s6[2]};
 #pragma unroll
-    for (int p = 0; p < 3; ++p)
+    for (int sl = 0; sl < 6; ++sl)
 #pragma unroll
-      for (int o = 0; o < 3; ++o)
-#pragma unroll
-        for (int q = 0; q < 3; ++q)
-#pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            if (fcc_s(a, q, r) > 0) M[9 * (3 * p + o) + 3 * q + r] += CU[p + 3 * o];
-            else if (fcc_s(a, q, r) < 0) M[9 * (3 * p + o) + 3 * q + r] -= CU[p + 3 * o];
-          }
+      for (int t = 0; t < 6; ++t) {
+        if (fcc_q(a, t) > 0) G6[6 * sl + t] += s6[sl];
+        else if (fcc_q(a, t) < 0) G6[6 * sl + t] -= s6[sl];
+      }
   }
-  // rhs(p,o,k,l) = (Fe C_po invFp^T)(k,l); stored B[(3k+l)*9 + (3p+o)] (9 rhs columns).
-  // Cubic C_pomn = C12 d_po d_mn + C44 (d_pm d_on + d_pn d_om) + (C11 - C12 - 2 C44) d_pomn:
+  // B~(s; k,l) for the symmetric slots s = (p,o), stored Bt[(3k+l)*6 + s].  Cubic
+  // C_pomn = C12 d_po d_mn + C44 (d_pm d_on + d_pn d_om) + (C11 - C12 - 2 C44) d_pomn:
   //   p == o: C12 (Fe invFp^T)(k,l) + (C11 - C12) Fe(k,p) invFp(l,p)
   //   p != o: C44 (Fe(k,p) invFp(l,o) + Fe(k,o) invFp(l,p))
-  double Bm[81];
+  double Bt[54];
   {
     double H[9];
     mmt(Fe, invFp, H);
 #pragma unroll
-    for (int p = 0; p < 3; ++p)
+    for (int sl = 0; sl < 6; ++sl) {
+      const int p = sl < 3 ? sl : (sl == 3 ? 1 : 0), o = sl < 3 ? sl : (sl == 5 ? 1 : 2);
 #pragma unroll
-      for (int o = 0; o < 3; ++o)
+      for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-#pragma unroll
-          for (int l = 0; l < 3; ++l) {
-            double v;
-            if (p == o) v = fma(mp.C11mC12, Fe[k + 3 * p] * invFp[l + 3 * p], mp.C12 * H[k + 3 * l]);
-            else v = mp.C44 * fma(Fe[k + 3 * p], invFp[l + 3 * o], Fe[k + 3 * o] * invFp[l + 3 * p]);
-            Bm[(3 * k + l) * 9 + 3 * p + o] = v;
-          }
+        for (int l = 0; l < 3; ++l) {
+          double v;
+          if (p == o) v = fma(mp.C11mC12, Fe[k + 3 * p] * invFp[l + 3 * p], mp.C12 * H[k + 3 * l]);
+          else v = mp.C44 * fma(Fe[k + 3 * p], invFp[l + 3 * o], Fe[k + 3 * o] * invFp[l + 3 * p]);
+          Bt[(3 * k + l) * 6 + sl] = v;
+        }
+    }
   }
-  lu_solve9(M, Bm, 9);   // Bm <- dSdF: Bm[(3k+l)*9 + 3p+o] = dS_po/dF_kl
+  {
+    int piv[6];
+    double rp[6];
+    lu_factor<6>(G6, piv, rp);
+    for (int kl = 0; kl < 9; ++kl) lu_apply<6>(G6, piv, rp, Bt + 6 * kl);   // Bt <- Y: dS in slots
+  }
   double u1[9], u2[9], u3[9], w[9];
   mmt(S, invFp, u1);                      // S invFp^T
   mm(F, invFp, u2);
@@ -844,12 +828,8 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
   for (int a = 0; a < NSLIP; ++a) mdd[a] = -cp2 * d[a];
   for (int kk = 0; kk < 3; ++kk)
     for (int ll = 0; ll < 3; ++ll) {
-      const double* dS = Bm + (3 * kk + ll) * 9;    // dS(p,o) at row 3p+o
-      double dSm[9];
-#pragma unroll
-      for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int o = 0; o < 3; ++o) dSm[p + 3 * o] = dS[3 * p + o];
+      const double* dS = Bt + (3 * kk + ll) * 6;    // dS in the symmetric slots
+      const double dSm[9] = {dS[0], dS[5], dS[4], dS[5], dS[1], dS[3], dS[4], dS[3], dS[2]};
       // G = -dt sum_a d_a (P_a : dS) P_a = pval^2 sum_a mdd_a (d_a . dS n_a) d_a (x) n_a,
       // through the slip planes' normals: v_p = dS n_p, then per-plane sums of d_a
       double Gs[4][3];

@@ -29,7 +29,7 @@ struct MatParams {
   double P[NSLIP][9];        // Schmid matrices d (x) n, column-major 3x3
   double h0h[7];             // h0 times the seven cF slip-slip interaction values (h_sl-sl)
   double xi_inf, h0, n, gdot0, a, c1, c2;
-  double C11mC12, C12, C44x2;  // cubic stiffness: C11 - C12, C12, 2 C44
+  double C11mC12, C12;         // cubic stiffness: C11 - C12, C12
   double C44;
   double hC11mC12, hC12;       // (C11 - C12) / 2, C12 / 2
   double ngdot0, rxi_inf;      // n * gdot0, 1 / xi_inf

@@ -354,7 +354,7 @@ MatParams make_params(const dgx_material& m) {
   p.N_iter_state_max = m.N_iter_state_max; p.N_iter_Lp_max = m.N_iter_Lp_max;
   p.f_update_jacobi_Lp = m.f_update_jacobi_Lp < 1 ? 1 : m.f_update_jacobi_Lp;
   p.n_int = (m.n == std::floor(m.n) && m.n >= 1 && m.n <= 64) ? (int)m.n : -1;
-  p.C11mC12 = m.C11 - m.C12; p.C12 = m.C12; p.C44x2 = 2.0 * m.C44; p.C44 = m.C44;
+  p.C11mC12 = m.C11 - m.C12; p.C12 = m.C12; p.C44 = m.C44;
   p.hC11mC12 = 0.5 * p.C11mC12; p.hC12 = 0.5 * m.C12;
   p.ngdot0 = m.n * m.dot_gamma_0; p.rxi_inf = 1.0 / m.xi_inf;
   p.pval = std::fabs(p.P[0][1]);                       // (1/sqrt2)(1/sqrt3), as the host computed P
