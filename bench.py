@@ -110,6 +110,39 @@ def cpu_oracle_sample(a, increments, threads):
     return n * ev / dt, dt, ev, recs
 
 
+def cpu_one_core_sample(a):
+    """One residual evaluation of the workload on one host core with the CPU oracle:
+    the constitutive response of every cell at the first iteration's deformation
+    (F = I + dot_F dt), the divergence RMS and the Gamma convolution (each with its own
+    forward FFT, as the reference does).  Point-updates/s = cells / time."""
+    import numpy as np
+    from oracle import dgo
+    cells, size, mat_at, q = workload(a)
+    n = cells[0] * cells[1] * cells[2]
+    mat = dgo.material()
+    ps = dgo.PointSet(mat, np.asarray(q)[np.asarray(mat_at)])
+    F = np.tile(np.eye(3).ravel(order="F"), (n, 1))
+    F[:, 0] += 1e-3
+    x1, _ = dgo.xi(cells, size)
+    sc = dgo.scaled_geom(cells, size, 0)
+    C11, C12, C44 = mat.C11, mat.C12, mat.C44
+    Cref = np.zeros(81)
+    for i in range(3):
+        for j in range(3):
+            for k in range(3):
+                for l in range(3):
+                    v = C12 * (i == j) * (k == l) + C44 * ((i == k) * (j == l) + (i == l) * (j == k))
+                    v += (C11 - C12 - 2 * C44) * (i == j == k == l)
+                    Cref[i + 3 * j + 9 * k + 27 * l] = v
+    t0 = time.perf_counter()
+    ps.response(F, 1.0, want_dPdF=False, nthreads=1)
+    P = ps.field("P")
+    dgo.divergence_rms(cells, size, sc, x1, P)
+    dgo.gamma_convolution(cells, x1, Cref, np.zeros(9), P)
+    dt = time.perf_counter() - t0
+    return n / dt, dt
+
+
 def reference_arm(a):
     rank, world = dist_env()
     if rank != 0:
@@ -541,6 +574,12 @@ def gpu_arm(a):
                                         "sample": f"solver init + first {a.cpu_sample_increments} increment(s) of the "
                                                   f"{a.cells}^3 workload ({ev} residual evaluations, {dt:.1f} s), "
                                                   "CPU oracle with OpenMP over cells"}
+                v1, dt1 = cpu_one_core_sample(a)
+                line["cpu_baseline"]["one_core"] = {
+                    "value": v1, "unit": UNIT, "cores": 1,
+                    "sample": f"one residual evaluation of the {a.cells}^3 workload at its first iteration "
+                              f"(constitutive response of every cell, divergence RMS, Gamma convolution; {dt1:.1f} s), "
+                              "CPU oracle on one thread (the reference's per-rank serial loop)"}
             except Exception as ex:  # the baseline is reported, never required
                 line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": threads, "kind": "port",
                                         "sample": f"failed: {ex}"}
