@@ -171,7 +171,8 @@ __device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, d
 // tau = S : P_a = pval t with t the signed sum of S's components of the system's sign
 // pattern (compile time; S symmetric).  Division free: with prxi = pval / xi and
 // r = |tau| / xi = |t| prxi, gdot = gdot0 r^n sign(tau) and
-// |dgdot/dtau| = n gdot0 r^(n-1) / xi = (n gdot0 / pval) prxi r^(n-1).
+// |dgdot/dtau| = n gdot0 r^(n-1) / xi = (n gdot0 / pval) prxi r^(n-1); dg receives
+// prxi r^(n-1), the callers apply the constant n gdot0 / pval with their own factors.
 // Accumulators start at -0.0 (the additive identity) so the first term is free.
 __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, const double* prxi,
                                          double* gdot, double* dg) {
@@ -195,7 +196,7 @@ __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, c
     const double r = fabs(t) * prxi[a];
     const double p = pow_nm1(r, mp);         // r^(n-1)
     gdot[a] = copysign(mp.gdot0 * (r * p), t);
-    if (dg) dg[a] = mp.ngdot0_p * (prxi[a] * p);
+    if (dg) dg[a] = prxi[a] * p;
   }
 }
 
@@ -378,7 +379,8 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       mtm(A, Fe_, W);
       double cd[NSLIP], co[NSLIP];
       {
-        const double sd = dt * mp.pval * mp.pval * mp.C11mC12, so = dt * mp.pval * mp.pval * mp.C44;
+        const double cdt = dt * mp.pval * mp.pval * mp.ngdot0_p;      // dg carries prxi r^(n-1)
+        const double sd = cdt * mp.C11mC12, so = cdt * mp.C44;
 #pragma unroll
         for (int a = 0; a < NSLIP; ++a) { cd[a] = sd * dg[a]; co[a] = so * dg[a]; }
       }
@@ -744,7 +746,7 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
   double G6[36];
 #pragma unroll
   for (int k = 0; k < 36; ++k) G6[k] = (k % 7) == 0 ? 1.0 : 0.0;
-  const double cp2 = dt * mp.pval * mp.pval;
+  const double cp2 = dt * mp.pval * mp.pval * mp.ngdot0_p;        // d carries prxi r^(n-1)
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
     const double c = cp2 * d[a];
@@ -823,7 +825,7 @@ __device__ void tangent_point(const MatParams& mp, const double* F, const double
     for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int l = 0; l < 3; ++l) dPdF[p + 3 * j + 9 * p + 27 * l] = w[l + 3 * j];
-  double mdd[NSLIP];                      // -dt pval^2 d_a
+  double mdd[NSLIP];                      // -dt pval^2 |dgdot_a/dtau_a|
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) mdd[a] = -cp2 * d[a];
   for (int kk = 0; kk < 3; ++kk)

@@ -78,14 +78,14 @@ struct ConsCounters {
 
 // Algorithmic FP64 flops of the constitutive kernel per counted unit (FMA = 2, division,
 // reciprocal and square root = 1), counted from its arithmetic: one Lp Newton iteration
-// (B, Fe, Hooke, 12-system kinetics with derivatives, Lp, residual and norms: 402), one
+// (B, Fe, Hooke, 12-system kinetics with derivatives, Lp, residual and norms: 390), one
 // Jacobian step (W, the signed sums T^ scaled by the cubic moduli, B^ b and the 6 x 6
 // matrix I + B^ T^, its LU with one right-hand side, the step b - T^ u: 923), one state
 // integration call (Fp0^-1, F Fp0^-1, pval/xi, first dot state, predictor, and once
 // the iteration ends Fp^-1, P, det and Fp scaling: 860) and one fixed-point iteration
 // (pval/xi, hardening from the slip rates of the last Lp iteration summed per
 // interaction type, damper, state update: 743).
-constexpr double FLOPS_LP = 402.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS_FPI = 743.0;
+constexpr double FLOPS_LP = 390.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS_FPI = 743.0;
 
 // Stress boundary condition of one RVE's solve, resident on the device so that the
 // BC step of a residual evaluation (form_residual) needs no host round trip.
