@@ -171,8 +171,9 @@ __device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, d
 // tau = S : P_a = pval t with t the signed sum of S's components of the system's sign
 // pattern (compile time; S symmetric).  Division free: with prxi = pval / xi and
 // r = |tau| / xi = |t| prxi, gdot = gdot0 r^n sign(tau) and
-// |dgdot/dtau| = n gdot0 r^(n-1) / xi = (n gdot0 / pval) prxi r^(n-1); dg receives
-// prxi r^(n-1), the callers apply the constant n gdot0 / pval with their own factors.
+// |dgdot/dtau| = n gdot0 r^(n-1) / xi = (n gdot0 / pval) prxi r^(n-1).  The constant
+// factors are left to the callers, which fold them into their own: gdot receives
+// r^n sign(tau) (= gdot / gdot0) and dg receives prxi r^(n-1).
 // Accumulators start at -0.0 (the additive identity) so the first term is free.
 __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, const double* prxi,
                                          double* gdot, double* dg) {
@@ -195,14 +196,14 @@ __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, c
     }
     const double r = fabs(t) * prxi[a];
     const double p = pow_nm1(r, mp);         // r^(n-1)
-    gdot[a] = copysign(mp.gdot0 * (r * p), t);
+    gdot[a] = copysign(r * p, t);
     if (dg) dg[a] = prxi[a] * p;
   }
 }
 
 // phenopowerlaw dotState: [dot xi (12), |gdot| (12)]
-// gdot: the slip rates of S if already known (the last Lp iteration evaluated them
-// for the same S and xi), else null
+// gdot: the slip rates of S in units of gdot0 if already known (the last Lp iteration
+// evaluated them for the same S and xi), else null
 __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, const double* prxi,
                                           double* dot, const double* gdot = nullptr) {
   double g[NSLIP];
@@ -218,8 +219,9 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
   for (int a = 0; a < NSLIP; ++a) {
     double x = 1.0 - xi[a] * mp.rxi_inf;
     double left = copysign(pow_a(fabs(x), mp), x);
-    // h0 sum_b h_ab |gdot_b| with h_ab one of seven values: the slip rates are summed
-    // per interaction type (compile-time grouping), then weighted by h0 h_t
+    // h0 sum_b h_ab |gdot_b| with h_ab one of seven values: the slip rates (in units of
+    // gdot0) are summed per interaction type (compile-time grouping), then weighted by
+    // h0 gdot0 h_t
     double gt[7];
 #pragma unroll
     for (int t = 0; t < 7; ++t) gt[t] = -0.0;
@@ -229,7 +231,7 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
 #pragma unroll
     for (int t = 1; t < 7; ++t) hs = fma(mp.h0h[t], gt[t], hs);
     dot[a] = left * hs;
-    dot[NSLIP + a] = g[a];
+    dot[NSLIP + a] = mp.gdot0 * g[a];
   }
 }
 
@@ -303,7 +305,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     kinetics(mp, S, prxi, gdot, dg);
     // Lp = pval sum_a gdot_a d_a (x) n_a with the cF signs folded at compile time: the
     // three systems of a slip plane share n, so the plane sums Y_p = sum_a gdot_a d_a
-    // come first, then Lp(k, l) = pval sum_p n_p(l) Y_p(k)
+    // come first, then Lp(k, l) = pval gdot0 sum_p n_p(l) Y_p(k) (gdot in units of gdot0)
     double Y[4][3];
 #pragma unroll
     for (int p = 0; p < 4; ++p)
@@ -327,7 +329,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
           if (fcc_n(3 * p, l) > 0) s += Y[p][k];
           else s -= Y[p][k];
         }
-        Lpc[k + 3 * l] = mp.pval * s;
+        Lpc[k + 3 * l] = mp.pgdot0 * s;
       }
     double res[9];
 #pragma unroll

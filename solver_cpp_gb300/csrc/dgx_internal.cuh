@@ -27,13 +27,14 @@ __host__ __device__ constexpr int cf_interaction(int r, int b) {
 struct MatParams {
   double C66[36];            // column-major 6x6, Voigt 11,22,33,23,13,12
   double P[NSLIP][9];        // Schmid matrices d (x) n, column-major 3x3
-  double h0h[7];             // h0 times the seven cF slip-slip interaction values (h_sl-sl)
+  double h0h[7];             // h0 gdot0 times the seven cF slip-slip interaction values (h_sl-sl)
   double xi_inf, h0, n, gdot0, a, c1, c2;
   double C11mC12, C12;         // cubic stiffness: C11 - C12, C12
   double C44;
   double hC11mC12, hC12;       // (C11 - C12) / 2, C12 / 2
   double ngdot0, rxi_inf;      // n * gdot0, 1 / xi_inf
   double ngdot0_p;             // n * gdot0 / pval
+  double pgdot0;               // pval * gdot0
   double pval;                 // magnitude of the non-zero Schmid entries (1/sqrt2 * 1/sqrt3)
   double atol_xi, atol_gamma;
   double r_cutback_min, r_cutback, r_increase, eps_rel_state;
@@ -78,14 +79,14 @@ struct ConsCounters {
 
 // Algorithmic FP64 flops of the constitutive kernel per counted unit (FMA = 2, division,
 // reciprocal and square root = 1), counted from its arithmetic: one Lp Newton iteration
-// (B, Fe, Hooke, 12-system kinetics with derivatives, Lp, residual and norms: 390), one
+// (B, Fe, Hooke, 12-system kinetics with derivatives, Lp, residual and norms: 378), one
 // Jacobian step (W, the signed sums T^ scaled by the cubic moduli, B^ b and the 6 x 6
 // matrix I + B^ T^, its LU with one right-hand side, the step b - T^ u: 923), one state
 // integration call (Fp0^-1, F Fp0^-1, pval/xi, first dot state, predictor, and once
 // the iteration ends Fp^-1, P, det and Fp scaling: 860) and one fixed-point iteration
 // (pval/xi, hardening from the slip rates of the last Lp iteration summed per
-// interaction type, damper, state update: 743).
-constexpr double FLOPS_LP = 390.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS_FPI = 743.0;
+// interaction type, damper, state update: 755).
+constexpr double FLOPS_LP = 378.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS_FPI = 755.0;
 
 // Stress boundary condition of one RVE's solve, resident on the device so that the
 // BC step of a residual evaluation (form_residual) needs no host round trip.

@@ -345,7 +345,7 @@ MatParams make_params(const dgx_material& m) {
   }
   p.xi_inf = m.xi_inf;
   p.h0 = m.h_0 * (1.0 + m.c_1 * std::pow(0.0, m.c_2));     // no twins: sum f = 0
-  for (int t = 0; t < 7; ++t) p.h0h[t] = p.h0 * m.h_sl_sl[t];
+  for (int t = 0; t < 7; ++t) p.h0h[t] = p.h0 * m.dot_gamma_0 * m.h_sl_sl[t];
   p.n = m.n; p.gdot0 = m.dot_gamma_0; p.a = m.a; p.c1 = m.c_1; p.c2 = m.c_2;
   p.atol_xi = m.atol_xi; p.atol_gamma = m.atol_gamma;
   p.r_cutback_min = m.r_cutback_min; p.r_cutback = m.r_cutback; p.r_increase = m.r_increase;
@@ -359,6 +359,7 @@ MatParams make_params(const dgx_material& m) {
   p.ngdot0 = m.n * m.dot_gamma_0; p.rxi_inf = 1.0 / m.xi_inf;
   p.pval = std::fabs(p.P[0][1]);                       // (1/sqrt2)(1/sqrt3), as the host computed P
   p.ngdot0_p = p.ngdot0 / p.pval;
+  p.pgdot0 = p.pval * m.dot_gamma_0;
   p.eps_rel_Lp2 = m.eps_rel_Lp * m.eps_rel_Lp; p.eps_abs_Lp2 = m.eps_abs_Lp * m.eps_abs_Lp;
   double aq = 4.0 * m.a;
   p.a_quarters = (aq == std::floor(aq) && aq >= 1 && aq <= 256) ? (int)aq : -1;
