@@ -259,6 +259,7 @@ def batch_leg(g, torch, n_rves, increments, seconds, compare):
            "seconds": ms * 1e-3, "all_done": not active,
            "constitutive_share": (s1["constitutive_ms"] - s0["constitutive_ms"]) / ms,
            "spectral_share": (s1["spectral_ms"] - s0["spectral_ms"]) / ms,
+           "round_device_share": (s1["round_device_ms"] - s0["round_device_ms"]) / ms,
            "launches": s1["launches"] - s0["launches"], "autotuned": batch.tuning()}
     batch.close()
     for r, _, _ in rves:

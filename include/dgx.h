@@ -233,7 +233,9 @@ dgx_status dgx_batch_member(const dgx_batch* batch, int32_t slot, int32_t* done,
                             int32_t* status);
 /* Detach a finished member: the RVE returns to its own stream and the single-RVE calls. */
 dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
-/* ms: CUDA-event time of [0] constitutive launches, [1] spectral chains, [2] unused;
+/* ms: CUDA-event time of [0] constitutive launches, [1] spectral chains, [2] the rounds'
+ * device work (each round from its first copy to its last; wall time beyond it is host
+ * work between rounds);
  * out: [0] point evaluations, [1] state integrations, [2] Lp iterations, [3] rounds,
  * [4] launches of the batched kernels, [5] Jacobian factorisations, [6] h2d bytes,
  * [7] d2h bytes of the executor, [8] fixed-point iterations, [9] rounds issued as a

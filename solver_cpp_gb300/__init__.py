@@ -303,9 +303,9 @@ class Batch:
     def stats(self):
         ms = (C.c_double * 3)(); a = (C.c_int64 * 10)()
         _d.check(_d.lib().dgx_batch_stats(self.h, ms, a), "dgx_batch_stats")
-        return dict(constitutive_ms=ms[0], spectral_ms=ms[1], point_evaluations=a[0], state_iterations=a[1],
-                    lp_iterations=a[2], rounds=a[3], launches=a[4], jacobians=a[5], h2d_bytes=a[6],
-                    d2h_bytes=a[7], fpi_iterations=a[8], graph_rounds=a[9])
+        return dict(constitutive_ms=ms[0], spectral_ms=ms[1], round_device_ms=ms[2], point_evaluations=a[0],
+                    state_iterations=a[1], lp_iterations=a[2], rounds=a[3], launches=a[4], jacobians=a[5],
+                    h2d_bytes=a[6], d2h_bytes=a[7], fpi_iterations=a[8], graph_rounds=a[9])
 
     def set_round_points(self, points):
         """Cap the residual evaluations per round (cells); 0 serves every request."""

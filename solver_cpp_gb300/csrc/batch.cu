@@ -197,7 +197,7 @@ struct Executor {
   ConsCounters cnt_last{};
   ConsCounters* h_cnt = nullptr;
   std::map<std::tuple<int, int, int, double, double, double, int, int, int>, SpecLaunch> spec_tuned;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // [4], [5]: a round's first and last copy
   double t_ms[3] = {0, 0, 0};
   int64_t t_n[3] = {0, 0, 0};
   int64_t launches = 0, bytes_h2d = 0, bytes_d2h = 0, point_evals = 0, rounds = 0;
@@ -277,7 +277,7 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
 
 void executor_stats(const Executor* e, double ms[3], int64_t n[3], int64_t* launches, int64_t* h2d_b, int64_t* d2h_b,
                     int64_t* graph_rounds) {
-  for (int i = 0; i < 3; ++i) { ms[i] += e->t_ms[i]; n[i] += e->t_n[i]; }
+  for (int i = 0; i < 2; ++i) { ms[i] += e->t_ms[i]; n[i] += e->t_n[i]; }
   *launches += e->launches; *h2d_b += e->bytes_h2d; *d2h_b += e->bytes_d2h;
   if (graph_rounds) *graph_rounds += e->graph_rounds;
 }
@@ -424,6 +424,7 @@ static dgx_status ex_issue(Executor* e, RoundPlan& p, bool capture, IssueCount& 
   auto h2d = [&](void* d, const void* h, size_t b) { c.h2d += (int64_t)b; return cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, st); };
   auto d2h = [&](void* h, const void* d, size_t b) { c.d2h += (int64_t)b; return cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, st); };
   const int n = p.n;
+  CK(rec(4));
   if (n > 0) {
     CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, st));
     CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * 16, st));
@@ -466,6 +467,7 @@ static dgx_status ex_issue(Executor* e, RoundPlan& p, bool capture, IssueCount& 
     c.launches += 2;
     CK(d2h(e->h_mout, e->d_mout, sizeof(double) * 64 * p.nm));
   }
+  CK(rec(5));
   CK(cudaGetLastError());
   return DGX_OK;
 }
@@ -610,6 +612,10 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
   CK(cudaStreamSynchronize(e->st));
   CK(cudaGetLastError());
   e->rounds++;
+  if (n > 0 || p.nm > 0) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e->ev[4], e->ev[5]); e->t_ms[2] += ms; e->t_n[2]++;
+  }
   if (n > 0) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[0] += ms; e->t_n[0]++;
