@@ -292,8 +292,7 @@ static GridKey grid_key(const dgx_rve* r) {
 // FFT tile shape of a grid: the tuned one, or (first time, when tuning) chosen per pass.
 // Each pass's time depends only on its own tile (x lines per block, x-frequencies per y
 // block, x-frequencies per z block), so every dimension is scanned with the others at
-// their defaults (x and y: 1/2 .. 8x the default, z: 1/2 .. 2x) and the fastest value of
-// each is kept.  Every candidate is timed on this group's own convolution and computes
+// their defaults and the fastest value of each is kept.  Every candidate is timed on this group's own convolution and computes
 // the same result.
 static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0, const SpecItem* items, int cnt,
                                     const GammaArgs& ga) {
@@ -307,26 +306,37 @@ static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0
   auto time_of = [&](const SpecLaunch& L) -> float {
     if (!spec_launch_fits(L)) return 1e30f;
     spec_prepare(L, fp32);
+    // best of three, on at most four of the group's RVEs (the tile choice is per RVE)
     float ms = 1e30f;
-    for (int rep = 0; rep < 2; ++rep) {
+    for (int rep = 0; rep < 3; ++rep) {
       cudaEventRecord(e->ev[2], e->st);
-      spec_convolve_batch(L, fp32, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan, items, cnt, ga, e->st);
+      spec_convolve_batch(L, fp32, r0->ax[0].plan, r0->ax[1].plan, r0->ax[2].plan, items, std::min(cnt, 4), ga,
+                          e->st);
       cudaEventRecord(e->ev[3], e->st);
       cudaEventSynchronize(e->ev[3]);
-      cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e->ev[2], e->ev[3]);
+      ms = std::min(ms, t);
     }
-    e->launches += 10;
+    e->launches += 15;
     return cudaGetLastError() == cudaSuccess ? ms : 1e30f;
   };
-  const int facs[5] = {-2, 2, 4, 8, 1};      // x1/2, x2, x4, x8 (1: the default itself)
   int best[3] = {base.LX, base.TIy, base.TIz};
   const float t0 = time_of(base);
   for (int d = 0; d < 3; ++d) {
     float bt = t0;
     const int v0 = d == 0 ? base.LX : d == 1 ? base.TIy : base.TIz;
-    for (int f = 0; f < 4; ++f) {
-      if (d == 2 && facs[f] > 2) continue;
-      const int v = facs[f] < 0 ? v0 / 2 : v0 * facs[f];
+    // x: 1/2 .. 8x the default; y and z: every tile width up to 16 x-frequencies (the
+    // z pass holds a whole tile's 9 components in shared memory, so its width sets both
+    // the blocks per SM and the number of waves), plus 2x and 4x the default for y
+    int cand[24], nc = 0;
+    if (d == 0) { cand[nc++] = v0 / 2; cand[nc++] = 2 * v0; cand[nc++] = 4 * v0; cand[nc++] = 8 * v0; }
+    else {
+      for (int v = 1; v <= 16; ++v) cand[nc++] = v;
+      if (d == 1) { cand[nc++] = 2 * v0; cand[nc++] = 4 * v0; }
+    }
+    for (int f = 0; f < nc; ++f) {
+      const int v = cand[f];
       if (v < 1 || v == v0 || (d > 0 && v > g.N0r) || (d == 0 && v > 9 * g.N1 * g.N2)) continue;
       int t[3] = {base.LX, base.TIy, base.TIz};
       t[d] = v;
