@@ -205,14 +205,21 @@ class RVE:
         _d.check(_d.lib().dgx_update_coords(self.h, _d.dptr(un), _d.dptr(up)), "dgx_update_coords")
         return un.reshape(-1, 3), up.reshape(-1, 3)
 
-    def get(self, name):
+    def get(self, name, out=None):
+        """A field (N, 3, 3) / (N, 12) or a volume quantity.  `out`: optional host buffer
+        of the field's size (float64, C-contiguous; e.g. pinned memory) to read into."""
         width = {"xi": 12, "gamma": 12}.get(name, 9)
         scalars = {"P_av": 9, "F_aim": 9, "C_volAvg": 81, "C_minMaxAvg": 81, "C_ref": 81, "S_compliance": 81}
         if name in scalars:
             out = np.zeros(scalars[name])
             _d.check(_d.lib().dgx_get(self.h, name.encode(), _d.dptr(out)), "dgx_get")
             return _unf9(out, 1)[0] if scalars[name] == 9 else out.reshape(3, 3, 3, 3, order="F")
-        out = np.zeros(width * self.N)
+        if out is None:
+            out = np.empty(width * self.N)
+        else:
+            out = out.reshape(-1)
+            if out.dtype != np.float64 or out.size != width * self.N or not out.flags.c_contiguous:
+                raise ValueError(f"dgx_get {name}: out must be {width * self.N} contiguous float64")
         _d.check(_d.lib().dgx_get(self.h, name.encode(), _d.dptr(out)), "dgx_get")
         return _unf9(out, self.N) if width == 9 else out.reshape(self.N, width)
 

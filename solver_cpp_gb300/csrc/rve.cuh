@@ -36,6 +36,8 @@ struct dgx_rve {
   dgx::ConsCounters* d_cnt = nullptr;
   double *d_xi_x = nullptr, *d_xi_y = nullptr, *d_xi_z = nullptr;
   double* d_dPdF = nullptr;        // optional (81 planes) for the boundary call
+  double* d_aos = nullptr;         // optional: 12 N doubles, device-side AoS staging of field reads
+                                   // (allocated on the first read; not part of the creation footprint)
   double *d_un = nullptr, *d_up = nullptr, *d_Favg = nullptr;   // optional: coordinate update
   dgx::BcBlock* d_bc = nullptr;    // stress BC of the current solve (device copy)
   int32_t* d_mat = nullptr;

@@ -538,7 +538,18 @@ dgx_status upload_aos(dgx_rve* r, const double* host, int w, double* planar) {
   r->n_launch++;
   return DGX_OK;
 }
+// planar device field -> AoS host array: transposed on the device (staging buffer of
+// 12 N doubles, allocated on first use), then one copy into the caller's memory
 dgx_status download_aos(dgx_rve* r, const double* planar, int w, double* host) {
+  if (w <= 12) {
+    if (!r->d_aos) TRY(dalloc(r, &r->d_aos, 12 * r->N));
+    k_planar2aos<<<nblk(w * r->N), 256, 0, r->st>>>(planar, r->N, w, r->N, r->d_aos);
+    r->n_launch++;
+    CK(d2h(r, host, r->d_aos, sizeof(double) * w * r->N));
+    CK(cudaStreamSynchronize(r->st));
+    CK(cudaGetLastError());
+    return DGX_OK;
+  }
   std::vector<double> tmp((size_t)w * r->N);
   CK(d2h(r, tmp.data(), planar, sizeof(double) * w * r->N));
   CK(cudaStreamSynchronize(r->st));

@@ -153,3 +153,26 @@ def test_mixed_precision_error_bound(gpu):
     b = mixed.loop_over_loadcase(steps)
     for ra, rb in zip(a, b):
         assert rel(rb["P_av"], ra["P_av"]) < 1e-5
+
+
+def test_field_reads_into_caller_buffers(gpu):
+    """dgx_get transposes on the device and copies into the caller's memory: the fields
+    read into a given buffer equal a fresh read, for 9- and 12-component fields, and a
+    buffer of the wrong size is refused."""
+    from solver_cpp_gb300.synthetic import microstructure
+    cells = (6, 5, 4)
+    mat_at, q = microstructure(cells, 4, seed=5)
+    rve = gpu.RVE(cells, (1, 1, 1), mat_at, q)
+    rve.loop_over_loadcase([gpu.load_step("tensionX", t=1.0, N=1)])
+    n = rve.N
+    for name, w in (("P", 9), ("F", 9), ("Fp", 9), ("xi", 12)):
+        fresh = rve.get(name)
+        buf = np.full(w * n, np.nan)
+        view = rve.get(name, out=buf)
+        assert np.array_equal(view, fresh) and not np.isnan(buf).any()
+    P = rve.get("P")
+    F = np.swapaxes(P, 1, 2).reshape(-1)
+    assert np.array_equal(rve.get("P", out=np.empty(9 * n)), P) and F.size == 9 * n
+    with pytest.raises(ValueError):
+        rve.get("P", out=np.empty(9 * n - 1))
+    rve.close()
