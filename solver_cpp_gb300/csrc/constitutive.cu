@@ -9,11 +9,14 @@
 //   src/phase_mechanical_elastic.f90:157-195, phase_mechanical_plastic_phenopowerlaw.f90:298-483
 //   src/homogenization.f90:219-324      per-cell restore / partition / homogenise (1 constituent)
 // GB300-specific restatement: FP64 is the scarce pipe on this part, so the
-// literal 3x3x3x3 algebra is replaced by exact rank-12 forms.  With Fi = I (no
+// literal 3x3x3x3 algebra is replaced by exact low-rank forms.  With Fi = I (no
 // eigenstrain kinematics) and dLp/dS = sum_a |dgamma_a/dtau_a| P_a (x) P_a:
 //   Jacobian  J = I + dt sum_a |dg_a| vec(P_a) vec(W Q_a)^T,  W = A^T Fe,  Q_a = C : P_a
 //   tangent   lhs = dt sum_a |dg_a| vec(C : U_a) vec(P_a)^T,  U_a = Fe^T (F Fp0^-1) P_a
-// which are algebraically identical to the reference's contractions.
+// Both have rank 6 in the basis of symmetric matrices (Q_a and C : U_a are
+// symmetric), so their linear systems are solved as 6 x 6 ones (Woodbury), and the
+// Schmid signs of the cF slip systems are folded in at compile time; all of it is
+// algebraically identical to the reference's contractions.
 #include <algorithm>
 
 #include "../../include/dgx.h"

@@ -3,7 +3,8 @@
 Tolerance (FP64 plain form): 1e-8 relative, normalised by the largest magnitude
 of the compared quantity (the bound required of the GPU drop-in).  Observed
 agreement is ~1e-12; the kernels reorder FP64 sums and use exact algebraic
-rewrites (rank-12 Jacobian, Fi = I), so bitwise equality is not expected.
+rewrites (low-rank Jacobian and tangent solved as 6x6 systems, Fi = I), so bitwise
+equality is not expected.
 """
 import numpy as np
 import pytest
