@@ -562,7 +562,7 @@ def gpu_arm(a):
             line["mixed"] = {"value": vals["mixed"], "unit": UNIT, "fp64_same_run": vals["fp64"],
                              "increments": a.steps, "max_rel_P_av_error_vs_fp64": max(errs),
                              "per_increment_error": errs,
-                             "note": "FP32 FFT / Gamma with FP64 accumulation; timed like value"}
+                             "note": "FP32 FFT / Gamma with FP64 accumulation; Lp Newton Jacobian and hardening rate in FP32 (residual, update, convergence tests, tangent FP64); timed like value"}
         if a.batch_rves > 0:
             line["batched"] = batch_leg(g, torch, a.batch_rves, 20, a.batch_seconds, a.batch_compare)
         if a.mixed_large:

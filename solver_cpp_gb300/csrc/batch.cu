@@ -191,7 +191,7 @@ struct Executor {
   // rounds per variant, and per grid the FFT tile shape, timed on the first round's data
   // (results do not depend on either)
   bool tune_cons = true, tune_spec = true;
-  int res_by_variant[CONS_VARIANTS] = {};
+  int res_by_variant[2][CONS_VARIANTS] = {};   // [mixed form][variant]: resident blocks
   double cons_cost[CONS_VARIANTS][3] = {};
   int cons_trials[CONS_VARIANTS] = {}, cons_round = 0;
   ConsCounters cnt_last{};
@@ -255,15 +255,16 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   else { EA(&e->cnt, (ConsCounters**)nullptr, 1); e->own_cnt = true; cudaMemset(e->cnt, 0, sizeof(ConsCounters)); }
 #undef EA
   for (auto& v : e->ev) cudaEventCreate(&v);
-  for (int k = 0; k < CONS_VARIANTS; ++k) e->res_by_variant[k] = constitutive_batch_resident(k);
-  e->resident = e->res_by_variant[e->cons_variant];
+  for (int k = 0; k < CONS_VARIANTS; ++k)
+    for (int m = 0; m < 2; ++m) e->res_by_variant[m][k] = constitutive_batch_resident(k, m == 1);
+  e->resident = e->res_by_variant[0][e->cons_variant];
   const char* at = std::getenv("DGX_AUTOTUNE");
   const bool tune = !(at && at[0] == '0');
   e->tune_cons = tune && cons_block <= 0;       // an explicit block size is kept
   const char* cv = std::getenv("DGX_CONS_VARIANT");   // pin a launch variant (0..4) for measurements
   if (cv && cv[0] >= '0' && cv[0] < '0' + CONS_VARIANTS && cv[1] == 0) {
     e->cons_variant = cv[0] - '0';
-    e->resident = e->res_by_variant[e->cons_variant];
+    e->resident = e->res_by_variant[0][e->cons_variant];
     e->tune_cons = false;
   }
   e->tune_spec = tune;
@@ -572,12 +573,12 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
     }
     p.variant = cand >= 0 ? cand : e->cons_variant;
     const int BS = cons_variant_bs(p.variant);
-    const int resident = e->res_by_variant[p.variant];
     for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
     {
       long long tiles = 0;
       int gstart = 0;
       auto close_group = [&](int jend) {
+        const int resident = e->res_by_variant[q[order[gstart]].r->mp.mixed ? 1 : 0][p.variant];
         const int grid = (int)std::max<long long>(1, std::min<long long>(tiles, resident));
         p.cons.push_back(ConsGroup{gstart, jend - gstart, grid, tiles, &q[order[gstart]].r->mp});
       };
@@ -653,7 +654,7 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
         int best = 0;
         for (int k = 1; k < CONS_VARIANTS; ++k) if (med[k] < med[best]) best = k;
         e->cons_variant = best;
-        e->resident = e->res_by_variant[best];
+        e->resident = e->res_by_variant[0][best];
         e->tune_cons = false;
       }
     }

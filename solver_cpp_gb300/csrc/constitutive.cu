@@ -33,7 +33,8 @@ __device__ __forceinline__ void mm(const double* __restrict__ A, const double* _
       C[i + 3 * j] = A[i] * B[3 * j] + A[i + 3] * B[1 + 3 * j] + A[i + 6] * B[2 + 3 * j];
 }
 // C = A^T B
-__device__ __forceinline__ void mtm(const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C) {
+template <typename R>
+__device__ __forceinline__ void mtm(const R* __restrict__ A, const R* __restrict__ B, R* __restrict__ C) {
 #pragma unroll
   for (int j = 0; j < 3; ++j)
 #pragma unroll
@@ -69,6 +70,16 @@ __device__ __forceinline__ double rcp(double x) {
   e = fma(-x, r, 1.0);
   return fma(r, e, r);
 }
+// FP32 forms for the mixed-precision Jacobian: magnitude bits and the hardware
+// reciprocal estimate rcp.approx.ftz.f32 (a Newton direction needs no more)
+__device__ __forceinline__ int absbits(float x) { return __float_as_int(x) & 0x7fffffff; }
+__device__ __forceinline__ float rcp(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ double fmx(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmx(float a, float b, float c) { return fmaf(a, b, c); }
 
 __device__ __forceinline__ bool inv33(const double* __restrict__ A, double* __restrict__ I, double* det = nullptr) {
   double c0 = A[4] * A[8] - A[7] * A[5];
@@ -206,7 +217,13 @@ __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, c
 
 // phenopowerlaw dotState: [dot xi (12), |gdot| (12)]
 // gdot: the slip rates of S in units of gdot0 if already known (the last Lp iteration
-// evaluated them for the same S and xi), else null
+// evaluated them for the same S and xi), else null.
+// MX (mixed form): the hardening rate dot xi_a = h0 sign(x)|x|^a sum_b h_ab |gdot_b|,
+// x = 1 - xi_a / xi_inf, is evaluated in FP32 from x and the slip rates formed in FP64
+// (the state itself, its update and the convergence test stay FP64: an FP32 rate
+// perturbs dot xi dt by ~1e-7 of itself, far below the state tolerance).  A rate of
+// magnitude 1e37 or more, or NaN, sends the point's dot state to the FP64 form.
+template <bool MX>
 __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, const double* prxi,
                                           double* dot, const double* gdot = nullptr) {
   double g[NSLIP];
@@ -218,6 +235,33 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
   }
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) g[a] = fabs(g[a]);
+  if constexpr (MX) {
+    float gf[NSLIP];
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) gf[a] = (float)g[a];
+    bool in_range = true;
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) {
+      const float x = (float)fma(-xi[a], mp.rxi_inf, 1.0);
+      const float y = fabsf(x);
+      float pa;
+      if (mp.a_quarters == 9) pa = (y * y) * sqrtf(sqrtf(y));   // y^(9/4)
+      else pa = powf(y, (float)mp.a);
+      float gt[7];
+#pragma unroll
+      for (int t = 0; t < 7; ++t) gt[t] = -0.0f;
+#pragma unroll
+      for (int b = 0; b < NSLIP; ++b) gt[cf_interaction(a, b) - 1] += gf[b];
+      float hs = mp.h0h_f[0] * gt[0];
+#pragma unroll
+      for (int t = 1; t < 7; ++t) hs = fmaf(mp.h0h_f[t], gt[t], hs);
+      const float d = copysignf(pa, x) * hs;
+      in_range &= fabsf(d) < 1e37f;                // false for NaN and overflow
+      dot[a] = (double)d;
+      dot[NSLIP + a] = mp.gdot0 * g[a];
+    }
+    if (in_range) return;
+  }
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
     double x = 1.0 - xi[a] * mp.rxi_inf;
@@ -240,58 +284,164 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
 
 // LU factorisation with partial pivoting of an NxN row-major matrix M[r][c] in place
 // (unit lower factor below the diagonal, reciprocal pivots in rp).  Returns false for
-// an exactly singular pivot.
-template <int N>
-__device__ __forceinline__ bool lu_factor(double (&M)[N * N], int (&piv)[N], double (&rp)[N]) {
+// an exactly singular pivot.  R: double (plain form) or float (mixed-form Jacobian).
+template <int N, typename R>
+__device__ __forceinline__ bool lu_factor(R (&M)[N * N], int (&piv)[N], R (&rp)[N]) {
   for (int k = 0; k < N; ++k) {
     int p = k;
-    long long mx = absbits(M[N * k + k]);
+    auto mx = absbits(M[N * k + k]);
     for (int i = k + 1; i < N; ++i) {
-      const long long v = absbits(M[N * i + k]);
+      const auto v = absbits(M[N * i + k]);
       if (v > mx) { mx = v; p = i; }
     }
     piv[k] = p;
     if (mx == 0) return false;
     if (p != k)
-      for (int j = 0; j < N; ++j) { double t = M[N * k + j]; M[N * k + j] = M[N * p + j]; M[N * p + j] = t; }
-    double r = rcp(M[N * k + k]);                  // reciprocal pivots: one reciprocal per pivot
+      for (int j = 0; j < N; ++j) { R t = M[N * k + j]; M[N * k + j] = M[N * p + j]; M[N * p + j] = t; }
+    R r = rcp(M[N * k + k]);                       // reciprocal pivots: one reciprocal per pivot
     rp[k] = r;
     for (int i = k + 1; i < N; ++i) {
-      double l = M[N * i + k] * r;
+      R l = M[N * i + k] * r;
       M[N * i + k] = l;
-      for (int j = k + 1; j < N; ++j) M[N * i + j] = fma(-l, M[N * k + j], M[N * i + j]);
+      for (int j = k + 1; j < N; ++j) M[N * i + j] = fmx(-l, M[N * k + j], M[N * i + j]);
     }
   }
   return true;
 }
 // x <- M^-1 x with the factors of lu_factor
-template <int N>
-__device__ __forceinline__ void lu_apply(const double (&M)[N * N], const int (&piv)[N], const double (&rp)[N], double* x) {
-  for (int k = 0; k < N; ++k) { int p = piv[k]; if (p != k) { double t = x[k]; x[k] = x[p]; x[p] = t; } }
-  for (int i = 1; i < N; ++i) { double s = x[i]; for (int j = 0; j < i; ++j) s = fma(-M[N * i + j], x[j], s); x[i] = s; }
+template <int N, typename R>
+__device__ __forceinline__ void lu_apply(const R (&M)[N * N], const int (&piv)[N], const R (&rp)[N], R* x) {
+  for (int k = 0; k < N; ++k) { int p = piv[k]; if (p != k) { R t = x[k]; x[k] = x[p]; x[p] = t; } }
+  for (int i = 1; i < N; ++i) { R s = x[i]; for (int j = 0; j < i; ++j) s = fmx(-M[N * i + j], x[j], s); x[i] = s; }
   for (int i = N - 1; i >= 0; --i) {
-    double s = x[i];
-    for (int j = i + 1; j < N; ++j) s = fma(-M[N * i + j], x[j], s);
+    R s = x[i];
+    for (int j = i + 1; j < N; ++j) s = fmx(-M[N * i + j], x[j], s);
     x[i] = s * rp[i];
   }
 }
 // LU with partial pivoting of an NxN row-major matrix M[r][c], solving M x = b in place
 // (one right-hand side).  Returns false for an exactly singular pivot.
-template <int N>
-__device__ __forceinline__ bool lu_solve(double (&M)[N * N], double* x) {
+template <int N, typename R>
+__device__ __forceinline__ bool lu_solve(R (&M)[N * N], R* x) {
   int piv[N];
-  double rp[N];
+  R rp[N];
   if (!lu_factor<N>(M, piv, rp)) return false;
   lu_apply<N>(M, piv, rp, x);
+  return true;
+}
+
+// One Newton direction of the Lp iteration: dLp = -J^-1 res.  Returns false for a
+// singular 6 x 6 system.  R is the arithmetic of the Jacobian: double in the plain
+// form; float in the mixed form, where A and Fe arrive rounded to FP32 and the
+// direction is widened back to FP64 (the residual, the update and the convergence
+// test stay FP64, so the iteration still converges to the FP64 fixed point; an
+// approximate Jacobian changes only the contraction rate, as the reference's own
+// lagged Jacobian update does).
+template <typename R>
+__device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, const R* Fe_, double dt,
+                                              const double* dg, const double* res, double* dLp) {
+  // Jacobian of R(Lp) = Lp - sum_a gdot_a(tau_a(Lp)) P_a, rows and columns in the
+  // order kl = 3k + l:
+  //   J(kl, pq) = delta + sum_r W(p, r) T_kl(r, q),  W = A^T Fe,
+  //   T_kl(r, q) = sum_a dt |dg_a| P_a(k, l) (C : P_a)(r, q)   (symmetric in r, q).
+  // With P_a = pval s_a (signs in {-1, 0, 1}, compile-time) and the cubic C : P_a
+  // (= (C11 - C12) P_a on the diagonal, C44 (P_a + P_a^T) off it), T_kl is a signed
+  // sum of cd_a = dt pval^2 (C11 - C12) |dg_a| (diagonal) and co_a = dt pval^2 C44
+  // |dg_a| (off-diagonal entries).  In the basis of symmetric matrices
+  // (00, 11, 22, 12, 02, 01) J = I + T^ B^ with T^ (9 x 6) the components of the T_kl
+  // and B^(s, pq) the coefficient of component s in (W T)(p, q).  J has rank-6
+  // structure, so the Newton step solves (Woodbury)
+  //   x = b - T^ u,  (I6 + B^ T^) u = B^ b,
+  // a 6 x 6 system instead of the 9 x 9 one; algebraically identical.
+  R W[9];
+  mtm(A, Fe_, W);
+  R cd[NSLIP], co[NSLIP];
+  {
+    const double cdt = dt * mp.pval * mp.pval * mp.ngdot0_p;      // dg carries prxi r^(n-1)
+    const R sd = (R)(cdt * mp.C11mC12), so = (R)(cdt * mp.C44);
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) { const R d = (R)dg[a]; cd[a] = sd * d; co[a] = so * d; }
+  }
+  R T[9][6];
+#pragma unroll
+  for (int kl = 0; kl < 8; ++kl) {
+    const int k = kl / 3, l = kl % 3;
+#pragma unroll
+    for (int sl = 0; sl < 6; ++sl) T[kl][sl] = R(-0.0);
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) {
+      if (fcc_s(a, k, l) == 0) continue;
+      const bool pos = fcc_s(a, k, l) > 0;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const int sg = fcc_s(a, r, r) * (pos ? 1 : -1);
+        if (sg > 0) T[kl][r] += cd[a];
+        else if (sg < 0) T[kl][r] -= cd[a];
+      }
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
+        const int sg = (fcc_s(a, r, q) + fcc_s(a, q, r)) * (pos ? 1 : -1);
+        if (sg > 0) T[kl][3 + m] += co[a];
+        else if (sg < 0) T[kl][3 + m] -= co[a];
+      }
+    }
+  }
+#pragma unroll
+  for (int sl = 0; sl < 6; ++sl) T[8][sl] = -T[0][sl] - T[4][sl];   // s_a(2,2) = -s_a(0,0) - s_a(1,1)
+  // B^ v for a vector v over pq (v(p, q) = v[3p + q]): component s of sum_pq B^(s, pq) v(p, q)
+  auto bhat = [&](const R* v, R* y) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) y[r] = W[3 * r] * v[r] + W[1 + 3 * r] * v[3 + r] + W[2 + 3 * r] * v[6 + r];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
+      R t = W[3 * r] * v[q];
+      t = fmx(W[1 + 3 * r], v[3 + q], t);
+      t = fmx(W[2 + 3 * r], v[6 + q], t);
+      t = fmx(W[3 * q], v[r], t);
+      t = fmx(W[1 + 3 * q], v[3 + r], t);
+      y[3 + m] = fmx(W[2 + 3 * q], v[6 + r], t);
+    }
+  };
+  R b9[9], u[6], G[36];
+#pragma unroll
+  for (int kl = 0; kl < 9; ++kl) b9[kl] = (R)res[kl / 3 + 3 * (kl % 3)];
+  bhat(b9, u);
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    R v[9], g[6];
+#pragma unroll
+    for (int kl = 0; kl < 9; ++kl) v[kl] = T[kl][t];
+    bhat(v, g);
+#pragma unroll
+    for (int sl = 0; sl < 6; ++sl) G[6 * sl + t] = sl == t ? R(1) + g[sl] : g[sl];
+  }
+  if (!lu_solve<6>(G, u)) return false;
+#pragma unroll
+  for (int kl = 0; kl < 8; ++kl) {
+    R x = b9[kl];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) x = fmx(-T[kl][t], u[t], x);
+    dLp[kl / 3 + 3 * (kl % 3)] = -(double)x;
+  }
+  dLp[8] = -dLp[0] - dLp[4];
+
   return true;
 }
 
 // integrateStress with Fi = I for fixed F and Fp0 (A = F Fp0^-1) and slip resistances
 // xi (prxi = pval / xi): the Lp Newton iteration.  Returns true if broken.  On success
 // writes S, Lp and the slip rates of S; Fp, Fe and P follow from stress_outputs().
+template <bool MX>
 __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt, const double* prxi, double* Lp,
                                  double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters) {
   double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
+  float Af[MX ? 9 : 1];
+  if constexpr (MX) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Af[k] = (float)A[k];
+  }
 #pragma unroll
   for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
   long long res_old_n = 0;
@@ -367,92 +517,16 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     if (jaco % mp.f_update_jacobi_Lp == 0) {
       ++jaco;
       (*jac_iters)++;
-      // Jacobian of R(Lp) = Lp - sum_a gdot_a(tau_a(Lp)) P_a, rows and columns in the
-      // order kl = 3k + l:
-      //   J(kl, pq) = delta + sum_r W(p, r) T_kl(r, q),  W = A^T Fe,
-      //   T_kl(r, q) = sum_a dt |dg_a| P_a(k, l) (C : P_a)(r, q)   (symmetric in r, q).
-      // With P_a = pval s_a (signs in {-1, 0, 1}, compile-time) and the cubic C : P_a
-      // (= (C11 - C12) P_a on the diagonal, C44 (P_a + P_a^T) off it), T_kl is a signed
-      // sum of cd_a = dt pval^2 (C11 - C12) |dg_a| (diagonal) and co_a = dt pval^2 C44
-      // |dg_a| (off-diagonal entries).  In the basis of symmetric matrices
-      // (00, 11, 22, 12, 02, 01) J = I + T^ B^ with T^ (9 x 6) the components of the T_kl
-      // and B^(s, pq) the coefficient of component s in (W T)(p, q).  J has rank-6
-      // structure, so the Newton step solves (Woodbury)
-      //   x = b - T^ u,  (I6 + B^ T^) u = B^ b,
-      // a 6 x 6 system instead of the 9 x 9 one; algebraically identical.
-      double W[9];
-      mtm(A, Fe_, W);
-      double cd[NSLIP], co[NSLIP];
-      {
-        const double cdt = dt * mp.pval * mp.pval * mp.ngdot0_p;      // dg carries prxi r^(n-1)
-        const double sd = cdt * mp.C11mC12, so = cdt * mp.C44;
+      bool ok;
+      if constexpr (MX) {
+        float Fef[9];
 #pragma unroll
-        for (int a = 0; a < NSLIP; ++a) { cd[a] = sd * dg[a]; co[a] = so * dg[a]; }
+        for (int k = 0; k < 9; ++k) Fef[k] = (float)Fe_[k];
+        ok = jacobian_step<float>(mp, Af, Fef, dt, dg, res, dLp);
+      } else {
+        ok = jacobian_step<double>(mp, A, Fe_, dt, dg, res, dLp);
       }
-      double T[9][6];
-#pragma unroll
-      for (int kl = 0; kl < 8; ++kl) {
-        const int k = kl / 3, l = kl % 3;
-#pragma unroll
-        for (int sl = 0; sl < 6; ++sl) T[kl][sl] = -0.0;
-#pragma unroll
-        for (int a = 0; a < NSLIP; ++a) {
-          if (fcc_s(a, k, l) == 0) continue;
-          const bool pos = fcc_s(a, k, l) > 0;
-#pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            const int sg = fcc_s(a, r, r) * (pos ? 1 : -1);
-            if (sg > 0) T[kl][r] += cd[a];
-            else if (sg < 0) T[kl][r] -= cd[a];
-          }
-#pragma unroll
-          for (int m = 0; m < 3; ++m) {
-            const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
-            const int sg = (fcc_s(a, r, q) + fcc_s(a, q, r)) * (pos ? 1 : -1);
-            if (sg > 0) T[kl][3 + m] += co[a];
-            else if (sg < 0) T[kl][3 + m] -= co[a];
-          }
-        }
-      }
-#pragma unroll
-      for (int sl = 0; sl < 6; ++sl) T[8][sl] = -T[0][sl] - T[4][sl];   // s_a(2,2) = -s_a(0,0) - s_a(1,1)
-      // B^ v for a vector v over pq (v(p, q) = v[3p + q]): component s of sum_pq B^(s, pq) v(p, q)
-      auto bhat = [&](const double* v, double* y) {
-#pragma unroll
-        for (int r = 0; r < 3; ++r) y[r] = W[3 * r] * v[r] + W[1 + 3 * r] * v[3 + r] + W[2 + 3 * r] * v[6 + r];
-#pragma unroll
-        for (int m = 0; m < 3; ++m) {
-          const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
-          double t = W[3 * r] * v[q];
-          t = fma(W[1 + 3 * r], v[3 + q], t);
-          t = fma(W[2 + 3 * r], v[6 + q], t);
-          t = fma(W[3 * q], v[r], t);
-          t = fma(W[1 + 3 * q], v[3 + r], t);
-          y[3 + m] = fma(W[2 + 3 * q], v[6 + r], t);
-        }
-      };
-      double b9[9], u[6], G[36];
-#pragma unroll
-      for (int kl = 0; kl < 9; ++kl) b9[kl] = res[kl / 3 + 3 * (kl % 3)];
-      bhat(b9, u);
-#pragma unroll
-      for (int t = 0; t < 6; ++t) {
-        double v[9], g[6];
-#pragma unroll
-        for (int kl = 0; kl < 9; ++kl) v[kl] = T[kl][t];
-        bhat(v, g);
-#pragma unroll
-        for (int sl = 0; sl < 6; ++sl) G[6 * sl + t] = sl == t ? 1.0 + g[sl] : g[sl];
-      }
-      if (!lu_solve<6>(G, u)) return true;
-#pragma unroll
-      for (int kl = 0; kl < 8; ++kl) {
-        double x = b9[kl];
-#pragma unroll
-        for (int t = 0; t < 6; ++t) x = fma(-T[kl][t], u[t], x);
-        dLp[kl / 3 + 3 * (kl % 3)] = -x;
-      }
-      dLp[8] = -dLp[0] - dLp[4];
+      if (!ok) return true;
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg[k]);
@@ -497,6 +571,7 @@ __device__ __forceinline__ double damper(const double* o0, const double* o1, con
 // integrateStateFPI; returns true if broken.  S on entry: stress used for the
 // first dot state (restored committed stress); state in/out.  F and Fp0 are fixed for
 // the whole iteration, so Fp0^-1 and F Fp0^-1 are formed once.
+template <bool MX>
 __device__ bool integrate_state(const MatParams& mp, const double* F, const double* Fp0, const double* state0,
                                 double dt, double* state, double* Lp, double* S, double* P, double* Fp,
                                 double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
@@ -508,7 +583,7 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
   mm(F, invFp0, A);
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
-  dot_state(mp, S, state, prxi, dot);
+  dot_state<MX>(mp, S, state, prxi, dot);
   {
     bool nan = false;
 #pragma unroll
@@ -524,9 +599,9 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
     (*fpi_iters)++;
-    broken = integrate_stress(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters);
+    broken = integrate_stress<MX>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters);
     if (broken) break;
-    dot_state(mp, S, state, prxi, dot, gdot);
+    dot_state<MX>(mp, S, state, prxi, dot, gdot);
     bool nan = false;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) nan |= nan_bits(dot[i]);
@@ -556,7 +631,7 @@ __device__ __forceinline__ double ldp(const double* p, int64_t ld, int c, int64_
 // Per-point constitutive response (restore, cut-back driver, FPI, P) of one tile of
 // BS points plus the partial sums of P (per 32 points, one warp) for P_av.  One thread
 // per point.
-template <int BS>
+template <int BS, bool MX>
 __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState& ps, const double* __restrict__ Fin,
                                           int64_t ldF, double dt, double* __restrict__ Ppart, int* __restrict__ ill,
                                           ConsCounters* cnt, int64_t tile) {
@@ -609,7 +684,7 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
       if (todo) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
-        converged = !integrate_state(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &jac_iters,
+        converged = !integrate_state<MX>(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &jac_iters,
                                      &st_iters, &fpi_iters);
       }
     }
@@ -658,11 +733,11 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
   }
 }
 
-template <int BS>
+template <int BS, bool MX>
 __global__ void __launch_bounds__(BS)
 k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int64_t ldF, double dt,
                double* __restrict__ Ppart, int* __restrict__ ill, ConsCounters* cnt) {
-  cons_tile<BS>(mp, ps, Fin, ldF, dt, Ppart, ill, cnt, blockIdx.x);
+  cons_tile<BS, MX>(mp, ps, Fin, ldF, dt, Ppart, ill, cnt, blockIdx.x);
 }
 
 // Batched form: the points of many RVEs (uneven sizes) in one persistent launch.
@@ -670,7 +745,7 @@ k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int6
 // queue (one atomic per tile) so that a few slow tiles do not idle the rest.  Every
 // tile is the same computation as in k_constitutive, so results do not depend on
 // which RVEs share the launch.
-template <int BS, int MINB>
+template <int BS, int MINB, bool MX>
 __global__ void __launch_bounds__(BS, MINB)
 k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitems, long long ntiles,
                      unsigned long long* __restrict__ queue, ConsCounters* cnt) {
@@ -691,7 +766,7 @@ k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitem
     __syncthreads();
     const long long t = s_tile;
     if (t >= ntiles) break;
-    cons_tile<BS>(mp, s_it.ps, s_it.F, s_it.ldF, s_it.dt, s_it.Ppart, s_it.ill, cnt, t - s_it.tile0);
+    cons_tile<BS, MX>(mp, s_it.ps, s_it.F, s_it.ldF, s_it.dt, s_it.Ppart, s_it.ill, cnt, t - s_it.tile0);
   }
 }
 
@@ -1021,38 +1096,45 @@ namespace dgx {
 // per 32 cells whatever the block size: ceil(n / 32) x 9 doubles
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
                          double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block) {
-  if (block == 32) {
-    k_constitutive<32><<<(int)((ps.n + 31) / 32), 32, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+  if (mp.mixed) {                                  // mixed form: one launch shape
+    k_constitutive<128, true><<<(int)((ps.n + 127) / 128), 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+  } else if (block == 32) {
+    k_constitutive<32, false><<<(int)((ps.n + 31) / 32), 32, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
   } else if (block == 64) {
-    k_constitutive<64><<<(int)((ps.n + 63) / 64), 64, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<64, false><<<(int)((ps.n + 63) / 64), 64, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
   } else if (block == 256) {
-    k_constitutive<256><<<(int)((ps.n + 255) / 256), 256, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<256, false><<<(int)((ps.n + 255) / 256), 256, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
   } else {
-    k_constitutive<128><<<(int)((ps.n + 127) / 128), 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<128, false><<<(int)((ps.n + 127) / 128), 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+  }
+}
+// the batched kernel of a launch variant and form
+template <bool MX>
+static void* cons_batch_fn(int variant) {
+  switch (variant) {
+    case 0: return (void*)k_constitutive_batch<64, 1, MX>;
+    case 2: return (void*)k_constitutive_batch<256, 1, MX>;
+    case 3: return (void*)k_constitutive_batch<128, 3, MX>;
+    case 4: return (void*)k_constitutive_batch<32, 1, MX>;
+    default: return (void*)k_constitutive_batch<128, 1, MX>;
   }
 }
 // persistent batched launch: grid = min(tiles, resident blocks); queue must be zero
 void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
                                unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int variant, int grid) {
-  switch (variant) {
-    case 0: k_constitutive_batch<64, 1><<<grid, 64, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
-    case 2: k_constitutive_batch<256, 1><<<grid, 256, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
-    case 3: k_constitutive_batch<128, 3><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
-    case 4: k_constitutive_batch<32, 1><<<grid, 32, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
-    default: k_constitutive_batch<128, 1><<<grid, 128, 0, st>>>(mp, items, nitems, ntiles, queue, cnt); break;
-  }
+  const int bs = cons_variant_bs(variant);
+  MatParams m = mp;
+  const ConsItem* it = items;
+  void* args[] = {&m, &it, &nitems, &ntiles, &queue, &cnt};
+  cudaLaunchKernel(mp.mixed ? cons_batch_fn<true>(variant) : cons_batch_fn<false>(variant), dim3(grid), dim3(bs), args,
+                   0, st);
 }
-int constitutive_batch_resident(int variant) {
+int constitutive_batch_resident(int variant, bool mixed) {
   int nb = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  switch (variant) {
-    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<64, 1>, 64, 0); break;
-    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<256, 1>, 256, 0); break;
-    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128, 3>, 128, 0); break;
-    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<32, 1>, 32, 0); break;
-    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_constitutive_batch<128, 1>, 128, 0); break;
-  }
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed ? cons_batch_fn<true>(variant) : cons_batch_fn<false>(variant),
+                                                cons_variant_bs(variant), 0);
   return std::max(1, nb) * std::max(1, sms);
 }
 void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st) {

@@ -43,6 +43,11 @@ struct MatParams {
   int N_iter_state_max, N_iter_Lp_max, f_update_jacobi_Lp;
   int n_int;                 // n if it is an integer in [1, 64], else -1
   int a_quarters;            // 4a if it is an integer in [1, 256], else -1
+  // mixed-precision constitutive form (numerics precision 1): the Lp Newton's residual,
+  // update and convergence test stay FP64; its Jacobian and the hardening rate are
+  // evaluated in FP32.  0 for the plain FP64 form.
+  int mixed;
+  float h0h_f[7];            // h0h in FP32 (hardening rate of the mixed form)
 };
 
 // Planes of the per-point constitutive state.  All pointers address component
@@ -123,7 +128,7 @@ __host__ __device__ constexpr int cons_variant_bs(int v) { return v == 0 ? 64 : 
 __host__ __device__ constexpr int cons_variant_minb(int v) { return v == 3 ? 3 : 1; }
 void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
                                unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int variant, int grid);
-int constitutive_batch_resident(int variant);
+int constitutive_batch_resident(int variant, bool mixed);
 void launch_pav_finish(const double* Ppart, int nblocks, double wgt, double* Pav, cudaStream_t st);
 void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st);
 void launch_tangent(const MatParams& mp, const PointState& ps, double dt, double* dPdF, int64_t ld_out,

@@ -363,6 +363,7 @@ MatParams make_params(const dgx_material& m) {
   p.eps_rel_Lp2 = m.eps_rel_Lp * m.eps_rel_Lp; p.eps_abs_Lp2 = m.eps_abs_Lp * m.eps_abs_Lp;
   double aq = 4.0 * m.a;
   p.a_quarters = (aq == std::floor(aq) && aq >= 1 && aq <= 256) ? (int)aq : -1;
+  for (int t = 0; t < 7; ++t) p.h0h_f[t] = (float)p.h0h[t];
   return p;
 }
 
@@ -658,6 +659,12 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
   r->wgt = std::pow((double)r->N, -1.0);
   r->mat = *mat; r->num = *num;
   r->mp = make_params(*mat);
+  // the mixed form also evaluates the Lp Jacobian and the hardening rate in FP32;
+  // DGX_MIXED_CONS=0 keeps the FP64 constitutive kernel under FP32 spectra (A/B runs)
+  {
+    const char* mc = getenv("DGX_MIXED_CONS");
+    r->mp.mixed = (num->precision == 1 && !(mc && mc[0] == '0')) ? 1 : 0;
+  }
   // the kernels fold the cF Schmid sparsity at compile time: the host table must agree
   for (int a = 0; a < 12; ++a)
     for (int k = 0; k < 3; ++k)

@@ -156,6 +156,29 @@ def test_mixed_precision_error_bound(gpu):
         assert rel(rb["P_av"], ra["P_av"]) < 1e-5
 
 
+def test_mixed_constitutive_fields(gpu):
+    """The mixed form (FP32 spectra, FP32 Lp Jacobian and hardening rate; FP64 residual,
+    updates, convergence tests and tangent) against the FP64 form: tension then simple
+    shear, volume averages per increment and the fields P, F_p, xi at the end within
+    1e-5 relative."""
+    from solver_cpp_gb300.synthetic import microstructure
+    cells = (16, 16, 16)
+    mat_at, q = microstructure(cells, 20, seed=77)
+    steps = [gpu.load_step("tensionX", t=4.0, N=4), gpu.load_step("shearXY", t=4.0, N=4)]
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        r = gpu.RVE(cells, (1.0, 1.0, 1.0), mat_at, q, num=gpu.numerics(precision=prec))
+        recs = r.loop_over_loadcase(steps)
+        runs[prec] = (recs, {k: r.get(k) for k in ("P", "Fp", "xi")})
+    (ra, fa), (rb, fb) = runs["fp64"], runs["mixed"]
+    assert len(ra) == len(rb) == 8
+    for x, y in zip(ra, rb):
+        assert rel(y["P_av"], x["P_av"]) < 1e-5
+        assert rel(y["F_av"], x["F_av"]) < 1e-5
+    for k in fa:
+        assert rel(fb[k], fa[k]) < 1e-5, k
+
+
 def test_field_reads_into_caller_buffers(gpu):
     """dgx_get transposes on the device and copies into the caller's memory: the fields
     read into a given buffer equal a fresh read, for 9- and 12-component fields, and a
