@@ -548,20 +548,39 @@ def gpu_arm(a):
                 r2 = g.RVE(cells, size, mat_at, q, num=g.numerics(precision=prec))
                 st2 = torch.cuda.ExternalStream(r2.stream)
                 run_increments(r2, step, 0, a.warmup, a.increments)
-                c0 = r2.counters()
+                c0, tm0 = r2.counters(), r2.timers()
                 e0.record(st2)
                 out = []
                 run_increments(r2, step, a.warmup, a.steps, a.increments, records=out)
                 e1.record(st2)
                 torch.cuda.synchronize()
-                vals[prec] = n * (r2.counters()["evaluations"] - c0["evaluations"]) / (e0.elapsed_time(e1) * 1e-3)
+                c1, tm1 = r2.counters(), r2.timers()
+                vals[prec] = n * (c1["evaluations"] - c0["evaluations"]) / (e0.elapsed_time(e1) * 1e-3)
                 recs[prec] = out
+                if prec == "mixed":
+                    kms_m = tm1["constitutive_ms"] - tm0["constitutive_ms"]
+                    nl_m = max(1, tm1["constitutive_launches"] - tm0["constitutive_launches"])
+                    f64, f32 = g.flop_model_mixed()
+                    units = {"lp": c1["lp_iterations"] - c0["lp_iterations"],
+                             "jacobian": c1["jacobians"] - c0["jacobians"],
+                             "state": c1["state_iterations"] - c0["state_iterations"],
+                             "fpi": c1["fpi_iterations"] - c0["fpi_iterations"]}
+                    fl64 = sum(f64[k] * v for k, v in units.items())
+                    fl32 = sum(f32[k] * v for k, v in units.items())
+                    ach = fl64 / (kms_m * 1e-3) / 1e12 if kms_m > 0 else 0.0
+                    mixed_roof = {"bound": "fp64", "kernel": "k_constitutive (mixed form)",
+                                  "ms_per_launch": kms_m / nl_m, "achieved": ach, "peak": peak.value,
+                                  "unit": "TFLOP/s", "frac": ach / peak.value if peak.value else None,
+                                  "fp64_flops_per_launch": fl64 / nl_m, "fp32_flops_per_launch": fl32 / nl_m,
+                                  "kernel_time_share": kms_m / e0.elapsed_time(e1),
+                                  "spectral_ms_per_residual": (tm1["spectral_ms"] - tm0["spectral_ms"]) /
+                                  max(1, tm1["spectral_launches"] - tm0["spectral_launches"])}
                 r2.close()
             errs = [float(abs(b["P_av"] - a_["P_av"]).max() / abs(a_["P_av"]).max())
                     for a_, b in zip(recs["fp64"], recs["mixed"])]
             line["mixed"] = {"value": vals["mixed"], "unit": UNIT, "fp64_same_run": vals["fp64"],
                              "increments": a.steps, "max_rel_P_av_error_vs_fp64": max(errs),
-                             "per_increment_error": errs,
+                             "per_increment_error": errs, "roofline": mixed_roof,
                              "note": "FP32 FFT / Gamma with FP64 accumulation; Lp Newton Jacobian and hardening rate in FP32 (residual, update, convergence tests, tangent FP64); timed like value"}
         if a.batch_rves > 0:
             line["batched"] = batch_leg(g, torch, a.batch_rves, 20, a.batch_seconds, a.batch_compare)

@@ -197,6 +197,10 @@ dgx_status dgx_counters(const dgx_rve* rve, int64_t out[10]);
  * [1] Jacobian, [2] state integration, [3] fixed-point iteration.  No reference
  * counterpart; the numerator of the kernel's roofline. */
 void dgx_flop_model(double out[4]);
+/* The same for the mixed-precision constitutive form (numerics precision 1), split
+ * into the FP64 flops (fp64) and the FP32 flops (fp32) per counted unit.  No reference
+ * counterpart. */
+void dgx_flop_model_mixed(double fp64[4], double fp32[4]);
 /* CUDA-event time (ms, accumulated) and launch counts of [0] the constitutive
  * kernel, [1] the spectral chain (FFT + Gamma + div-RMS), [2] the tangent kernel,
  * measured on the RVE's stream. */

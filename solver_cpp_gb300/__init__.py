@@ -336,6 +336,16 @@ def flop_model():
     return dict(lp=a[0], jacobian=a[1], state=a[2], fpi=a[3])
 
 
+def flop_model_mixed():
+    """FP64 and FP32 flops per counted unit of the mixed-precision constitutive form
+    (dgx_flop_model_mixed): ({lp, jacobian, state, fpi} FP64, the same FP32)."""
+    a = (C.c_double * 4)()
+    b = (C.c_double * 4)()
+    _d.lib().dgx_flop_model_mixed(a, b)
+    keys = ("lp", "jacobian", "state", "fpi")
+    return dict(zip(keys, a)), dict(zip(keys, b))
+
+
 def footprint(cells, num=None, n_materials=1):
     """Device bytes an RVE of this grid and numerics holds (dgx_rve_footprint)."""
     b = C.c_int64(0)

@@ -18,6 +18,7 @@
 // Schmid signs of the cF slip systems are folded in at compile time; all of it is
 // algebraically identical to the reference's contractions.
 #include <algorithm>
+#include <type_traits>
 
 #include "../../include/dgx.h"
 #include "dgx_internal.cuh"
@@ -123,6 +124,22 @@ __device__ __forceinline__ double pow_nm1(double x, const MatParams& mp) {
   }
   return pow(x, mp.n - 1.0);
 }
+// x^n (the mixed form's slip rate: x^20 = x^16 x^4, five multiplies)
+__device__ __forceinline__ double pow_n(double x, const MatParams& mp) {
+  if (mp.n_int == 20) {
+    double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8;
+    return x16 * x4;
+  }
+  return x * pow_nm1(x, mp);
+}
+// x^(n-1) in FP32 (the mixed form's Jacobian)
+__device__ __forceinline__ float pow_nm1_f(float x, const MatParams& mp) {
+  if (mp.n_int == 20) {
+    float x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8;
+    return x16 * (x2 * x);
+  }
+  return powf(x, (float)mp.n - 1.0f);
+}
 __device__ __forceinline__ double pow_a(double y, const MatParams& mp) {
   if (mp.a_quarters == 9 && y > 1e-30) {
     // y^(9/4) = y^2 y^(1/4) (the configurations' a = 2.25): y^(-1/4) from an FP32
@@ -181,6 +198,43 @@ __device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, d
   S[1] = S[3] = mp.C44 * E01;
 }
 
+// The four cF slip-plane normals of the system table (unnormalised, three systems per
+// plane, plane p = a / 3): n_0 = (1,1,1), n_1 = (-1,-1,1), n_2 = (1,-1,-1), n_3 = (-1,1,-1).
+// The butterflies below depend on this order.
+static_assert(fcc_n(0, 0) == 1 && fcc_n(0, 1) == 1 && fcc_n(0, 2) == 1 && fcc_n(3, 0) == -1 && fcc_n(3, 1) == -1 &&
+              fcc_n(3, 2) == 1 && fcc_n(6, 0) == 1 && fcc_n(6, 1) == -1 && fcc_n(6, 2) == -1 && fcc_n(9, 0) == -1 &&
+              fcc_n(9, 1) == 1 && fcc_n(9, 2) == -1, "cF plane normals");
+
+// Mixed form: resolved shear tau_a = S : P_a = pval t_a with t_a = d_a . (S n_p)
+// (S symmetric).  The four products S n_p share partial sums: for row i with a = S(i,0), b = S(i,1),
+// c = S(i,2) and u = a + b, v = a - b, (S n_0)_i = u + c, (S n_1)_i = c - u,
+// (S n_2)_i = v - c, (S n_3)_i = -(v + c) (18 additions for all four); each t_a then adds
+// the two non-zero components of its direction (compile-time signs, one addition).
+__device__ __forceinline__ void resolved_shear(const double* S, double* t) {
+  double Sn[4][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double a = S[i], b = S[i + 3], c = S[i + 6];
+    const double u = a + b, v = a - b;
+    Sn[0][i] = u + c;
+    Sn[1][i] = c - u;
+    Sn[2][i] = v - c;
+    Sn[3][i] = v + c;                          // -(S n_3)_i: the sign is folded below
+  }
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) {
+    const int p = a / 3, sg = p == 3 ? -1 : 1;
+    double s = -0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int d = fcc_d(a, k) * sg;
+      if (d > 0) s += Sn[p][k];
+      else if (d < 0) s -= Sn[p][k];
+    }
+    t[a] = s;
+  }
+}
+
 // resolved shear, slip rates and |d gdot / d tau| on the 12 systems (Mp = S).
 // tau = S : P_a = pval t with t the signed sum of S's components of the system's sign
 // pattern (compile time; S symmetric).  Division free: with prxi = pval / xi and
@@ -190,7 +244,7 @@ __device__ __forceinline__ void hooke_S(const MatParams& mp, const double* Fe, d
 // r^n sign(tau) (= gdot / gdot0) and dg receives prxi r^(n-1).
 // Accumulators start at -0.0 (the additive identity) so the first term is free.
 __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, const double* prxi,
-                                         double* gdot, double* dg) {
+                                         double* gdot, double* dg, double* pnm1 = nullptr) {
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
     double t = -0.0;
@@ -212,18 +266,13 @@ __device__ __forceinline__ void kinetics(const MatParams& mp, const double* S, c
     const double p = pow_nm1(r, mp);         // r^(n-1)
     gdot[a] = copysign(r * p, t);
     if (dg) dg[a] = prxi[a] * p;
+    if (pnm1) pnm1[a] = p;
   }
 }
 
 // phenopowerlaw dotState: [dot xi (12), |gdot| (12)]
 // gdot: the slip rates of S in units of gdot0 if already known (the last Lp iteration
-// evaluated them for the same S and xi), else null.
-// MX (mixed form): the hardening rate dot xi_a = h0 sign(x)|x|^a sum_b h_ab |gdot_b|,
-// x = 1 - xi_a / xi_inf, is evaluated in FP32 from x and the slip rates formed in FP64
-// (the state itself, its update and the convergence test stay FP64: an FP32 rate
-// perturbs dot xi dt by ~1e-7 of itself, far below the state tolerance).  A rate of
-// magnitude 1e37 or more, or NaN, sends the point's dot state to the FP64 form.
-template <bool MX>
+// evaluated them for the same S and xi), else null
 __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, const double* xi, const double* prxi,
                                           double* dot, const double* gdot = nullptr) {
   double g[NSLIP];
@@ -235,33 +284,6 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
   }
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) g[a] = fabs(g[a]);
-  if constexpr (MX) {
-    float gf[NSLIP];
-#pragma unroll
-    for (int a = 0; a < NSLIP; ++a) gf[a] = (float)g[a];
-    bool in_range = true;
-#pragma unroll
-    for (int a = 0; a < NSLIP; ++a) {
-      const float x = (float)fma(-xi[a], mp.rxi_inf, 1.0);
-      const float y = fabsf(x);
-      float pa;
-      if (mp.a_quarters == 9) pa = (y * y) * sqrtf(sqrtf(y));   // y^(9/4)
-      else pa = powf(y, (float)mp.a);
-      float gt[7];
-#pragma unroll
-      for (int t = 0; t < 7; ++t) gt[t] = -0.0f;
-#pragma unroll
-      for (int b = 0; b < NSLIP; ++b) gt[cf_interaction(a, b) - 1] += gf[b];
-      float hs = mp.h0h_f[0] * gt[0];
-#pragma unroll
-      for (int t = 1; t < 7; ++t) hs = fmaf(mp.h0h_f[t], gt[t], hs);
-      const float d = copysignf(pa, x) * hs;
-      in_range &= fabsf(d) < 1e37f;                // false for NaN and overflow
-      dot[a] = (double)d;
-      dot[NSLIP + a] = mp.gdot0 * g[a];
-    }
-    if (in_range) return;
-  }
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
     double x = 1.0 - xi[a] * mp.rxi_inf;
@@ -279,6 +301,67 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
     for (int t = 1; t < 7; ++t) hs = fma(mp.h0h[t], gt[t], hs);
     dot[a] = left * hs;
     dot[NSLIP + a] = mp.gdot0 * g[a];
+  }
+}
+
+// Mixed form: |slip rates| (units of gdot0) of S in FP32, for the predictor's dot state
+// (the first rate of a state integration, which only seeds the fixed-point iteration)
+__device__ __forceinline__ void kinetics_abs_f(const MatParams& mp, const double* S, const double* prxi, float* g) {
+  float Sf[9];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) Sf[4 * k] = (float)S[4 * k];
+  Sf[7] = (float)S[7]; Sf[6] = (float)S[6]; Sf[3] = (float)S[3];   // S symmetric: (1,2), (0,2), (0,1)
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) {
+    float t = -0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (fcc_s(a, k, k) > 0) t += Sf[4 * k];
+      else if (fcc_s(a, k, k) < 0) t -= Sf[4 * k];
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const int r = m == 0 ? 1 : 0, q = m == 2 ? 1 : 2;
+      const int sg = fcc_s(a, r, q) + fcc_s(a, q, r);
+      if (sg == 1) t += Sf[r + 3 * q];
+      else if (sg == -1) t -= Sf[r + 3 * q];
+      else if (sg == 2) t = fmaf(2.0f, Sf[r + 3 * q], t);
+      else if (sg == -2) t = fmaf(-2.0f, Sf[r + 3 * q], t);
+    }
+    const float r = fabsf(t) * (float)prxi[a];
+    float p;
+    if (mp.n_int == 20) {
+      const float r2 = r * r, r4 = r2 * r2, r8 = r4 * r4, r16 = r8 * r8;
+      p = r16 * (r2 * r);
+    } else {
+      p = powf(r, (float)mp.n - 1.0f);
+    }
+    g[a] = r * p;
+  }
+}
+
+// Mixed form of dotState: dot xi_a = h0 sign(x)|x|^a sum_b h_ab |gdot_b| (x = 1 - xi_a /
+// xi_inf formed in FP64, then FP32) and |gdot_a|, in FP32 from the |slip rates| gabs
+// (units of gdot0).  The state, its update and the convergence test stay FP64; an FP32
+// rate perturbs an increment dot dt by ~1e-7 of itself, far below the state tolerance.
+__device__ __forceinline__ void dot_state_f(const MatParams& mp, const double* xi, const float* gabs, float* dot) {
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) {
+    const float x = (float)fma(-xi[a], mp.rxi_inf, 1.0);
+    const float y = fabsf(x);
+    float pa;
+    if (mp.a_quarters == 9) pa = (y * y) * sqrtf(sqrtf(y));   // y^(9/4)
+    else pa = powf(y, (float)mp.a);
+    float gt[7];
+#pragma unroll
+    for (int t = 0; t < 7; ++t) gt[t] = -0.0f;
+#pragma unroll
+    for (int b = 0; b < NSLIP; ++b) gt[cf_interaction(a, b) - 1] += gabs[b];
+    float hs = mp.h0h_f[0] * gt[0];
+#pragma unroll
+    for (int t = 1; t < 7; ++t) hs = fmaf(mp.h0h_f[t], gt[t], hs);
+    dot[a] = copysignf(pa, x) * hs;
+    dot[NSLIP + a] = mp.gdot0_f * gabs[a];
   }
 }
 
@@ -330,6 +413,57 @@ __device__ __forceinline__ bool lu_solve(R (&M)[N * N], R* x) {
   return true;
 }
 
+// lu_solve with every index known at compile time (loops unrolled, the pivot row
+// exchange done by predicated swaps), so that the matrix stays in registers: the same
+// pivots and the same arithmetic as lu_solve.
+template <int N, typename R>
+__device__ __forceinline__ bool lu_solve_unrolled(R (&M)[N * N], R* x) {
+  R rp[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    auto mx = absbits(M[N * k + k]);
+    int p = k;
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const auto v = absbits(M[N * i + k]);
+      if (v > mx) { mx = v; p = i; }
+    }
+    if (mx == 0) return false;
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      if (p == i) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) { R t = M[N * k + j]; M[N * k + j] = M[N * i + j]; M[N * i + j] = t; }
+        R t = x[k]; x[k] = x[i]; x[i] = t;
+      }
+    }
+    R r = rcp(M[N * k + k]);
+    rp[k] = r;
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      R l = M[N * i + k] * r;
+      M[N * i + k] = l;
+#pragma unroll
+      for (int j = k + 1; j < N; ++j) M[N * i + j] = fmx(-l, M[N * k + j], M[N * i + j]);
+    }
+  }
+#pragma unroll
+  for (int i = 1; i < N; ++i) {
+    R s = x[i];
+#pragma unroll
+    for (int j = 0; j < i; ++j) s = fmx(-M[N * i + j], x[j], s);
+    x[i] = s;
+  }
+#pragma unroll
+  for (int i = N - 1; i >= 0; --i) {
+    R s = x[i];
+#pragma unroll
+    for (int j = i + 1; j < N; ++j) s = fmx(-M[N * i + j], x[j], s);
+    x[i] = s * rp[i];
+  }
+  return true;
+}
+
 // One Newton direction of the Lp iteration: dLp = -J^-1 res.  Returns false for a
 // singular 6 x 6 system.  R is the arithmetic of the Jacobian: double in the plain
 // form; float in the mixed form, where A and Fe arrive rounded to FP32 and the
@@ -339,7 +473,7 @@ __device__ __forceinline__ bool lu_solve(R (&M)[N * N], R* x) {
 // lagged Jacobian update does).
 template <typename R>
 __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, const R* Fe_, double dt,
-                                              const double* dg, const double* res, double* dLp) {
+                                              const R* dg, const double* res, double* dLp) {
   // Jacobian of R(Lp) = Lp - sum_a gdot_a(tau_a(Lp)) P_a, rows and columns in the
   // order kl = 3k + l:
   //   J(kl, pq) = delta + sum_r W(p, r) T_kl(r, q),  W = A^T Fe,
@@ -417,7 +551,11 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
 #pragma unroll
     for (int sl = 0; sl < 6; ++sl) G[6 * sl + t] = sl == t ? R(1) + g[sl] : g[sl];
   }
-  if (!lu_solve<6>(G, u)) return false;
+  if constexpr (std::is_same<R, float>::value) {
+    if (!lu_solve_unrolled<6>(G, u)) return false;
+  } else {
+    if (!lu_solve<6>(G, u)) return false;
+  }
 #pragma unroll
   for (int kl = 0; kl < 8; ++kl) {
     R x = b9[kl];
@@ -437,10 +575,12 @@ template <bool MX>
 __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt, const double* prxi, double* Lp,
                                  double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters) {
   double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
-  float Af[MX ? 9 : 1];
+  float Af[MX ? 9 : 1], prxi_f[MX ? NSLIP : 1];
   if constexpr (MX) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) Af[k] = (float)A[k];
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) prxi_f[a] = (float)prxi[a];
   }
 #pragma unroll
   for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
@@ -454,11 +594,26 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     for (int k = 0; k < 9; ++k) B[k] = ((k % 4) == 0 ? 1.0 : 0.0) - dt * Lpg[k];
     mm(A, B, Fe_);
     hooke_S(mp, Fe_, S);
-    double gdot[NSLIP], dg[NSLIP];
-    kinetics(mp, S, prxi, gdot, dg);
-    // Lp = pval sum_a gdot_a d_a (x) n_a with the cF signs folded at compile time: the
-    // three systems of a slip plane share n, so the plane sums Y_p = sum_a gdot_a d_a
-    // come first, then Lp(k, l) = pval gdot0 sum_p n_p(l) Y_p(k) (gdot in units of gdot0)
+    // slip rates (units of gdot0) and what the Jacobian needs of them: plain form
+    // r^(n-1) (dg = prxi r^(n-1) is formed with the Jacobian), mixed form r in FP32
+    using KT = typename std::conditional<MX, float, double>::type;
+    double gdot[NSLIP];
+    KT kaux[NSLIP];
+    if constexpr (MX) {
+      double t[NSLIP];
+      resolved_shear(S, t);
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) {
+        const double r = fabs(t[a]) * prxi[a];
+        gdot[a] = copysign(pow_n(r, mp), t[a]);
+        kaux[a] = (float)r;
+      }
+    } else {
+      kinetics(mp, S, prxi, gdot, nullptr, kaux);
+    }
+    // Lp = pval gdot0 sum_a gdot_a d_a (x) n_a (gdot in units of gdot0) with the cF signs
+    // folded at compile time: the three systems of a slip plane share n, so the plane
+    // sums Y_p = sum_a gdot_a d_a come first, then L(k, l) = sum_p n_p(l) Y_p(k)
     double Y[4][3];
 #pragma unroll
     for (int p = 0; p < 4; ++p)
@@ -471,27 +626,45 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
           else if (fcc_d(3 * p + j, k) < 0) Y[p][k] -= gdot[3 * p + j];
         }
       }
-    double Lpc[9];
+    double res[9], Lpc[9];
+    double nLg2 = 0.0, nLc2 = 0.0, nr2 = 0.0;
+    if constexpr (MX) {
+      // butterfly over the four normals: with D = Y_0 - Y_1, E = Y_2 - Y_3,
+      // L(k, 0) = D + E, L(k, 1) = D - E, L(k, 2) = (Y_0 + Y_1) - (Y_2 + Y_3); the
+      // factor pval gdot0 folded into the residual (one FMA per entry) and the norm
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int l = 0; l < 3; ++l) {
-        double s = -0.0;
-#pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          if (fcc_n(3 * p, l) > 0) s += Y[p][k];
-          else s -= Y[p][k];
-        }
-        Lpc[k + 3 * l] = mp.pgdot0 * s;
+      for (int k = 0; k < 3; ++k) {
+        const double D = Y[0][k] - Y[1][k], E = Y[2][k] - Y[3][k];
+        Lpc[k] = D + E;
+        Lpc[k + 3] = D - E;
+        Lpc[k + 6] = (Y[0][k] + Y[1][k]) - (Y[2][k] + Y[3][k]);
       }
-    double res[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) res[k] = Lpg[k] - Lpc[k];
+      for (int k = 0; k < 9; ++k) res[k] = fma(-mp.pgdot0, Lpc[k], Lpg[k]);
+      double nL2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nL2 = fma(Lpc[k], Lpc[k], nL2); nr2 = fma(res[k], res[k], nr2); }
+      nLc2 = mp.pgdot0_sq * nL2;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          double sm = -0.0;
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            if (fcc_n(3 * p, l) > 0) sm += Y[p][k];
+            else sm -= Y[p][k];
+          }
+          Lpc[k + 3 * l] = mp.pgdot0 * sm;
+        }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) res[k] = Lpg[k] - Lpc[k];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nLc2 = fma(Lpc[k], Lpc[k], nLc2); nr2 = fma(res[k], res[k], nr2); }
+    }
     // convergence tests on squared norms (no square roots); the norms are non-negative
     // and, past the NaN test, not NaN, so they compare exactly as integers
-    double nLg2 = 0.0, nLc2 = 0.0, nr2 = 0.0;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nLc2 = fma(Lpc[k], Lpc[k], nLc2); nr2 = fma(res[k], res[k], nr2); }
     if (nan_bits(nr2)) return true;
     const long long nr2b = absbits(nr2);
     const long long atol2 = max(absbits(mp.eps_rel_Lp2 * __longlong_as_double(max(absbits(nLg2), absbits(nLc2)))),
@@ -518,6 +691,12 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       ++jaco;
       (*jac_iters)++;
       bool ok;
+      KT dg[NSLIP];                             // |dgdot/dtau| up to the factor n gdot0 / pval
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) {
+        if constexpr (MX) dg[a] = prxi_f[a] * pow_nm1_f(kaux[a], mp);
+        else dg[a] = prxi[a] * kaux[a];
+      }
       if constexpr (MX) {
         float Fef[9];
 #pragma unroll
@@ -557,16 +736,20 @@ __device__ bool stress_outputs(const double* F, const double* invFp0, double dt,
   return false;
 }
 
-__device__ __forceinline__ double damper(const double* o0, const double* o1, const double* o2) {
-  double d12 = 0.0, d22 = 0.0, d01 = 0.0;
+template <typename R>
+__device__ __forceinline__ R damper(const R* o0, const R* o1, const R* o2) {
+  R d12 = R(0), d22 = R(0), d01 = R(0);
 #pragma unroll
   for (int i = 0; i < 2 * NSLIP; ++i) {
-    double a = o0[i] - o1[i], b = o1[i] - o2[i];
-    d12 = fma(a, b, d12); d22 = fma(b, b, d22); d01 = fma(o0[i], o1[i], d01);
+    R a = o0[i] - o1[i], b = o1[i] - o2[i];
+    d12 = fmx(a, b, d12); d22 = fmx(b, b, d22); d01 = fmx(o0[i], o1[i], d01);
   }
-  if (fmin(d01, d12) < 0.0 && d22 > 0.0) return 0.75 + 0.25 * tanh(2.0 + 4.0 * d12 * rcp(d22));
-  return 1.0;
+  if (fmin(d01, d12) < R(0) && d22 > R(0)) return R(0.75) + R(0.25) * tanh(R(2) + R(4) * d12 * rcp(d22));
+  return R(1);
 }
+// true for NaN (plain form) or for any non-finite value (mixed form, FP32 rates)
+__device__ __forceinline__ bool bad_rate(double x) { return nan_bits(x); }
+__device__ __forceinline__ bool bad_rate(float x) { return absbits(x) >= 0x7f800000; }
 
 // integrateStateFPI; returns true if broken.  S on entry: stress used for the
 // first dot state (restored committed stress); state in/out.  F and Fp0 are fixed for
@@ -576,42 +759,58 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
                                 double dt, double* state, double* Lp, double* S, double* P, double* Fp,
                                 double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
                                 unsigned* fpi_iters) {
-  double dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP], prxi[NSLIP], gdot[NSLIP];
+  // rates and their history: FP64 in the plain form, FP32 in the mixed form
+  using DT = typename std::conditional<MX, float, double>::type;
+  DT dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
+  double prxi[NSLIP], gdot[NSLIP];
   (*st_iters)++;
   double invFp0[9], A[9];
   if (!inv33(Fp0, invFp0)) return true;
   mm(F, invFp0, A);
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
-  dot_state<MX>(mp, S, state, prxi, dot);
+  if constexpr (MX) {
+    float gf[NSLIP];
+    kinetics_abs_f(mp, S, prxi, gf);
+    dot_state_f(mp, state, gf, dot);
+  } else {
+    dot_state(mp, S, state, prxi, dot);
+  }
   {
     bool nan = false;
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) nan |= nan_bits(dot[i]);
+    for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
     if (nan) return true;
   }
 #pragma unroll
-  for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(dot[i], dt, state0[i]);
+  for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma((double)dot[i], dt, state0[i]);
   bool broken = true;
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) { last2[i] = it > 1 ? last1[i] : 0.0; last1[i] = dot[i]; }
+    for (int i = 0; i < 2 * NSLIP; ++i) { last2[i] = it > 1 ? last1[i] : DT(0); last1[i] = dot[i]; }
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
     (*fpi_iters)++;
     broken = integrate_stress<MX>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters);
     if (broken) break;
-    dot_state<MX>(mp, S, state, prxi, dot, gdot);
+    if constexpr (MX) {
+      float gf[NSLIP];
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) gf[a] = (float)fabs(gdot[a]);
+      dot_state_f(mp, state, gf, dot);
+    } else {
+      dot_state(mp, S, state, prxi, dot, gdot);
+    }
     bool nan = false;
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) nan |= nan_bits(dot[i]);
+    for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
     if (nan) break;
-    double z = damper(dot, last1, last2);
+    const DT z = damper(dot, last1, last2);
     bool conv = true;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) {
-      double d = dot[i] * z + last1[i] * (1.0 - z);
-      double r = state[i] - state0[i] - d * dt;
+      const DT d = dot[i] * z + last1[i] * (DT(1) - z);
+      double r = state[i] - state0[i] - (double)d * dt;
       state[i] = state[i] - r;
       // |r| <= max(atol, eps |state|), compared exactly as integers (r and state are
       // not NaN here: a NaN dot state ended the iteration above)

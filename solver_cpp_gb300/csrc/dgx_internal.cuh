@@ -35,6 +35,7 @@ struct MatParams {
   double ngdot0, rxi_inf;      // n * gdot0, 1 / xi_inf
   double ngdot0_p;             // n * gdot0 / pval
   double pgdot0;               // pval * gdot0
+  double pgdot0_sq;            // (pval * gdot0)^2
   double pval;                 // magnitude of the non-zero Schmid entries (1/sqrt2 * 1/sqrt3)
   double atol_xi, atol_gamma;
   double r_cutback_min, r_cutback, r_increase, eps_rel_state;
@@ -48,6 +49,7 @@ struct MatParams {
   // evaluated in FP32.  0 for the plain FP64 form.
   int mixed;
   float h0h_f[7];            // h0h in FP32 (hardening rate of the mixed form)
+  float gdot0_f;             // gdot0 in FP32
 };
 
 // Planes of the per-point constitutive state.  All pointers address component
@@ -92,6 +94,16 @@ struct ConsCounters {
 // (pval/xi, hardening from the slip rates of the last Lp iteration summed per
 // interaction type, damper, state update: 755).
 constexpr double FLOPS_LP = 378.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS_FPI = 755.0;
+// The mixed form evaluates in FP32: the Jacobian step (all but the 5 FP64 multiplies
+// of its scale factors: 918 flops); in every dot state the hardening rate and the gamma
+// rate (FP64 31 flops per slip system -> FP32 24; x = 1 - xi / xi_inf stays FP64); the
+// predictor's slip rates (13 per system); the damper's three dot products (144) and
+// the blended rate (72).  Per counted unit:
+//   state: FP64 860 - 156 - 372 = 332, FP32 156 + 288 = 444
+//   fpi:   FP64 755 - 372 - 144 - 72 = 167, FP32 288 + 144 + 72 = 504
+constexpr double FLOPS_MX_JAC64 = 5.0, FLOPS_MX_JAC32 = FLOPS_JAC - FLOPS_MX_JAC64;
+constexpr double FLOPS_MX_STATE64 = 332.0, FLOPS_MX_STATE32 = 444.0;
+constexpr double FLOPS_MX_FPI64 = 167.0, FLOPS_MX_FPI32 = 504.0;
 
 // Stress boundary condition of one RVE's solve, resident on the device so that the
 // BC step of a residual evaluation (form_residual) needs no host round trip.

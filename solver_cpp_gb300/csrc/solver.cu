@@ -360,10 +360,12 @@ MatParams make_params(const dgx_material& m) {
   p.pval = std::fabs(p.P[0][1]);                       // (1/sqrt2)(1/sqrt3), as the host computed P
   p.ngdot0_p = p.ngdot0 / p.pval;
   p.pgdot0 = p.pval * m.dot_gamma_0;
+  p.pgdot0_sq = p.pgdot0 * p.pgdot0;
   p.eps_rel_Lp2 = m.eps_rel_Lp * m.eps_rel_Lp; p.eps_abs_Lp2 = m.eps_abs_Lp * m.eps_abs_Lp;
   double aq = 4.0 * m.a;
   p.a_quarters = (aq == std::floor(aq) && aq >= 1 && aq <= 256) ? (int)aq : -1;
   for (int t = 0; t < 7; ++t) p.h0h_f[t] = (float)p.h0h[t];
+  p.gdot0_f = (float)p.gdot0;
   return p;
 }
 
@@ -1051,4 +1053,11 @@ extern "C" dgx_status dgx_counters(const dgx_rve* r, int64_t out[10]) {
 extern "C" void dgx_flop_model(double out[4]) {
   if (!out) return;
   out[0] = FLOPS_LP; out[1] = FLOPS_JAC; out[2] = FLOPS_STATE; out[3] = FLOPS_FPI;
+}
+extern "C" void dgx_flop_model_mixed(double fp64[4], double fp32[4]) {
+  if (fp64) {
+    fp64[0] = FLOPS_LP; fp64[1] = FLOPS_MX_JAC64;
+    fp64[2] = FLOPS_MX_STATE64; fp64[3] = FLOPS_MX_FPI64;
+  }
+  if (fp32) { fp32[0] = 0.0; fp32[1] = FLOPS_MX_JAC32; fp32[2] = FLOPS_MX_STATE32; fp32[3] = FLOPS_MX_FPI32; }
 }

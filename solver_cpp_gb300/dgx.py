@@ -75,7 +75,8 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_batch_stats", "dgx_batch_stream", "dgx_rve_footprint", "dgx_server_create", "dgx_server_destroy",
            "dgx_server_submit", "dgx_server_poll", "dgx_server_release", "dgx_server_stats",
            "dgx_update_coords", "dgx_result_open", "dgx_result_add_setup", "dgx_result_write_increment",
-           "dgx_result_close", "dgx_restart_write", "dgx_restart_read", "dgx_run_loadcase_output", "dgx_batch_tuning", "dgx_flop_model", "dgx_batch_set_round_points",
+           "dgx_result_close", "dgx_restart_write", "dgx_restart_read", "dgx_run_loadcase_output", "dgx_batch_tuning", "dgx_flop_model", "dgx_flop_model_mixed",
+           "dgx_batch_set_round_points",
            "dgx_server_set_round_points", "dgx_device_math"]
 
 
@@ -141,6 +142,7 @@ def lib():
     L.dgx_batch_set_round_points.argtypes = [vp, C.c_int64]
     L.dgx_server_set_round_points.argtypes = [vp, C.c_int64]
     L.dgx_flop_model.restype = None
+    L.dgx_flop_model_mixed.argtypes = [dp, dp]
     L.dgx_result_open.argtypes = [C.c_char_p, vp, C.c_char_p, C.c_char_p, C.POINTER(vp)]
     L.dgx_result_add_setup.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int64]
     L.dgx_result_write_increment.argtypes = [vp, vp, C.c_int32, C.c_double]
@@ -163,7 +165,7 @@ def lib():
         f = getattr(L, name)
         if name not in ("dgx_material_default", "dgx_numerics_default", "dgx_rve_destroy", "dgx_last_error",
                         "dgx_rve_points", "dgx_rve_device_bytes", "dgx_rve_stream", "dgx_batch_destroy",
-                        "dgx_batch_stream", "dgx_server_destroy", "dgx_flop_model"):
+                        "dgx_batch_stream", "dgx_server_destroy", "dgx_flop_model", "dgx_flop_model_mixed"):
             f.restype = C.c_int32
     _lib = L
     return L
