@@ -196,6 +196,7 @@ struct Executor {
   int cons_trials[CONS_VARIANTS] = {}, cons_round = 0;
   ConsCounters cnt_last{};
   ConsCounters* h_cnt = nullptr;
+  double* h_tan = nullptr;                     // pinned: C_volAvg, C_minMaxAvg (162) per tangent request
   std::map<std::tuple<int, int, int, double, double, double, int, int, int>, SpecLaunch> spec_tuned;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // [4], [5]: a round's first and last copy
   double t_ms[3] = {0, 0, 0};
@@ -251,6 +252,7 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   EA(&e->d_bcout, &e->h_bcout, 10 * cap);
   EA(&e->d_queue, (unsigned long long**)nullptr, 16);
   EA((ConsCounters**)nullptr, &e->h_cnt, 1);
+  EA((double**)nullptr, &e->h_tan, 162 * (size_t)cap);
   if (cnt) e->cnt = cnt;
   else { EA(&e->cnt, (ConsCounters**)nullptr, 1); e->own_cnt = true; cudaMemset(e->cnt, 0, sizeof(ConsCounters)); }
 #undef EA
@@ -753,6 +755,10 @@ static dgx_status advance(Task& t) {
       case T_SUB_CHECK: {
         const dgx_loadstep* ls = t.cur_step();
         if (t.step_fraction < (int)std::pow(2, r->cut_back_level)) {
+          // forward needs the tangent of the converged state: requested from the next
+          // round (computed there beside the other members' work) instead of a
+          // synchronous launch of its own
+          if (!r->cut_back && !r->tangent_fresh) { t.want |= 4; return DGX_OK; }
           double t_remaining = ls->t + r->t_0 - r->t;
           r->t += r->dt;
           t.step_fraction++;
@@ -959,11 +965,26 @@ static double remaining_work(const Task& t) {
 // round), so none starves.  Requests of reductions alone are cheap and always served.
 // A task that fails is finished with its error; the others go on.
 static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks, int64_t point_budget) {
-  std::vector<Task*> res_tasks, served;
+  std::vector<Task*> res_tasks, served, tan_tasks;
   for (Task* t : tasks) {
     if (t->done() || t->want == 0) continue;
+    if (t->want & 4) { tan_tasks.push_back(t); served.push_back(t); continue; }   // tangent only
     if (t->want & 1) res_tasks.push_back(t);
     else served.push_back(t);                         // reductions only
+  }
+  // the requested tangents go first on the round's stream; their averages are read
+  // back with the round (pinned staging) and take effect after its synchronisation
+  for (size_t i = 0; i < tan_tasks.size(); ++i) {
+    dgx_rve* r = tan_tasks[i]->r;
+    if (r->timing) CK(cudaEventRecord(r->ev[4], e->st));
+    launch_tangent(r->mp, r->ps, r->tangent_dt, r->d_dPdF, r->N, r->d_tpart, e->st);
+    if (r->timing) CK(cudaEventRecord(r->ev[5], e->st));
+    launch_tangent_finish(r->d_tpart, r->nb_tan, r->wgt, r->d_Cvol, r->d_Cmm, e->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(e->h_tan + 162 * i, r->d_Cvol, 81 * sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    CK(cudaMemcpyAsync(e->h_tan + 162 * i + 81, r->d_Cmm, 81 * sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    r->n_launch += 2;
+    r->bytes_d2h += 162 * sizeof(double);
   }
   int64_t total = 0;
   for (Task* t : res_tasks) total += t->r->N;
@@ -984,6 +1005,20 @@ static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks, int64_t po
   std::vector<MultiReq> mq;
   for (Task* t : served) for (int i = 0; i < t->nmq; ++i) mq.push_back(t->mq[i]);
   TRY(ex_round(e, rq, mq));
+  if (!tan_tasks.empty()) {
+    CK(cudaStreamSynchronize(e->st));
+    for (size_t i = 0; i < tan_tasks.size(); ++i) {
+      dgx_rve* r = tan_tasks[i]->r;
+      memcpy(r->C_volAvg, e->h_tan + 162 * i, 81 * sizeof(double));
+      memcpy(r->C_minMaxAvg, e->h_tan + 162 * i + 81, 81 * sizeof(double));
+      r->n_tangent++;
+      r->tangent_fresh = true;
+      if (r->timing) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r->ev[4], r->ev[5]); r->t_ms[2] += ms; r->t_n[2]++;
+      }
+    }
+  }
   for (Task* t : served) {
     t->want = 0; t->nmq = 0;
     dgx_status s = advance(*t);

@@ -79,6 +79,36 @@ __device__ __forceinline__ float rcp(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
+// FP64 <-> FP32 conversions of the mixed form on the integer pipe.  On this part the
+// hardware conversions run on the FP64 unit at its rate (two per SM per clock, measured),
+// and the FP64 unit is what bounds the constitutive kernel; these take a few integer
+// instructions instead.  to_f32: round toward zero (relative error below 2^-23),
+// magnitudes beyond FP32 range -> inf, below its normal range -> signed zero, NaN ->
+// NaN.  to_f64: exact for normal FP32 values and zero (FP32 subnormals -> signed zero),
+// inf and NaN kept.
+__device__ __forceinline__ float to_f32(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned s = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;          // FP32 exponent field
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 mantissa bits
+  unsigned u = s | ((unsigned)e << 23) | m;
+  if (e <= 0) u = s;
+  else if (e >= 255) u = s | 0x7f800000u | ((e == 1151 && ((hi & 0xfffffu) | lo)) ? 0x400000u : 0u);
+  return __uint_as_float(u);
+}
+__device__ __forceinline__ double to_f64(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu, s = u & 0x80000000u;
+  unsigned hi = s | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu), lo = u << 29;
+  if (e == 0) { hi = s; lo = 0; }
+  else if (e == 255) hi = s | 0x7ff00000u | ((u >> 3) & 0xfffffu);
+  return __hiloint2double((int)hi, (int)lo);
+}
+template <typename R> __device__ __forceinline__ R to_R(double x);
+template <> __device__ __forceinline__ double to_R<double>(double x) { return x; }
+template <> __device__ __forceinline__ float to_R<float>(double x) { return to_f32(x); }
+__device__ __forceinline__ double to_f64(double x) { return x; }
+
 __device__ __forceinline__ double fmx(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fmx(float a, float b, float c) { return fmaf(a, b, c); }
 
@@ -309,8 +339,8 @@ __device__ __forceinline__ void dot_state(const MatParams& mp, const double* S, 
 __device__ __forceinline__ void kinetics_abs_f(const MatParams& mp, const double* S, const double* prxi, float* g) {
   float Sf[9];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) Sf[4 * k] = (float)S[4 * k];
-  Sf[7] = (float)S[7]; Sf[6] = (float)S[6]; Sf[3] = (float)S[3];   // S symmetric: (1,2), (0,2), (0,1)
+  for (int k = 0; k < 3; ++k) Sf[4 * k] = to_f32(S[4 * k]);
+  Sf[7] = to_f32(S[7]); Sf[6] = to_f32(S[6]); Sf[3] = to_f32(S[3]);   // S symmetric: (1,2), (0,2), (0,1)
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
     float t = -0.0f;
@@ -328,7 +358,7 @@ __device__ __forceinline__ void kinetics_abs_f(const MatParams& mp, const double
       else if (sg == 2) t = fmaf(2.0f, Sf[r + 3 * q], t);
       else if (sg == -2) t = fmaf(-2.0f, Sf[r + 3 * q], t);
     }
-    const float r = fabsf(t) * (float)prxi[a];
+    const float r = fabsf(t) * to_f32(prxi[a]);
     float p;
     if (mp.n_int == 20) {
       const float r2 = r * r, r4 = r2 * r2, r8 = r4 * r4, r16 = r8 * r8;
@@ -347,7 +377,7 @@ __device__ __forceinline__ void kinetics_abs_f(const MatParams& mp, const double
 __device__ __forceinline__ void dot_state_f(const MatParams& mp, const double* xi, const float* gabs, float* dot) {
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
-    const float x = (float)fma(-xi[a], mp.rxi_inf, 1.0);
+    const float x = to_f32(fma(-xi[a], mp.rxi_inf, 1.0));
     const float y = fabsf(x);
     float pa;
     if (mp.a_quarters == 9) pa = (y * y) * sqrtf(sqrtf(y));   // y^(9/4)
@@ -492,9 +522,9 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
   R cd[NSLIP], co[NSLIP];
   {
     const double cdt = dt * mp.pval * mp.pval * mp.ngdot0_p;      // dg carries prxi r^(n-1)
-    const R sd = (R)(cdt * mp.C11mC12), so = (R)(cdt * mp.C44);
+    const R sd = to_R<R>(cdt * mp.C11mC12), so = to_R<R>(cdt * mp.C44);
 #pragma unroll
-    for (int a = 0; a < NSLIP; ++a) { const R d = (R)dg[a]; cd[a] = sd * d; co[a] = so * d; }
+    for (int a = 0; a < NSLIP; ++a) { const R d = dg[a]; cd[a] = sd * d; co[a] = so * d; }
   }
   R T[9][6];
 #pragma unroll
@@ -540,7 +570,7 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
   };
   R b9[9], u[6], G[36];
 #pragma unroll
-  for (int kl = 0; kl < 9; ++kl) b9[kl] = (R)res[kl / 3 + 3 * (kl % 3)];
+  for (int kl = 0; kl < 9; ++kl) b9[kl] = to_R<R>(res[kl / 3 + 3 * (kl % 3)]);
   bhat(b9, u);
 #pragma unroll
   for (int t = 0; t < 6; ++t) {
@@ -561,7 +591,7 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
     R x = b9[kl];
 #pragma unroll
     for (int t = 0; t < 6; ++t) x = fmx(-T[kl][t], u[t], x);
-    dLp[kl / 3 + 3 * (kl % 3)] = -(double)x;
+    dLp[kl / 3 + 3 * (kl % 3)] = -to_f64(x);
   }
   dLp[8] = -dLp[0] - dLp[4];
 
@@ -578,9 +608,9 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
   float Af[MX ? 9 : 1], prxi_f[MX ? NSLIP : 1];
   if constexpr (MX) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Af[k] = (float)A[k];
+    for (int k = 0; k < 9; ++k) Af[k] = to_f32(A[k]);
 #pragma unroll
-    for (int a = 0; a < NSLIP; ++a) prxi_f[a] = (float)prxi[a];
+    for (int a = 0; a < NSLIP; ++a) prxi_f[a] = to_f32(prxi[a]);
   }
 #pragma unroll
   for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
@@ -606,7 +636,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       for (int a = 0; a < NSLIP; ++a) {
         const double r = fabs(t[a]) * prxi[a];
         gdot[a] = copysign(pow_n(r, mp), t[a]);
-        kaux[a] = (float)r;
+        kaux[a] = to_f32(r);
       }
     } else {
       kinetics(mp, S, prxi, gdot, nullptr, kaux);
@@ -700,7 +730,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       if constexpr (MX) {
         float Fef[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Fef[k] = (float)Fe_[k];
+        for (int k = 0; k < 9; ++k) Fef[k] = to_f32(Fe_[k]);
         ok = jacobian_step<float>(mp, Af, Fef, dt, dg, res, dLp);
       } else {
         ok = jacobian_step<double>(mp, A, Fe_, dt, dg, res, dLp);
@@ -783,7 +813,7 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
     if (nan) return true;
   }
 #pragma unroll
-  for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma((double)dot[i], dt, state0[i]);
+  for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(to_f64(dot[i]), dt, state0[i]);
   bool broken = true;
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
 #pragma unroll
@@ -796,7 +826,7 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
     if constexpr (MX) {
       float gf[NSLIP];
 #pragma unroll
-      for (int a = 0; a < NSLIP; ++a) gf[a] = (float)fabs(gdot[a]);
+      for (int a = 0; a < NSLIP; ++a) gf[a] = to_f32(fabs(gdot[a]));
       dot_state_f(mp, state, gf, dot);
     } else {
       dot_state(mp, S, state, prxi, dot, gdot);
@@ -810,7 +840,7 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) {
       const DT d = dot[i] * z + last1[i] * (DT(1) - z);
-      double r = state[i] - state0[i] - (double)d * dt;
+      double r = state[i] - state0[i] - to_f64(d) * dt;
       state[i] = state[i] - r;
       // |r| <= max(atol, eps |state|), compared exactly as integers (r and state are
       // not NaN here: a NaN dot state ended the iteration above)
