@@ -572,6 +572,8 @@ def gpu_arm(a):
                                   "ms_per_launch": kms_m / nl_m, "achieved": ach, "peak": peak.value,
                                   "unit": "TFLOP/s", "frac": ach / peak.value if peak.value else None,
                                   "fp64_flops_per_launch": fl64 / nl_m, "fp32_flops_per_launch": fl32 / nl_m,
+                                  "units_per_evaluation": {k: v / max(1, n * (c1["evaluations"] - c0["evaluations"]))
+                                                           for k, v in units.items()},
                                   "kernel_time_share": kms_m / e0.elapsed_time(e1),
                                   "spectral_ms_per_residual": (tm1["spectral_ms"] - tm0["spectral_ms"]) /
                                   max(1, tm1["spectral_launches"] - tm0["spectral_launches"])}

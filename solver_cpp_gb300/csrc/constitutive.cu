@@ -108,6 +108,8 @@ template <typename R> __device__ __forceinline__ R to_R(double x);
 template <> __device__ __forceinline__ double to_R<double>(double x) { return x; }
 template <> __device__ __forceinline__ float to_R<float>(double x) { return to_f32(x); }
 __device__ __forceinline__ double to_f64(double x) { return x; }
+template <typename R> __device__ __forceinline__ R conv(double x) { return to_R<R>(x); }
+template <typename R> __device__ __forceinline__ R conv(float x) { return (R)x; }
 
 __device__ __forceinline__ double fmx(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fmx(float a, float b, float c) { return fmaf(a, b, c); }
@@ -501,9 +503,9 @@ __device__ __forceinline__ bool lu_solve_unrolled(R (&M)[N * N], R* x) {
 // test stay FP64, so the iteration still converges to the FP64 fixed point; an
 // approximate Jacobian changes only the contraction rate, as the reference's own
 // lagged Jacobian update does).
-template <typename R>
+template <typename R, typename RS>
 __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, const R* Fe_, double dt,
-                                              const R* dg, const double* res, double* dLp) {
+                                              const R* dg, const RS* res, double* dLp) {
   // Jacobian of R(Lp) = Lp - sum_a gdot_a(tau_a(Lp)) P_a, rows and columns in the
   // order kl = 3k + l:
   //   J(kl, pq) = delta + sum_r W(p, r) T_kl(r, q),  W = A^T Fe,
@@ -570,7 +572,7 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
   };
   R b9[9], u[6], G[36];
 #pragma unroll
-  for (int kl = 0; kl < 9; ++kl) b9[kl] = to_R<R>(res[kl / 3 + 3 * (kl % 3)]);
+  for (int kl = 0; kl < 9; ++kl) b9[kl] = conv<R>(res[kl / 3 + 3 * (kl % 3)]);
   bhat(b9, u);
 #pragma unroll
   for (int t = 0; t < 6; ++t) {
@@ -598,12 +600,53 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
   return true;
 }
 
+// Mixed form: L(k, l) = sum_a g_a s_a(k, l) (s_a = d_a (x) n_a, compile-time signs) through
+// the plane sums Y_p = sum over the plane's systems of g_a d_a and a butterfly over the
+// four plane normals: with D = Y_0 - Y_1, E = Y_2 - Y_3, L(k, 0) = D + E,
+// L(k, 1) = D - E, L(k, 2) = (Y_0 + Y_1) - (Y_2 + Y_3).  Column-major L[k + 3 l].
+template <typename T>
+__device__ __forceinline__ void plane_butterfly(const T* g, T* L) {
+  T Y[4][3];
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      Y[p][k] = T(-0.0);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        if (fcc_d(3 * p + j, k) > 0) Y[p][k] += g[3 * p + j];
+        else if (fcc_d(3 * p + j, k) < 0) Y[p][k] -= g[3 * p + j];
+      }
+    }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const T D = Y[0][k] - Y[1][k], E = Y[2][k] - Y[3][k];
+    L[k] = D + E;
+    L[k + 3] = D - E;
+    L[k + 6] = (Y[0][k] + Y[1][k]) - (Y[2][k] + Y[3][k]);
+  }
+}
+
+// Mixed form: what a first-order start of the next Lp Newton needs from the converged
+// one of the previous fixed-point pass (FP32): Fe, r = |tau| prxi, prxi and the slip
+// rates g there, and the state change of the xi half that followed (xi - xi').
+struct LpPredictor {
+  bool valid;
+  float Fe[9], r[NSLIP], prxi[NSLIP], g[NSLIP], dxi[NSLIP];
+};
+
 // integrateStress with Fi = I for fixed F and Fp0 (A = F Fp0^-1) and slip resistances
 // xi (prxi = pval / xi): the Lp Newton iteration.  Returns true if broken.  On success
 // writes S, Lp and the slip rates of S; Fp, Fe and P follow from stress_outputs().
+// Mixed form (pr not null): a converged previous pass of the same state integration
+// (pr->valid) gives the Newton a first-order start, Lp + J^-1 dLp_c with dLp_c the
+// change of Lp(S) from the new slip resistances, dg_a / dprxi_a = n g_a / prxi_a, and J
+// the FP32 Jacobian at the previous solution; on convergence the solution's data are
+// stored for the next pass.  The iteration from that start is the same FP64 Newton.
 template <bool MX>
 __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt, const double* prxi, double* Lp,
-                                 double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters) {
+                                 double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters,
+                                 LpPredictor* pr = nullptr) {
   double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
   float Af[MX ? 9 : 1], prxi_f[MX ? NSLIP : 1];
   if constexpr (MX) {
@@ -613,7 +656,35 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     for (int a = 0; a < NSLIP; ++a) prxi_f[a] = to_f32(prxi[a]);
   }
 #pragma unroll
-  for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
+  for (int k = 0; k < 9; ++k) Lpg[k] = Lp[k];
+  if constexpr (MX) {
+    if (pr && pr->valid) {
+      // u_a = n g_a rho_a, rho_a = prxi'_a / prxi_a - 1 = (xi_a - xi'_a) / xi'_a
+      float u[NSLIP], dg0[NSLIP], dLc[9], delta_[9];
+      double delta[9];
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) {
+        u[a] = mp.n_f * pr->g[a] * (pr->dxi[a] * (prxi_f[a] * mp.rpval_f));
+        dg0[a] = pr->prxi[a] * pow_nm1_f(pr->r[a], mp);
+      }
+      plane_butterfly(u, dLc);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) delta_[k] = -mp.pgdot0_f * dLc[k];      // R(Lp, xi') ~ -dLp_c
+      (*jac_iters)++;
+      if (jacobian_step<float, float>(mp, Af, pr->Fe, dt, dg0, delta_, delta)) {
+        bool finite = true;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) finite &= !nan_bits(delta[k]) && absbits(delta[k]) != 0x7ff0000000000000LL;
+        if (finite) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Lpg[k] += delta[k];
+        }
+      }
+      pr->valid = false;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
   long long res_old_n = 0;
   double step = 1.0;
   int jaco = 0;
@@ -644,31 +715,12 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     // Lp = pval gdot0 sum_a gdot_a d_a (x) n_a (gdot in units of gdot0) with the cF signs
     // folded at compile time: the three systems of a slip plane share n, so the plane
     // sums Y_p = sum_a gdot_a d_a come first, then L(k, l) = sum_p n_p(l) Y_p(k)
-    double Y[4][3];
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        Y[p][k] = -0.0;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          if (fcc_d(3 * p + j, k) > 0) Y[p][k] += gdot[3 * p + j];
-          else if (fcc_d(3 * p + j, k) < 0) Y[p][k] -= gdot[3 * p + j];
-        }
-      }
     double res[9], Lpc[9];
     double nLg2 = 0.0, nLc2 = 0.0, nr2 = 0.0;
     if constexpr (MX) {
-      // butterfly over the four normals: with D = Y_0 - Y_1, E = Y_2 - Y_3,
-      // L(k, 0) = D + E, L(k, 1) = D - E, L(k, 2) = (Y_0 + Y_1) - (Y_2 + Y_3); the
+      // plane sums and the butterfly over the four normals (plane_butterfly); the
       // factor pval gdot0 folded into the residual (one FMA per entry) and the norm
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const double D = Y[0][k] - Y[1][k], E = Y[2][k] - Y[3][k];
-        Lpc[k] = D + E;
-        Lpc[k + 3] = D - E;
-        Lpc[k + 6] = (Y[0][k] + Y[1][k]) - (Y[2][k] + Y[3][k]);
-      }
+      plane_butterfly(gdot, Lpc);
 #pragma unroll
       for (int k = 0; k < 9; ++k) res[k] = fma(-mp.pgdot0, Lpc[k], Lpg[k]);
       double nL2 = 0.0;
@@ -676,6 +728,18 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nL2 = fma(Lpc[k], Lpc[k], nL2); nr2 = fma(res[k], res[k], nr2); }
       nLc2 = mp.pgdot0_sq * nL2;
     } else {
+      double Y[4][3];
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          Y[p][k] = -0.0;
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            if (fcc_d(3 * p + j, k) > 0) Y[p][k] += gdot[3 * p + j];
+            else if (fcc_d(3 * p + j, k) < 0) Y[p][k] -= gdot[3 * p + j];
+          }
+        }
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -704,6 +768,17 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       for (int a = 0; a < NSLIP; ++a) gdot_out[a] = gdot[a];   // slip rates of the final S
 #pragma unroll
       for (int k = 0; k < 9; ++k) Lp[k] = Lpg[k];
+      if constexpr (MX) {
+        if (pr) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) pr->Fe[k] = to_f32(Fe_[k]);
+#pragma unroll
+          for (int a = 0; a < NSLIP; ++a) {
+            pr->r[a] = kaux[a]; pr->prxi[a] = prxi_f[a]; pr->g[a] = to_f32(gdot[a]);
+          }
+          pr->valid = true;
+        }
+      }
       return false;
     }
     if (it == 1 || nr2b < res_old_n) {
@@ -731,9 +806,9 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
         float Fef[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fef[k] = to_f32(Fe_[k]);
-        ok = jacobian_step<float>(mp, Af, Fef, dt, dg, res, dLp);
+        ok = jacobian_step<float, double>(mp, Af, Fef, dt, dg, res, dLp);
       } else {
-        ok = jacobian_step<double>(mp, A, Fe_, dt, dg, res, dLp);
+        ok = jacobian_step<double, double>(mp, A, Fe_, dt, dg, res, dLp);
       }
       if (!ok) return true;
     }
@@ -793,6 +868,8 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
   using DT = typename std::conditional<MX, float, double>::type;
   DT dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
   double prxi[NSLIP], gdot[NSLIP];
+  LpPredictor pred;                  // mixed form: start of the next pass's Lp Newton
+  pred.valid = false;
   (*st_iters)++;
   double invFp0[9], A[9];
   if (!inv33(Fp0, invFp0)) return true;
@@ -821,7 +898,7 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
     (*fpi_iters)++;
-    broken = integrate_stress<MX>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters);
+    broken = integrate_stress<MX>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters, MX ? &pred : nullptr);
     if (broken) break;
     if constexpr (MX) {
       float gf[NSLIP];
@@ -847,6 +924,9 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
       const long long atol = absbits(i < NSLIP ? mp.atol_xi : mp.atol_gamma);
       conv &= absbits(r) <= max(atol, absbits(mp.eps_rel_state * state[i]));
       dot[i] = d;
+      if constexpr (MX) {
+        if (i < NSLIP) pred.dxi[i] = to_f32(r);   // xi - xi' of this update
+      }
     }
     if (conv) { broken = false; break; }
   }

@@ -50,6 +50,7 @@ struct MatParams {
   int mixed;
   float h0h_f[7];            // h0h in FP32 (hardening rate of the mixed form)
   float gdot0_f;             // gdot0 in FP32
+  float n_f, rpval_f, pgdot0_f;   // n, 1 / pval, pval gdot0 in FP32
 };
 
 // Planes of the per-point constitutive state.  All pointers address component

@@ -366,6 +366,7 @@ MatParams make_params(const dgx_material& m) {
   p.a_quarters = (aq == std::floor(aq) && aq >= 1 && aq <= 256) ? (int)aq : -1;
   for (int t = 0; t < 7; ++t) p.h0h_f[t] = (float)p.h0h[t];
   p.gdot0_f = (float)p.gdot0;
+  p.n_f = (float)p.n; p.rpval_f = (float)(1.0 / p.pval); p.pgdot0_f = (float)p.pgdot0;
   return p;
 }
 
