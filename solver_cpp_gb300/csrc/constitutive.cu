@@ -600,6 +600,14 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
   return true;
 }
 
+// The mixed form's FP32 Newton direction as one out-of-line function shared by its two
+// call sites (the Newton step and the first-order start): one copy of the code keeps
+// the kernel's instruction footprint down.
+__device__ __noinline__ bool jacobian_step_f32(const MatParams& mp, const float* A, const float* Fe_, double dt,
+                                               const float* dg, const double* res, double* dLp) {
+  return jacobian_step<float, double>(mp, A, Fe_, dt, dg, res, dLp);
+}
+
 // Mixed form: L(k, l) = sum_a g_a s_a(k, l) (s_a = d_a (x) n_a, compile-time signs) through
 // the plane sums Y_p = sum over the plane's systems of g_a d_a and a butterfly over the
 // four plane normals: with D = Y_0 - Y_1, E = Y_2 - Y_3, L(k, 0) = D + E,
@@ -660,8 +668,8 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
   if constexpr (MX) {
     if (pr && pr->valid) {
       // u_a = n g_a rho_a, rho_a = prxi'_a / prxi_a - 1 = (xi_a - xi'_a) / xi'_a
-      float u[NSLIP], dg0[NSLIP], dLc[9], delta_[9];
-      double delta[9];
+      float u[NSLIP], dg0[NSLIP], dLc[9];
+      double delta_[9], delta[9];
 #pragma unroll
       for (int a = 0; a < NSLIP; ++a) {
         u[a] = mp.n_f * pr->g[a] * (pr->dxi[a] * (prxi_f[a] * mp.rpval_f));
@@ -669,9 +677,9 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       }
       plane_butterfly(u, dLc);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) delta_[k] = -mp.pgdot0_f * dLc[k];      // R(Lp, xi') ~ -dLp_c
+      for (int k = 0; k < 9; ++k) delta_[k] = to_f64(-mp.pgdot0_f * dLc[k]);   // R(Lp, xi') ~ -dLp_c
       (*jac_iters)++;
-      if (jacobian_step<float, float>(mp, Af, pr->Fe, dt, dg0, delta_, delta)) {
+      if (jacobian_step_f32(mp, Af, pr->Fe, dt, dg0, delta_, delta)) {
         bool finite = true;
 #pragma unroll
         for (int k = 0; k < 9; ++k) finite &= !nan_bits(delta[k]) && absbits(delta[k]) != 0x7ff0000000000000LL;
@@ -806,7 +814,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
         float Fef[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fef[k] = to_f32(Fe_[k]);
-        ok = jacobian_step<float, double>(mp, Af, Fef, dt, dg, res, dLp);
+        ok = jacobian_step_f32(mp, Af, Fef, dt, dg, res, dLp);
       } else {
         ok = jacobian_step<double, double>(mp, A, Fe_, dt, dg, res, dLp);
       }
