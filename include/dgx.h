@@ -311,7 +311,8 @@ dgx_status dgx_measure_fp64_peak(double* tflops, double* ms);
 /* The constitutive kernel's own device math on n host values (validation against the
  * CUDA library functions; no reference counterpart): fn 0 the Newton-Raphson
  * reciprocal 1/x, fn 1 x^(9/4) (slip-resistance saturation, a = 2.25), fn 2 x^19
- * (the power law's x^(n-1), n = 20). */
+ * (the power law's x^(n-1), n = 20), fn 3 the mixed form's FP64 -> FP32 -> FP64 round
+ * trip on the integer pipe (FP32 rounded toward zero, subnormals flushed). */
 dgx_status dgx_device_math(int32_t fn, int64_t n, const double* x, double* out);
 
 #ifdef __cplusplus

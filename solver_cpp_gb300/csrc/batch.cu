@@ -172,6 +172,8 @@ struct GraphEntry {
 };
 constexpr size_t GRAPH_CACHE = 16;
 
+constexpr int TUNE_TRIALS = 5;               // interleaved timed rounds per constitutive launch variant
+
 struct Executor {
   cudaStream_t st = nullptr;
   int cap = 0;                               // residual items per round; 2 cap reductions
@@ -187,12 +189,12 @@ struct Executor {
   bool own_cnt = false;
   int cons_variant = 1, resident = 0;          // launch variant (points per block, blocks per SM)
   // autotuner: the constitutive launch variant (points per block, blocks per SM),
-  // chosen online from the median cost per counted FP64 flop of three interleaved
+  // chosen online from the median cost per counted FP64 flop of five interleaved
   // rounds per variant, and per grid the FFT tile shape, timed on the first round's data
   // (results do not depend on either)
   bool tune_cons = true, tune_spec = true;
   int res_by_variant[2][CONS_VARIANTS] = {};   // [mixed form][variant]: resident blocks
-  double cons_cost[CONS_VARIANTS][3] = {};
+  double cons_cost[CONS_VARIANTS][5] = {};     // TUNE_TRIALS per variant
   int cons_trials[CONS_VARIANTS] = {}, cons_round = 0;
   ConsCounters cnt_last{};
   ConsCounters* h_cnt = nullptr;
@@ -571,7 +573,7 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
     });
     if (e->tune_cons) {
       cand = e->cons_round % CONS_VARIANTS;
-      if (e->cons_trials[cand] >= 3) cand = -1;
+      if (e->cons_trials[cand] >= TUNE_TRIALS) cand = -1;
     }
     p.variant = cand >= 0 ? cand : e->cons_variant;
     const int BS = cons_variant_bs(p.variant);
@@ -635,23 +637,30 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
     const float cons_ms = ms;
     cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[1] += ms; e->t_n[1]++;
     if (e->tune_cons) {
-      // cost per counted flop (the constitutive roofline's own flop model)
+      // cost per counted FP64 flop (the constitutive roofline's own flop model; the
+      // mixed form's FP64 model when every member of the round is mixed)
       const ConsCounters& c1 = *e->h_cnt;
-      double flops = FLOPS_LP * (double)(c1.lp_iters - e->cnt_last.lp_iters) +
-                     FLOPS_JAC * (double)(c1.jac_iters - e->cnt_last.jac_iters) +
-                     FLOPS_STATE * (double)(c1.state_iters - e->cnt_last.state_iters) +
-                     FLOPS_FPI * (double)(c1.fpi_iters - e->cnt_last.fpi_iters);
+      bool all_mixed = true;
+      for (int i = 0; i < n; ++i) all_mixed &= q[i].r->mp.mixed != 0;
+      const double f_lp = FLOPS_LP, f_jac = all_mixed ? FLOPS_MX_JAC64 : FLOPS_JAC,
+                   f_st = all_mixed ? FLOPS_MX_STATE64 : FLOPS_STATE, f_fpi = all_mixed ? FLOPS_MX_FPI64 : FLOPS_FPI;
+      double flops = f_lp * (double)(c1.lp_iters - e->cnt_last.lp_iters) +
+                     f_jac * (double)(c1.jac_iters - e->cnt_last.jac_iters) +
+                     f_st * (double)(c1.state_iters - e->cnt_last.state_iters) +
+                     f_fpi * (double)(c1.fpi_iters - e->cnt_last.fpi_iters);
       e->cnt_last = c1;
       if (cand >= 0 && flops > 0.0) e->cons_cost[cand][e->cons_trials[cand]++] = cons_ms / flops;
       e->cons_round++;
       bool all = true;
-      for (int k = 0; k < CONS_VARIANTS; ++k) all &= e->cons_trials[k] >= 3;
+      for (int k = 0; k < CONS_VARIANTS; ++k) all &= e->cons_trials[k] >= TUNE_TRIALS;
       if (all) {
-        // median of three interleaved trials per variant
+        // median of the interleaved trials per variant
         double med[CONS_VARIANTS];
         for (int k = 0; k < CONS_VARIANTS; ++k) {
-          double* c = e->cons_cost[k];
-          med[k] = std::max(std::min(c[0], c[1]), std::min(std::max(c[0], c[1]), c[2]));
+          double c[TUNE_TRIALS];
+          std::copy(e->cons_cost[k], e->cons_cost[k] + TUNE_TRIALS, c);
+          std::sort(c, c + TUNE_TRIALS);
+          med[k] = c[TUNE_TRIALS / 2];
         }
         int best = 0;
         for (int k = 1; k < CONS_VARIANTS; ++k) if (med[k] < med[best]) best = k;

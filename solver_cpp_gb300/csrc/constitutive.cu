@@ -1477,12 +1477,12 @@ __global__ void k_device_math(int fn, int64_t n, const double* __restrict__ x, d
   MatParams mp{};
   mp.n = 20.0; mp.n_int = 20; mp.a = 2.25; mp.a_quarters = 9;
   const double v = x[i];
-  out[i] = fn == 0 ? rcp(v) : fn == 1 ? pow_a(v, mp) : pow_nm1(v, mp);
+  out[i] = fn == 0 ? rcp(v) : fn == 1 ? pow_a(v, mp) : fn == 2 ? pow_nm1(v, mp) : to_f64(to_f32(v));
 }
 }  // namespace dgx
 
 extern "C" dgx_status dgx_device_math(int32_t fn, int64_t n, const double* x, double* out) {
-  if (fn < 0 || fn > 2 || n < 0 || (n > 0 && (!x || !out))) return DGX_ERR_ARG;
+  if (fn < 0 || fn > 3 || n < 0 || (n > 0 && (!x || !out))) return DGX_ERR_ARG;
   if (n == 0) return DGX_OK;
   double* d = nullptr;
   if (cudaMalloc(&d, 2 * sizeof(double) * (size_t)n) != cudaSuccess) return DGX_ERR_NOMEM;

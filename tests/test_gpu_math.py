@@ -1,6 +1,7 @@
 """The constitutive kernel's own device math (dgx_device_math) against IEEE results:
 the Newton-Raphson reciprocal within one ulp of the correctly rounded 1/x (exact where
-it falls back to the division), x^(9/4) and x^19 within a few ulps of numpy's power."""
+it falls back to the division), x^(9/4) and x^19 within a few ulps of numpy's power, and
+the mixed form's integer-pipe FP32 conversions bit-exact against a numpy restatement."""
 import ctypes as C
 
 import numpy as np
@@ -53,3 +54,27 @@ def test_powers(dm):
     p = dm(2, x)
     ref = x ** 19
     assert np.max(np.abs(p - ref) / np.maximum(ref, 1e-300)) < 1e-14
+
+
+def f32_toward_zero(x):
+    """FP64 -> FP32 rounded toward zero, FP32 subnormals flushed to signed zero, values
+    beyond FP32 range to signed inf, NaN kept (numpy restatement of the device's to_f32)."""
+    with np.errstate(over="ignore", invalid="ignore"):
+        f = x.astype(np.float32)
+        over = np.abs(f.astype(np.float64)) > np.abs(x)
+        f = np.where(over & np.isfinite(x), np.nextafter(f, np.float32(0)), f)
+        f = np.where(np.isfinite(x) & (np.abs(x) >= 2.0 ** 128), np.copysign(np.float32(np.inf), x), f)
+        f = np.where(np.abs(f) < np.finfo(np.float32).tiny, np.copysign(np.float32(0), x), f)
+    return f.astype(np.float64)
+
+
+def test_integer_pipe_conversions(dm):
+    rng = np.random.default_rng(7)
+    x = np.concatenate([rng.uniform(-2.0, 2.0, 20000), 10.0 ** rng.uniform(-37, 38, 20000),
+                        -(10.0 ** rng.uniform(-37, 38, 5000)), 2.0 ** np.arange(-126, 128.0),
+                        np.nextafter(2.0 ** np.arange(-126, 128.0), 0.0),
+                        [0.0, -0.0, 1e-40, -1e-45, 1e-300, 3.5e38, -1e39, 1e300, np.inf, -np.inf]])
+    got = dm(3, x)
+    ref = f32_toward_zero(x)
+    assert np.array_equal(got.view(np.int64), ref.view(np.int64))
+    assert np.isnan(dm(3, np.array([np.nan]))[0])
