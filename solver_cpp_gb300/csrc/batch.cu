@@ -594,6 +594,8 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
         ConsItem& it = e->h_cons[j];
         it.ps = r->ps; it.F = q[order[j]].in; it.ldF = r->N; it.dt = r->delta_t; it.wgt = r->wgt;
         it.Ppart = r->d_Ppart; it.ill = e->d_ill + j; it.tile0 = tiles;
+        it.warm = (r->mp.mixed && r->evals_in_step > 0) ? 1 : 0;
+        r->evals_in_step++;
         tiles += (r->N + BS - 1) / BS;
         r->n_eval++;
         r->tangent_dt = r->delta_t;

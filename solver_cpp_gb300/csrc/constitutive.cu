@@ -867,11 +867,15 @@ __device__ __forceinline__ bool bad_rate(float x) { return absbits(x) >= 0x7f800
 // integrateStateFPI; returns true if broken.  S on entry: stress used for the
 // first dot state (restored committed stress); state in/out.  F and Fp0 are fixed for
 // the whole iteration, so Fp0^-1 and F Fp0^-1 are formed once.
+// guess (mixed form, may be null): a state (planes of stride gld) that replaces the
+// explicit predictor state0 + dot(S) dt as the iteration's start, with the rate it
+// implies, (guess - state0) / dt, as the first rate of the damper's history.  The
+// fixed point and its FP64 test are unchanged.
 template <bool MX>
 __device__ bool integrate_state(const MatParams& mp, const double* F, const double* Fp0, const double* state0,
                                 double dt, double* state, double* Lp, double* S, double* P, double* Fp,
                                 double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
-                                unsigned* fpi_iters) {
+                                unsigned* fpi_iters, const double* guess = nullptr, int64_t gld = 0) {
   // rates and their history: FP64 in the plain form, FP32 in the mixed form
   using DT = typename std::conditional<MX, float, double>::type;
   DT dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
@@ -882,23 +886,41 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
   double invFp0[9], A[9];
   if (!inv33(Fp0, invFp0)) return true;
   mm(F, invFp0, A);
+  bool seeded = false;
+  if (MX && guess && dt > 0.0) {
+    // the guess seeds the iteration only if its slip resistances are positive and its
+    // implied rates finite; otherwise the explicit predictor below is used
+    const float rdt = to_f32(rcp(dt));
+    bool ok = true;
 #pragma unroll
-  for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
-  if constexpr (MX) {
-    float gf[NSLIP];
-    kinetics_abs_f(mp, S, prxi, gf);
-    dot_state_f(mp, state, gf, dot);
-  } else {
-    dot_state(mp, S, state, prxi, dot);
+    for (int i = 0; i < 2 * NSLIP; ++i) {
+      const double g = guess[i * gld];
+      dot[i] = (DT)to_f32(g - state0[i]) * (DT)rdt;
+      ok &= !bad_rate(dot[i]) && (i >= NSLIP || g > 0.0);
+    }
+    if (ok) {
+#pragma unroll
+      for (int i = 0; i < 2 * NSLIP; ++i) state[i] = guess[i * gld];
+      seeded = true;
+    }
   }
-  {
+  if (!seeded) {
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
+    if constexpr (MX) {
+      float gf[NSLIP];
+      kinetics_abs_f(mp, S, prxi, gf);
+      dot_state_f(mp, state, gf, dot);
+    } else {
+      dot_state(mp, S, state, prxi, dot);
+    }
     bool nan = false;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
     if (nan) return true;
-  }
 #pragma unroll
-  for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(to_f64(dot[i]), dt, state0[i]);
+    for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(to_f64(dot[i]), dt, state0[i]);
+  }
   bool broken = true;
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
 #pragma unroll
@@ -948,10 +970,12 @@ __device__ __forceinline__ double ldp(const double* p, int64_t ld, int c, int64_
 // Per-point constitutive response (restore, cut-back driver, FPI, P) of one tile of
 // BS points plus the partial sums of P (per 32 points, one warp) for P_av.  One thread
 // per point.
+// Mixed form with warm set: the state planes hold the converged state of the previous
+// evaluation in the same step, which seeds the state iteration of the full step.
 template <int BS, bool MX>
 __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState& ps, const double* __restrict__ Fin,
                                           int64_t ldF, double dt, double* __restrict__ Ppart, int* __restrict__ ill,
-                                          ConsCounters* cnt, int64_t tile) {
+                                          ConsCounters* cnt, int64_t tile, int warm = 0) {
   const int64_t e = tile * BS + threadIdx.x;
   double P[9];
   unsigned lp_iters = 0, st_iters = 0, jac_iters = 0, fpi_iters = 0;
@@ -1001,8 +1025,9 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
       if (todo) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
+        const double* guess = (MX && warm && passes == 1) ? ps.st + e : nullptr;
         converged = !integrate_state<MX>(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &jac_iters,
-                                     &st_iters, &fpi_iters);
+                                     &st_iters, &fpi_iters, guess, ps.ld);
       }
     }
     ok = converged;
@@ -1083,7 +1108,7 @@ k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitem
     __syncthreads();
     const long long t = s_tile;
     if (t >= ntiles) break;
-    cons_tile<BS, MX>(mp, s_it.ps, s_it.F, s_it.ldF, s_it.dt, s_it.Ppart, s_it.ill, cnt, t - s_it.tile0);
+    cons_tile<BS, MX>(mp, s_it.ps, s_it.F, s_it.ldF, s_it.dt, s_it.Ppart, s_it.ill, cnt, t - s_it.tile0, s_it.warm);
   }
 }
 

@@ -127,6 +127,8 @@ struct ConsItem {
   double* Ppart;             // ceil(n / 32) x 9 partial sums of P
   int* ill;                  // terminally-ill flag of this RVE
   long long tile0;           // first tile of this item in the launch
+  int warm;                  // mixed form: the state planes hold the previous evaluation of
+                             // the same step (its converged state seeds the state iteration)
 };
 
 // constitutive.cu launchers

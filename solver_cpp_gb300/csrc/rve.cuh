@@ -66,6 +66,7 @@ struct dgx_rve {
   int guess = 0, cur_step = -1;
   // counters
   int64_t n_eval = 0, n_tangent = 0, n_launch = 0;
+  int64_t evals_in_step = 0;   // constitutive evaluations since the last forward (commit or cut-back)
   // CUDA-event timers on the RVE stream: [0] constitutive kernel, [1] spectral chain, [2] tangent
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double t_ms[3] = {0, 0, 0};

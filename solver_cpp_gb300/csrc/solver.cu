@@ -889,6 +889,7 @@ extern "C" dgx_status dgx_solver_forward(dgx_rve* r, int32_t cutback, int32_t gu
   if (!r || !ls) return DGX_ERR_ARG;
   if (!r->initialized) { set_err("dgx_solver_forward before dgx_solver_init"); return DGX_ERR_STATE; }
   const int64_t N = r->N;
+  r->evals_in_step = 0;
   if (cutback) {
     memcpy(r->C_volAvg, r->C_volAvgLastInc, sizeof(r->C_volAvg));
     memcpy(r->C_minMaxAvg, r->C_minMaxAvgLastInc, sizeof(r->C_minMaxAvg));
