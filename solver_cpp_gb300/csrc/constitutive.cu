@@ -242,12 +242,13 @@ static_assert(fcc_n(0, 0) == 1 && fcc_n(0, 1) == 1 && fcc_n(0, 2) == 1 && fcc_n(
 // c = S(i,2) and u = a + b, v = a - b, (S n_0)_i = u + c, (S n_1)_i = c - u,
 // (S n_2)_i = v - c, (S n_3)_i = -(v + c) (18 additions for all four); each t_a then adds
 // the two non-zero components of its direction (compile-time signs, one addition).
-__device__ __forceinline__ void resolved_shear(const double* S, double* t) {
-  double Sn[4][3];
+template <typename T>
+__device__ __forceinline__ void resolved_shear(const T* S, T* t) {
+  T Sn[4][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const double a = S[i], b = S[i + 3], c = S[i + 6];
-    const double u = a + b, v = a - b;
+    const T a = S[i], b = S[i + 3], c = S[i + 6];
+    const T u = a + b, v = a - b;
     Sn[0][i] = u + c;
     Sn[1][i] = c - u;
     Sn[2][i] = v - c;
@@ -256,7 +257,7 @@ __device__ __forceinline__ void resolved_shear(const double* S, double* t) {
 #pragma unroll
   for (int a = 0; a < NSLIP; ++a) {
     const int p = a / 3, sg = p == 3 ? -1 : 1;
-    double s = -0.0;
+    T s = T(-0.0);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const int d = fcc_d(a, k) * sg;
@@ -638,9 +639,19 @@ __device__ __forceinline__ void plane_butterfly(const T* g, T* L) {
 // Mixed form: what a first-order start of the next Lp Newton needs from the converged
 // one of the previous fixed-point pass (FP32): Fe, r = |tau| prxi, prxi and the slip
 // rates g there, and the state change of the xi half that followed (xi - xi').
+// mode 2 (first pass of a warm evaluation): g holds the precomputed u_a of the change
+// of Lp(S) and dxi is unused.
 struct LpPredictor {
   bool valid;
+  int mode;                          // 1: change of the slip resistances, 2: u given
   float Fe[9], r[NSLIP], prxi[NSLIP], g[NSLIP], dxi[NSLIP];
+};
+
+// The previous evaluation of the same step (planes of stride ld at one cell): its
+// deformation gradient, elastic deformation gradient, stress and converged state.
+struct WarmPrev {
+  const double *F, *Fe, *S, *st;
+  int64_t ld;
 };
 
 // integrateStress with Fi = I for fixed F and Fp0 (A = F Fp0^-1) and slip resistances
@@ -672,7 +683,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       double delta_[9], delta[9];
 #pragma unroll
       for (int a = 0; a < NSLIP; ++a) {
-        u[a] = mp.n_f * pr->g[a] * (pr->dxi[a] * (prxi_f[a] * mp.rpval_f));
+        u[a] = pr->mode == 2 ? pr->g[a] : mp.n_f * pr->g[a] * (pr->dxi[a] * (prxi_f[a] * mp.rpval_f));
         dg0[a] = pr->prxi[a] * pow_nm1_f(pr->r[a], mp);
       }
       plane_butterfly(u, dLc);
@@ -785,6 +796,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
             pr->r[a] = kaux[a]; pr->prxi[a] = prxi_f[a]; pr->g[a] = to_f32(gdot[a]);
           }
           pr->valid = true;
+          pr->mode = 1;
         }
       }
       return false;
@@ -875,7 +887,7 @@ template <bool MX>
 __device__ bool integrate_state(const MatParams& mp, const double* F, const double* Fp0, const double* state0,
                                 double dt, double* state, double* Lp, double* S, double* P, double* Fp,
                                 double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
-                                unsigned* fpi_iters, const double* guess = nullptr, int64_t gld = 0) {
+                                unsigned* fpi_iters, const WarmPrev* wp = nullptr) {
   // rates and their history: FP64 in the plain form, FP32 in the mixed form
   using DT = typename std::conditional<MX, float, double>::type;
   DT dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
@@ -887,21 +899,81 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
   if (!inv33(Fp0, invFp0)) return true;
   mm(F, invFp0, A);
   bool seeded = false;
-  if (MX && guess && dt > 0.0) {
+  if (MX && wp && dt > 0.0) {
     // the guess seeds the iteration only if its slip resistances are positive and its
     // implied rates finite; otherwise the explicit predictor below is used
     const float rdt = to_f32(rcp(dt));
     bool ok = true;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) {
-      const double g = guess[i * gld];
+      const double g = wp->st[i * wp->ld];
       dot[i] = (DT)to_f32(g - state0[i]) * (DT)rdt;
       ok &= !bad_rate(dot[i]) && (i >= NSLIP || g > 0.0);
     }
     if (ok) {
 #pragma unroll
-      for (int i = 0; i < 2 * NSLIP; ++i) state[i] = guess[i * gld];
+      for (int i = 0; i < 2 * NSLIP; ++i) state[i] = wp->st[i * wp->ld];
       seeded = true;
+    }
+  }
+  if constexpr (MX) {
+    if (seeded) {
+      // first-order start of the first pass: the previous evaluation converged at Lp for
+      // F_prev and the same slip resistances, so R(Lp; F) ~ -dLp_c with dLp_c the change
+      // of Lp(S) from dF = F - F_prev: dFe = dF Fp0^-1 (I - dt Lp), 2 dE = Fe^T dFe +
+      // dFe^T Fe, dS = C : dE, dt_a = d_a . (dS n_a), u_a = n prxi r^(n-1) dt_a (FP32)
+      float M[9], dF[9], dFe[9], Fep[9], Sp[9], B[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        dF[k] = to_f32(F[k] - wp->F[k * wp->ld]);
+        Fep[k] = to_f32(wp->Fe[k * wp->ld]);
+        Sp[k] = to_f32(wp->S[k * wp->ld]);
+        B[k] = ((k % 4) == 0 ? 1.0f : 0.0f) - to_f32(dt) * to_f32(Lp[k]);
+        M[k] = to_f32(invFp0[k]);
+      }
+      float IB[9];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) IB[i + 3 * j] = M[i] * B[3 * j] + M[i + 3] * B[1 + 3 * j] + M[i + 6] * B[2 + 3 * j];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) dFe[i + 3 * j] = dF[i] * IB[3 * j] + dF[i + 3] * IB[1 + 3 * j] + dF[i + 6] * IB[2 + 3 * j];
+      // 2 dE (symmetric), then dS by the cubic Hooke law on 2 dE with the halved moduli
+      float E2[9];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i <= j; ++i) {
+          float v = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) v += Fep[k + 3 * i] * dFe[k + 3 * j] + dFe[k + 3 * i] * Fep[k + 3 * j];
+          E2[i + 3 * j] = v; E2[j + 3 * i] = v;
+        }
+      float dS[9];
+      const float ct = mp.hC12_f * (E2[0] + E2[4] + E2[8]);
+      dS[0] = fmaf(mp.hC11mC12_f, E2[0], ct);
+      dS[4] = fmaf(mp.hC11mC12_f, E2[4], ct);
+      dS[8] = fmaf(mp.hC11mC12_f, E2[8], ct);
+      dS[5] = dS[7] = mp.C44_f * E2[7];
+      dS[2] = dS[6] = mp.C44_f * E2[6];
+      dS[1] = dS[3] = mp.C44_f * E2[3];
+      float tp[NSLIP], dtt[NSLIP];
+      resolved_shear(Sp, tp);
+      resolved_shear(dS, dtt);
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) {
+        const float px = mp.pval_f * rcp(to_f32(state[a]));
+        const float r = fabsf(tp[a]) * px;
+        pred.r[a] = r;
+        pred.prxi[a] = px;
+        pred.g[a] = mp.n_f * px * pow_nm1_f(r, mp) * dtt[a];
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) pred.Fe[k] = Fep[k];
+      pred.mode = 2;
+      pred.valid = true;
     }
   }
   if (!seeded) {
@@ -1025,9 +1097,9 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
       if (todo) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
-        const double* guess = (MX && warm && passes == 1) ? ps.st + e : nullptr;
+        const WarmPrev wp{ps.F + e, ps.Fe + e, ps.S + e, ps.st + e, ps.ld};
         converged = !integrate_state<MX>(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &jac_iters,
-                                     &st_iters, &fpi_iters, guess, ps.ld);
+                                     &st_iters, &fpi_iters, (MX && warm && passes == 1) ? &wp : nullptr);
       }
     }
     ok = converged;

@@ -51,6 +51,7 @@ struct MatParams {
   float h0h_f[7];            // h0h in FP32 (hardening rate of the mixed form)
   float gdot0_f;             // gdot0 in FP32
   float n_f, rpval_f, pgdot0_f;   // n, 1 / pval, pval gdot0 in FP32
+  float pval_f, hC11mC12_f, hC12_f, C44_f;   // pval and the halved cubic moduli in FP32
 };
 
 // Planes of the per-point constitutive state.  All pointers address component

@@ -367,6 +367,7 @@ MatParams make_params(const dgx_material& m) {
   for (int t = 0; t < 7; ++t) p.h0h_f[t] = (float)p.h0h[t];
   p.gdot0_f = (float)p.gdot0;
   p.n_f = (float)p.n; p.rpval_f = (float)(1.0 / p.pval); p.pgdot0_f = (float)p.pgdot0;
+  p.pval_f = (float)p.pval; p.hC11mC12_f = (float)p.hC11mC12; p.hC12_f = (float)p.hC12; p.C44_f = (float)p.C44;
   return p;
 }
 
