@@ -103,6 +103,10 @@ constexpr double FLOPS_LP = 378.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS
 // the blended rate (72).  Per counted unit:
 //   state: FP64 860 - 156 - 372 = 332, FP32 156 + 288 = 444
 //   fpi:   FP64 755 - 372 - 144 - 72 = 167, FP32 288 + 144 + 72 = 504
+// A first-order Newton start counts as one Jacobian unit (its own right-hand side, at
+// most ~300 FP32 flops, is not counted), and a warm-started state integration still
+// counts the explicit predictor it skips (156 FP32 flops and 12 FP64 reciprocals), so
+// the mixed model counts cold evaluations exactly and warm ones approximately.
 constexpr double FLOPS_MX_JAC64 = 5.0, FLOPS_MX_JAC32 = FLOPS_JAC - FLOPS_MX_JAC64;
 constexpr double FLOPS_MX_STATE64 = 332.0, FLOPS_MX_STATE32 = 444.0;
 constexpr double FLOPS_MX_FPI64 = 167.0, FLOPS_MX_FPI32 = 504.0;
