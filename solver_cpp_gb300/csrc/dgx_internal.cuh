@@ -45,8 +45,10 @@ struct MatParams {
   int n_int;                 // n if it is an integer in [1, 64], else -1
   int a_quarters;            // 4a if it is an integer in [1, 256], else -1
   // mixed-precision constitutive form (numerics precision 1): the Lp Newton's residual,
-  // update and convergence test stay FP64; its Jacobian and the hardening rate are
-  // evaluated in FP32.  0 for the plain FP64 form.
+  // updates and convergence test, the state update and its test stay FP64; the Newton
+  // Jacobian, its first-order starts, the hardening and gamma rates and the damper are
+  // evaluated in FP32, and later evaluations of a step start from the previous one.
+  // 0 for the plain FP64 form.
   int mixed;
   float h0h_f[7];            // h0h in FP32 (hardening rate of the mixed form)
   float gdot0_f;             // gdot0 in FP32
