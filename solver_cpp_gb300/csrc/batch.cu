@@ -195,7 +195,7 @@ struct Executor {
   bool tune_cons = true, tune_spec = true;
   int res_by_variant[2][CONS_VARIANTS] = {};   // [mixed form][variant]: resident blocks
   double cons_cost[CONS_VARIANTS][5] = {};     // TUNE_TRIALS per variant
-  int cons_trials[CONS_VARIANTS] = {}, cons_round = 0;
+  int cons_trials[CONS_VARIANTS] = {}, cons_round = 0, tune_skipped = 0;
   ConsCounters cnt_last{};
   ConsCounters* h_cnt = nullptr;
   double* h_tan = nullptr;                     // pinned: C_volAvg, C_minMaxAvg (162) per tangent request
@@ -651,8 +651,17 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
                      f_st * (double)(c1.state_iters - e->cnt_last.state_iters) +
                      f_fpi * (double)(c1.fpi_iters - e->cnt_last.fpi_iters);
       e->cnt_last = c1;
-      if (cand >= 0 && flops > 0.0) e->cons_cost[cand][e->cons_trials[cand]++] = cons_ms / flops;
-      e->cons_round++;
+      // a mixed round is timed only when every member starts warm (the previous
+      // evaluation of its step seeds it): cold and warm evaluations differ in cost per
+      // counted flop, and nearly all of a solve's evaluations are warm (cold rounds are
+      // taken too once 200 rounds have passed without completing the trials)
+      bool all_warm = true;
+      for (int j = 0; j < n; ++j) all_warm &= e->h_cons[j].warm != 0;
+      const bool usable = !all_mixed || all_warm || ++e->tune_skipped > 200;
+      if (usable) {
+        if (cand >= 0 && flops > 0.0) e->cons_cost[cand][e->cons_trials[cand]++] = cons_ms / flops;
+        e->cons_round++;
+      }
       bool all = true;
       for (int k = 0; k < CONS_VARIANTS; ++k) all &= e->cons_trials[k] >= TUNE_TRIALS;
       if (all) {
