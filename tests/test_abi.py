@@ -35,3 +35,16 @@ def test_no_silent_fallback_without_gpu():
     import solver_cpp_gb300 as g
     with pytest.raises(g.DgxError):
         g.RVE((4, 4, 4), (1, 1, 1), np.zeros(64, int), [[1, 0, 0, 0]])
+
+
+def test_flop_models_are_consistent():
+    """The mixed form's flop model moves work from FP64 to FP32 and never adds FP64:
+    the Lp iteration is unchanged, the Jacobian's FP64 and FP32 parts add up to the
+    plain count, and every FP64 part is at most the plain one (host-only calls)."""
+    import solver_cpp_gb300 as g
+    plain = g.flop_model()
+    f64, f32 = g.flop_model_mixed()
+    assert f64["lp"] == plain["lp"] and f32["lp"] == 0.0
+    assert f64["jacobian"] + f32["jacobian"] == plain["jacobian"]
+    for k in plain:
+        assert 0.0 <= f64[k] <= plain[k] and f32[k] >= 0.0
