@@ -609,9 +609,36 @@ def gpu_arm(a):
                 line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": threads, "kind": "port",
                                         "sample": f"failed: {ex}"}
     if rank == 0:
+        ratios = north_star_ratios(line)
+        if ratios:
+            line["north_star_ratios"] = ratios
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def north_star_ratios(line):
+    """The mixed form against the plain FP64 form, from the legs of this run that
+    measured both: same workload (64^3 and, with --mixed-large, 128^3), the batched
+    population against the same RVEs one at a time in FP64, the served mix against the
+    same mix served in FP64.  A summary of values already in the line."""
+    r = {}
+    try:
+        m = line.get("mixed")
+        if m and m.get("fp64_same_run"):
+            r["mixed_vs_fp64_same_workload"] = m["value"] / m["fp64_same_run"]
+        m128 = line.get("mixed_128")
+        if m128 and m128.get("fp64", {}).get("value"):
+            r["mixed_vs_fp64_128cube"] = m128["mixed"]["value"] / m128["fp64"]["value"]
+        seq = (line.get("batched") or {}).get("vs_plain_fp64_sequential")
+        if seq:
+            r["batched_mixed_vs_fp64_one_at_a_time"] = seq["speedup"]
+        sv = {x["precision"]: x["value"] for x in line.get("serving") or [] if x.get("value")}
+        if "mixed" in sv and "fp64" in sv:
+            r["served_mixed_vs_served_fp64"] = sv["mixed"] / sv["fp64"]
+    except (KeyError, TypeError, ZeroDivisionError):
+        pass
+    return r
 
 
 def main():
