@@ -87,6 +87,15 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
 
 
+def max_over_ranks(ms, device):
+    """The timed region's milliseconds, maximum over all ranks: N independent replicas
+    finish when the slowest does, so the job's value is all ranks' units over this."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------- CPU oracle timing
 def oracle_increments(a, count, threads):
     """Run `count` increments of the workload on the CPU oracle (load case restarted
@@ -481,9 +490,7 @@ def gpu_arm(a):
     ms = e0.elapsed_time(e1)
     c1, t1 = rve.counters(), rve.timers()
     if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+        ms = max_over_ranks(ms, "cuda")
     evals = c1["evaluations"] - c0["evaluations"]
     value = n * evals * world / (ms * 1e-3)
     # roofline of the dominant kernel (constitutive, FP64-bound)
