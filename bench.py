@@ -56,15 +56,17 @@ def args_():
     p.add_argument("--increments", type=int, default=40)
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--no-extras", action="store_true", help="skip e2e / mixed / CPU-baseline legs")
-    p.add_argument("--cpu-sample-increments", type=int, default=1)
+    p.add_argument("--cpu-sample-increments", type=int, default=2,
+                   help="increments of the CPU oracle sample (also the mixed form's error against the oracle)")
     p.add_argument("--batch-rves", type=int, default=256, help="RVEs of the batched leg (0: skip)")
-    p.add_argument("--batch-seconds", type=float, default=20.0, help="time bound of the batched leg")
-    p.add_argument("--batch-compare", type=int, default=24, help="RVEs of the batched-vs-plain comparison")
-    p.add_argument("--mixed-large", action="store_true",
-                   help="also run the 128^3 / 1000-grain tension-then-shear mixed-precision configuration (~2 min)")
+    p.add_argument("--batch-seconds", type=float, default=300.0,
+                   help="safety bound of each batched run (runs end when every member is done)")
+    p.add_argument("--batch-compare", type=int, default=64, help="RVEs of the batched-vs-one-at-a-time comparison")
+    p.add_argument("--no-mixed-large", action="store_true",
+                   help="skip the 128^3 / 1000-grain tension-then-shear configuration (both forms, ~1 min)")
     p.add_argument("--serve-requests", type=int, default=12, help="requests of each serving leg (0: skip)")
-    p.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate (requests/s)")
-    p.add_argument("--serve-seconds", type=float, default=45.0, help="time bound of each serving leg")
+    p.add_argument("--serve-rates", default="5,20,50,200", help="Poisson arrival rates of the sweep (requests/s)")
+    p.add_argument("--serve-seconds", type=float, default=60.0, help="time bound of each serving leg")
     return p.parse_args()
 
 
@@ -117,6 +119,12 @@ def cpu_oracle_sample(a, increments, threads):
     dt = sum(r["seconds"] for r in recs)
     ev = sum(r["evaluations"] for r in recs)
     return n * ev / dt, dt, ev, recs
+
+
+def from_fortran9(v):
+    """reference (3,3) column-major 9 values -> 3x3 numpy [i][j]"""
+    import numpy as np
+    return np.asarray(v).reshape(3, 3).T
 
 
 def cpu_one_core_sample(a):
@@ -218,101 +226,121 @@ class Clocks:
 
 
 # ---------------------------------------------------------------- GPU arm
-BATCH_SIZES = (8, 16, 32, 48)
-BATCH_KINDS = ("tensionX", "tensionY", "tensionZ", "shearXY")
+BATCH_KINDS = ("tensionX", "tensionY", "tensionZ", "shearXY")   # as solver_cpp_gb300.synthetic
 
 
 def batch_population(count, seed=1000):
     """RVEs of the batched configuration: grid uniform in {8,16,32,48}^3, 8-200
     grains, load case uniform in tension x/y/z and shear xy (1e-3/s), per-RVE seeds."""
-    import numpy as np
     from solver_cpp_gb300 import synthetic
-    out = []
-    for k in range(count):
-        rng = np.random.default_rng(seed + k)
-        c = int(BATCH_SIZES[rng.integers(len(BATCH_SIZES))])
-        ng = int(rng.integers(8, 201))
-        kind = BATCH_KINDS[rng.integers(len(BATCH_KINDS))]
-        mat, q = synthetic.microstructure((c, c, c), ng, seed + k)
-        out.append(((c, c, c), ng, kind, mat, q))
-    return out
+    return synthetic.batch_population(count, seed)
 
 
-def batch_leg(g, torch, n_rves, increments, seconds, compare):
-    """Batched mixed-precision throughput on the batched configuration, and on a
-    subset the same RVEs solved one at a time in plain FP64 (throughput, P_av error)."""
-    pop = batch_population(n_rves)
-    mixed = g.numerics(precision="mixed")
+def _pct(v, p):
+    import numpy as np
+    return float(np.percentile(v, p)) if len(v) else None
+
+
+def _run_batch(g, torch, pop, precision, increments, seconds):
+    """One batch over the population in the given form, run until every member is done
+    (or `seconds` pass): CUDA-event time on the batch's stream, per-member completion
+    times (wall clock from the first round) and per-increment latencies."""
+    num = g.numerics(precision=precision)
     steps = {k: [g.load_step(k, t=float(increments), N=increments)] for k in BATCH_KINDS}
-    batch = g.Batch(n_rves)
+    batch = g.Batch(len(pop))
     rves = []
     for cells, ng, kind, mat, q in pop:
-        r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=mixed)
-        rves.append((r, batch.add(r, steps[kind]), kind))
+        r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=num)
+        rves.append((r, batch.add(r, steps[kind])))
     st = torch.cuda.ExternalStream(batch.stream)
     s0 = batch.stats()
     e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(st)
     t_start = time.perf_counter()
+    pending = {slot for _, slot in rves}
+    done_at = {}
     active = 1
     while active and time.perf_counter() - t_start < seconds:
         active = batch.step()
+        now = time.perf_counter() - t_start
+        for slot in list(pending):
+            if batch.member(slot)["done"]:
+                done_at[slot] = now
+                pending.discard(slot)
     e1.record(st)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     s1 = batch.stats()
-    pts = s1["point_evaluations"] - s0["point_evaluations"]
-    out = {"value": pts / (ms * 1e-3), "unit": UNIT, "rves": n_rves,
-           "points": int(sum(r.N for r, _, _ in rves)), "rounds": s1["rounds"] - s0["rounds"],
-           "seconds": ms * 1e-3, "all_done": not active,
+    inc_lat, recs = [], {}
+    for r, slot in rves:
+        recs[slot] = batch.records(slot)
+        inc_lat += [x["seconds"] for x in recs[slot]]
+    comp = sorted(done_at.values())
+    out = {"value": (s1["point_evaluations"] - s0["point_evaluations"]) / (ms * 1e-3), "unit": UNIT,
+           "precision": precision, "rves": len(pop), "points": int(sum(r.N for r, _ in rves)),
+           "increments": increments, "rounds": s1["rounds"] - s0["rounds"], "seconds": ms * 1e-3,
+           "all_done": not active, "completed": len(comp),
+           "p50_rve_completion_s": _pct(comp, 50), "p99_rve_completion_s": _pct(comp, 99),
+           "p50_increment_ms": 1e3 * _pct(inc_lat, 50) if inc_lat else None,
+           "p99_increment_ms": 1e3 * _pct(inc_lat, 99) if inc_lat else None,
            "constitutive_share": (s1["constitutive_ms"] - s0["constitutive_ms"]) / ms,
            "spectral_share": (s1["spectral_ms"] - s0["spectral_ms"]) / ms,
            "round_device_share": (s1["round_device_ms"] - s0["round_device_ms"]) / ms,
+           "graph_rounds": s1["graph_rounds"] - s0["graph_rounds"],
            "launches": s1["launches"] - s0["launches"], "autotuned": batch.tuning()}
     batch.close()
-    for r, _, _ in rves:
+    for r, _ in rves:
         r.close()
+    return out, [recs[slot] for _, slot in rves]
+
+
+def _max_err(recs_a, recs_b):
+    err = 0.0
+    for ra, rb in zip(recs_a, recs_b):
+        for a_, b_ in zip(ra, rb):
+            err = max(err, float(abs(a_["P_av"] - b_["P_av"]).max() / abs(b_["P_av"]).max()))
+    return err
+
+
+def batch_leg(g, torch, n_rves, increments, seconds, compare):
+    """The batched configuration to completion in the mixed form and in FP64 (equal work:
+    the same population, load cases and increments), and the first `compare` RVEs solved
+    one at a time in plain FP64 (the drop-in's use) against the same RVEs batched mixed,
+    both timed with CUDA events."""
+    pop = batch_population(n_rves)
+    mixed, recs_m = _run_batch(g, torch, pop, "mixed", increments, seconds)
+    fp64, recs_f = _run_batch(g, torch, pop, "fp64", increments, seconds)
+    out = {"mixed": mixed, "fp64": fp64, "value": mixed["value"], "unit": UNIT,
+           "mixed_vs_fp64_batched": mixed["value"] / fp64["value"] if fp64["value"] else None,
+           "max_rel_P_av_error_mixed_vs_fp64": _max_err(recs_m, recs_f)}
     if compare:
-        # the first `compare` RVEs: batched mixed vs one-at-a-time plain FP64, `inc` increments each
-        inc = 2
         sub = pop[:compare]
         plain = g.numerics(precision="fp64")
-        steps2 = {k: [g.load_step(k, t=float(increments), N=increments)] for k in BATCH_KINDS}
-        ref_recs, t_seq, pts_seq = [], 0.0, 0
+        steps = {k: g.load_step(k, t=float(increments), N=increments) for k in BATCH_KINDS}
+        ref_recs, ms_seq, pts_seq = [], 0.0, 0
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
         for cells, ng, kind, mat, q in sub:
             r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=plain)
+            st = torch.cuda.ExternalStream(r.stream)
             r.init()
             c0 = r.counters()
-            torch.cuda.synchronize(); t0 = time.perf_counter()
-            recs = [r.run_increment(steps2[kind][0], 0, i) for i in range(inc)]
-            torch.cuda.synchronize(); t_seq += time.perf_counter() - t0
+            torch.cuda.synchronize()
+            e0.record(st)
+            recs = [r.run_increment(steps[kind], 0, i) for i in range(increments)]
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms_seq += e0.elapsed_time(e1)
             pts_seq += r.N * (r.counters()["evaluations"] - c0["evaluations"])
             ref_recs.append(recs)
             r.close()
-        # same dt (1 s) as the population's load case, `inc` increments
-        steps3 = {k: [g.load_step(k, t=float(inc), N=inc)] for k in BATCH_KINDS}
-        b2 = g.Batch(len(sub))
-        members = []
-        for cells, ng, kind, mat, q in sub:
-            r = g.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=mixed)
-            members.append((r, b2.add(r, steps3[kind])))
-        s0 = b2.stats()
-        torch.cuda.synchronize(); t0 = time.perf_counter()
-        b2.run()
-        torch.cuda.synchronize(); t_b = time.perf_counter() - t0
-        pts_b = b2.stats()["point_evaluations"] - s0["point_evaluations"]
-        err = 0.0
-        for (r, slot), rr in zip(members, ref_recs):
-            for a_, b_ in zip(b2.records(slot), rr):
-                err = max(err, float(abs(a_["P_av"] - b_["P_av"]).max() / abs(b_["P_av"]).max()))
-        b2.close()
-        for r, _ in members:
-            r.close()
-        out["vs_plain_fp64_sequential"] = {
-            "rves": compare, "increments": inc, "plain_fp64_one_at_a_time": pts_seq / t_seq,
-            "batched_mixed": pts_b / t_b, "speedup": (pts_b / t_b) / (pts_seq / t_seq),
-            "max_rel_P_av_error_vs_fp64": err, "timing": "host wall clock, both sides"}
+        bm, recs_b = _run_batch(g, torch, sub, "mixed", increments, seconds)
+        seq = pts_seq / (ms_seq * 1e-3)
+        out["vs_plain_fp64_one_at_a_time"] = {
+            "rves": compare, "increments": increments, "plain_fp64_one_at_a_time": seq,
+            "batched_mixed": bm["value"], "speedup": bm["value"] / seq,
+            "max_rel_P_av_error_vs_fp64": _max_err(recs_b, ref_recs),
+            "timing": "CUDA events on each solver's stream (one at a time: sum over the RVEs' solves)"}
     return out
 
 
@@ -339,11 +367,15 @@ def mixed_large_leg(g, torch, cells=128, grains=1000, inc_each=30):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         ev = rve.counters()["evaluations"]
-        out[prec] = {"value": rve.N * ev / (ms * 1e-3), "unit": UNIT, "seconds": ms * 1e-3, "evaluations": ev}
+        lat = [x["seconds"] for x in recs[prec]]
+        out[prec] = {"value": rve.N * ev / (ms * 1e-3), "unit": UNIT, "seconds": ms * 1e-3, "evaluations": ev,
+                     "p50_increment_ms": 1e3 * _pct(lat, 50), "p99_increment_ms": 1e3 * _pct(lat, 99)}
         rve.close()
     errs = [float(abs(a["P_av"] - b["P_av"]).max() / abs(b["P_av"]).max()) for a, b in zip(recs["mixed"], recs["fp64"])]
     out["max_rel_P_av_error_vs_fp64"] = max(errs)
     out["per_increment_error"] = errs
+    out["error_reference"] = ("the GPU FP64 form of the same load case (itself within 1e-8 of the CPU oracle in the "
+                              "parity tests at 16^3 and 64^3; the oracle needs minutes per 128^3 increment)")
     return out
 
 
@@ -545,24 +577,27 @@ def gpu_arm(a):
                        "d2h_bytes_per_step": (c1["d2h_bytes"] - c0["d2h_bytes"]) / a.steps,
                        "note": "public C-ABI increments, P and F fields copied every step into pinned host "
                                "buffers (AoS, transposed on the device)"}
-        # mixed precision form on the same workload, measured like `value` (same warm-up and
-        # timed increments, CUDA events on the solver's stream); P_av error per increment
-        # against the FP64 run of the same increments
+        # both forms over the whole load case of the workload (solver init and all
+        # increments, CUDA events on each solver's stream); P_av error of the mixed form
+        # per increment against the FP64 run, and against the CPU oracle for the
+        # increments of the oracle sample (below)
+        recs = {}
         if a.precision == "fp64":
-            recs = {}
-            vals = {}
+            vals, secs = {}, {}
             for prec in ("fp64", "mixed"):
                 r2 = g.RVE(cells, size, mat_at, q, num=g.numerics(precision=prec))
                 st2 = torch.cuda.ExternalStream(r2.stream)
-                run_increments(r2, step, 0, a.warmup, a.increments)
+                torch.cuda.synchronize()
                 c0, tm0 = r2.counters(), r2.timers()
                 e0.record(st2)
                 out = []
-                run_increments(r2, step, a.warmup, a.steps, a.increments, records=out)
+                run_increments(r2, step, 0, a.increments, a.increments, records=out)
                 e1.record(st2)
                 torch.cuda.synchronize()
                 c1, tm1 = r2.counters(), r2.timers()
-                vals[prec] = n * (c1["evaluations"] - c0["evaluations"]) / (e0.elapsed_time(e1) * 1e-3)
+                ms2 = e0.elapsed_time(e1)
+                vals[prec] = n * (c1["evaluations"] - c0["evaluations"]) / (ms2 * 1e-3)
+                secs[prec] = ms2 * 1e-3
                 recs[prec] = out
                 if prec == "mixed":
                     kms_m = tm1["constitutive_ms"] - tm0["constitutive_ms"]
@@ -581,27 +616,37 @@ def gpu_arm(a):
                                   "fp64_flops_per_launch": fl64 / nl_m, "fp32_flops_per_launch": fl32 / nl_m,
                                   "units_per_evaluation": {k: v / max(1, n * (c1["evaluations"] - c0["evaluations"]))
                                                            for k, v in units.items()},
-                                  "kernel_time_share": kms_m / e0.elapsed_time(e1),
+                                  "kernel_time_share": kms_m / ms2,
                                   "spectral_ms_per_residual": (tm1["spectral_ms"] - tm0["spectral_ms"]) /
                                   max(1, tm1["spectral_launches"] - tm0["spectral_launches"])}
                 r2.close()
             errs = [float(abs(b["P_av"] - a_["P_av"]).max() / abs(a_["P_av"]).max())
                     for a_, b in zip(recs["fp64"], recs["mixed"])]
             line["mixed"] = {"value": vals["mixed"], "unit": UNIT, "fp64_same_run": vals["fp64"],
-                             "increments": a.steps, "max_rel_P_av_error_vs_fp64": max(errs),
-                             "per_increment_error": errs, "roofline": mixed_roof,
-                             "note": "FP32 FFT / Gamma with FP64 accumulation; Lp Newton Jacobian and hardening rate in FP32 (residual, update, convergence tests, tangent FP64); timed like value"}
+                             "increments": a.increments, "seconds": secs,
+                             "timed": "whole load case (solver init and every increment) in each form",
+                             "max_rel_P_av_error_vs_fp64": max(errs),
+                             "per_increment_error_vs_fp64": errs, "roofline": mixed_roof,
+                             "note": "FP32 FFT / Gamma with FP64 accumulation; Lp Newton Jacobian and hardening rate in FP32 (residual, update, convergence tests, tangent FP64)"}
         if a.batch_rves > 0:
             line["batched"] = batch_leg(g, torch, a.batch_rves, 20, a.batch_seconds, a.batch_compare)
-        if a.mixed_large:
+        if not a.no_mixed_large:
             line["mixed_128"] = mixed_large_leg(g, torch)
         if a.serve_requests > 0:
-            line["serving"] = [serve_leg(g, p, a.serve_rate, a.serve_requests, a.serve_seconds)
-                               for p in ("fp64", "mixed")]
+            line["serving"] = [serve_leg(g, p, float(rate), a.serve_requests, a.serve_seconds)
+                               for rate in a.serve_rates.split(",") for p in ("fp64", "mixed")]
         if rank == 0:
             threads = os.cpu_count() or 1
             try:
-                v, dt, ev, _ = cpu_oracle_sample(a, a.cpu_sample_increments, threads)
+                v, dt, ev, orecs = cpu_oracle_sample(a, a.cpu_sample_increments, threads)
+                if "mixed" in line:
+                    k = min(len(orecs), len(recs.get("mixed", [])))
+                    ev_or = [float(abs(recs[pr][i]["P_av"] - from_fortran9(orecs[i]["P_av"])).max() /
+                                   abs(from_fortran9(orecs[i]["P_av"])).max()) for pr in ("mixed", "fp64")
+                             for i in range(k)]
+                    line["mixed"]["max_rel_P_av_error_vs_oracle"] = max(ev_or[:k]) if k else None
+                    line["mixed"]["fp64_max_rel_P_av_error_vs_oracle"] = max(ev_or[k:]) if k else None
+                    line["mixed"]["oracle_increments"] = k
                 line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                         "sample": f"solver init + first {a.cpu_sample_increments} increment(s) of the "
                                                   f"{a.cells}^3 workload ({ev} residual evaluations, {dt:.1f} s), "
@@ -626,9 +671,10 @@ def gpu_arm(a):
 
 def north_star_ratios(line):
     """The mixed form against the plain FP64 form, from the legs of this run that
-    measured both: same workload (64^3 and, with --mixed-large, 128^3), the batched
-    population against the same RVEs one at a time in FP64, the served mix against the
-    same mix served in FP64.  A summary of values already in the line."""
+    measured both on equal work: the 64^3 workload's whole load case, the 128^3
+    configuration, the batched population in both forms, the batched population's
+    first RVEs batched mixed against one at a time in FP64, and the served mix at each
+    arrival rate in both forms.  A summary of values already in the line."""
     r = {}
     try:
         m = line.get("mixed")
@@ -637,12 +683,21 @@ def north_star_ratios(line):
         m128 = line.get("mixed_128")
         if m128 and m128.get("fp64", {}).get("value"):
             r["mixed_vs_fp64_128cube"] = m128["mixed"]["value"] / m128["fp64"]["value"]
-        seq = (line.get("batched") or {}).get("vs_plain_fp64_sequential")
+        b = line.get("batched") or {}
+        if b.get("mixed_vs_fp64_batched"):
+            r["batched_mixed_vs_batched_fp64"] = b["mixed_vs_fp64_batched"]
+        seq = b.get("vs_plain_fp64_one_at_a_time")
         if seq:
             r["batched_mixed_vs_fp64_one_at_a_time"] = seq["speedup"]
-        sv = {x["precision"]: x["value"] for x in line.get("serving") or [] if x.get("value")}
-        if "mixed" in sv and "fp64" in sv:
-            r["served_mixed_vs_served_fp64"] = sv["mixed"] / sv["fp64"]
+        sv = {}
+        for x in line.get("serving") or []:
+            if x.get("value"):
+                sv.setdefault(x["rate_req_per_s"], {})[x["precision"]] = x["value"]
+        for rate, v in sorted(sv.items()):
+            if "mixed" in v and "fp64" in v:
+                r[f"served_mixed_vs_served_fp64_{rate:g}_req_s"] = v["mixed"] / v["fp64"]
+        if "value" in line and b.get("value"):
+            r["batched_mixed_vs_plain_fp64_value"] = b["value"] / line["value"]
     except (KeyError, TypeError, ZeroDivisionError):
         pass
     return r

@@ -131,8 +131,12 @@ dgx_status dgx_fft_forward(dgx_rve* rve, const double* field, double* spectrum);
  * (larger grids return DGX_ERR_ARG).  All calls share that array and leave their
  * contents in it, so calls that overlap on the GPU race and must be serialised.
  * The first call on a device looks up the array's address (make it before any
- * stream capture).  P_device: device (3,3,N) reference layout; rms_device: one
- * device double; stream: cudaStream_t (0 = default stream); asynchronous. */
+ * stream capture).  divergence_correction 0 none, 1 size, 2 size+grid (else
+ * DGX_ERR_ARG); derivative 0 continuous, 1 central difference.  A CUDA error left
+ * pending by earlier work is reported (DGX_ERR_CUDA) and not cleared.
+ * P_device: device (3,3,N) reference layout; rms_device: one device double;
+ * stream: cudaStream_t (0 = default stream); the result is written asynchronously
+ * on the stream (the small FFT tables are staged from host memory first). */
 dgx_status dgx_divergence_rms_static(const int32_t cells[3], const double size[3], int32_t divergence_correction,
                                      int32_t derivative, const double* P_device, double* rms_device, void* stream);
 

@@ -180,6 +180,7 @@ struct Executor {
   ConsItem* d_cons = nullptr; SpecItem* d_spec = nullptr; MultiItem* d_multi = nullptr;
   int* d_ill = nullptr; double* d_Pav = nullptr; double* d_aim = nullptr; double* d_rms = nullptr;
   double* d_mout = nullptr; unsigned long long* d_queue = nullptr;
+  int qcap = 16;                               // tile queues: one per constitutive group of a round
   ConsItem* h_cons = nullptr; SpecItem* h_spec = nullptr; MultiItem* h_multi = nullptr;
   int* h_ill = nullptr; double* h_Pav = nullptr; double* h_rms = nullptr;
   double* h_mout = nullptr;
@@ -252,7 +253,8 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   EA(&e->d_mout, &e->h_mout, 64 * 2 * cap);
   EA(&e->d_bcitem, &e->h_bcitem, cap);
   EA(&e->d_bcout, &e->h_bcout, 10 * cap);
-  EA(&e->d_queue, (unsigned long long**)nullptr, 16);
+  e->qcap = std::max(16, cap);
+  EA(&e->d_queue, (unsigned long long**)nullptr, e->qcap);
   EA((ConsCounters**)nullptr, &e->h_cnt, 1);
   EA((double**)nullptr, &e->h_tan, 162 * (size_t)cap);
   if (cnt) e->cnt = cnt;
@@ -309,8 +311,7 @@ static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0
   const size_t cs = fp32 ? sizeof(float2) : sizeof(double2);
   const SpecGeom& g = base.g;
   auto time_of = [&](const SpecLaunch& L) -> float {
-    if (!spec_launch_fits(L)) return 1e30f;
-    spec_prepare(L, fp32);
+    if (!spec_prepare(L, fp32)) return 1e30f;
     // best of three, on at most four of the group's RVEs (the tile choice is per RVE)
     float ms = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
@@ -350,8 +351,7 @@ static const SpecLaunch& spec_tiles(Executor* e, const GridKey& key, dgx_rve* r0
     }
   }
   SpecLaunch L = spec_launch_tiles(g.N0, g.N1, g.N2, cs, best[0], best[1], best[2]);
-  if (!spec_launch_fits(L)) L = base;
-  spec_prepare(L, fp32);
+  if (!spec_prepare(L, fp32)) L = base;
   return e->spec_tuned.emplace(key, L).first->second;
 }
 
@@ -442,7 +442,7 @@ static dgx_status ex_issue(Executor* e, RoundPlan& p, bool capture, IssueCount& 
   CK(rec(4));
   if (n > 0) {
     CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, st));
-    CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * 16, st));
+    CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * e->qcap, st));
     CK(h2d(e->d_cons, e->h_cons, sizeof(ConsItem) * n));
     CK(h2d(e->d_bcitem, e->h_bcitem, sizeof(BcItem) * n));
     CK(h2d(e->d_spec, e->h_spec, sizeof(SpecItem) * n));
@@ -602,7 +602,7 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
         e->point_evals += r->N;
       }
       close_group(n);
-      if (p.cons.size() > 16) { set_err("executor: more than 16 materials in one round"); return DGX_ERR_UNSUPPORTED; }
+      if ((int)p.cons.size() > e->qcap) { set_err("executor: more constitutive groups than queue slots"); return DGX_ERR_STATE; }
     }
     for (int i = 0; i < n; ++i)
       e->h_bcitem[i] = BcItem{q[i].r->d_bc, e->d_Pav + 9 * slot_of[i], e->d_aim + 9 * i, e->d_bcout + 10 * i};

@@ -17,14 +17,23 @@
 //    calls concurrently) race on it and must be serialised by the caller;
 //  * the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress, with that device current); make that first call
-//    before any stream capture on the device.
+//    before any stream capture on the device;
+//  * the FFT twiddles and frequency tables are built on the host by the same code
+//    as the regular entry point and copied into the array on every call
+//    (cudaMemcpyAsync from pageable host memory: the call returns once the host
+//    data is staged), so both entry points use identical tables.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "../../include/dgx.h"
 #include "spectral.cuh"
+
+namespace dgx { void set_err(const char* fmt, ...); }
 
 namespace {
 
@@ -40,38 +49,21 @@ constexpr long long SCRATCH_DOUBLES = OFF_PART + MAXC + 64;
 
 static __device__ __align__(256) double g_scratch[SCRATCH_DOUBLES];
 
+// device address of g_scratch per device, looked up once per device (host threads may
+// call concurrently: the lookup runs under a lock, readers see a published pointer)
 constexpr int MAX_DEVICES = 64;
-static double* g_scratch_ptr[MAX_DEVICES] = {nullptr};
+static std::atomic<double*> g_scratch_ptr[MAX_DEVICES];
+static std::mutex g_scratch_mu;
 
-// twiddles exp(-2 pi i j / n) (FP64 and FP32) with the octant reduction used by
-// the host tables, and the xi1st frequency table (imaginary parts) of one axis
-__global__ void k_axis_tables(int n, int nxi, int axis_is_x, double size, int derivative, double2* tw, float2* twf,
-                              double* xi) {
-  const double TAU = 6.283185307179586476925286766559;
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n || j < nxi; j += gridDim.x * blockDim.x) {
-    if (j < n) {
-      long q = (4L * j) / n, r = 4L * j - q * n;
-      double c0, s0;
-      if (r == 0) { c0 = 1.0; s0 = 0.0; }
-      else if (2 * r <= n) { double a = (TAU / 4.0) * ((double)r / (double)n); c0 = cos(a); s0 = sin(a); }
-      else { double a = (TAU / 4.0) * ((double)(n - r) / (double)n); c0 = sin(a); s0 = cos(a); }
-      double c, s;
-      switch (q) {
-        case 0: c = c0; s = s0; break;
-        case 1: c = -s0; s = c0; break;
-        case 2: c = -c0; s = -s0; break;
-        default: c = s0; s = -c0; break;
-      }
-      tw[j] = make_double2(c, -s);
-      twf[j] = make_float2((float)c, (float)-s);
-    }
-    if (j < nxi) {
-      int k = axis_is_x ? j : (j > n / 2 ? j - n : j);
-      double val = derivative == 0 ? TAU * k / size : sin(TAU * k / n) / (2.0 * size / n);
-      bool nyq = (n % 2 == 0) && (j == n / 2) && derivative == 0;
-      xi[j] = nyq ? 0.0 : val;
-    }
-  }
+double* scratch_address(int dev) {
+  double* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (p) return p;
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  p = g_scratch_ptr[dev].load(std::memory_order_relaxed);
+  if (p) return p;
+  if (cudaGetSymbolAddress((void**)&p, g_scratch) != cudaSuccess || !p) return nullptr;
+  g_scratch_ptr[dev].store(p, std::memory_order_release);
+  return p;
 }
 
 // reference layout (3,3,N) interleaved -> 9 planes
@@ -88,61 +80,60 @@ __global__ void k_interleaved_to_planes(const double* __restrict__ a, long long 
 extern "C" dgx_status dgx_divergence_rms_static(const int32_t cells[3], const double size[3],
                                                 int32_t divergence_correction, int32_t derivative,
                                                 const double* P_device, double* rms_device, void* stream) {
-  if (!cells || !size || !P_device || !rms_device) return DGX_ERR_ARG;
+  using dgx::set_err;
+  if (!cells || !size || !P_device || !rms_device) { set_err("dgx_divergence_rms_static: null argument"); return DGX_ERR_ARG; }
   for (int i = 0; i < 3; ++i)
-    if (cells[i] < 1 || !(size[i] > 0.0)) return DGX_ERR_ARG;
+    if (cells[i] < 1 || !(size[i] > 0.0)) { set_err("dgx_divergence_rms_static: bad cells / size"); return DGX_ERR_ARG; }
+  if (divergence_correction < 0 || divergence_correction > 2) {
+    set_err("dgx_divergence_rms_static: divergence_correction must be 0, 1 or 2"); return DGX_ERR_ARG;
+  }
+  if (derivative == 2) { set_err("dgx_divergence_rms_static: FWBW derivative not supported here"); return DGX_ERR_UNSUPPORTED; }
+  if (derivative != 0 && derivative != 1) { set_err("dgx_divergence_rms_static: derivative must be 0 or 1"); return DGX_ERR_ARG; }
   const long long N = (long long)cells[0] * cells[1] * cells[2];
-  if (N > MAXC) return DGX_ERR_ARG;                    // beyond the static scratch
-  if (derivative != 0 && derivative != 1) return DGX_ERR_UNSUPPORTED;
+  if (N > MAXC) { set_err("dgx_divergence_rms_static: %lld cells exceed the static limit of %lld", N, MAXC); return DGX_ERR_ARG; }
   dgx::AxisPlan plan[3];
-  for (int i = 0; i < 3; ++i) {
-    plan[i].n = cells[i];
-    plan[i].nstages = dgx::factorize(cells[i], plan[i].radix);
-    if (plan[i].nstages < 0) return DGX_ERR_UNSUPPORTED;
-    for (int k = 0; k < plan[i].nstages; ++k)
-      if (plan[i].radix[k] > 16) return DGX_ERR_UNSUPPORTED;
+  for (int i = 0; i < 3; ++i)
+    if (!dgx::axis_plan(cells[i], &plan[i])) { set_err("dgx_divergence_rms_static: no FFT plan for %d", cells[i]); return DGX_ERR_UNSUPPORTED; }
+  // an error left pending by earlier work on this thread is reported as such, and
+  // left in place, rather than attributed to this call
+  cudaError_t pend = cudaPeekAtLastError();
+  if (pend != cudaSuccess) {
+    set_err("dgx_divergence_rms_static: CUDA error pending from earlier work: %s", cudaGetErrorString(pend));
+    return DGX_ERR_CUDA;
   }
-  dgx::SpecLaunch L = dgx::spec_launch(cells[0], cells[1], cells[2], sizeof(double2));
-  const size_t SMEM_MAX = 227 * 1024;                  // one line tile per pass must fit shared memory
-  if (L.smx > SMEM_MAX || L.smy > SMEM_MAX || L.smz > SMEM_MAX) return DGX_ERR_UNSUPPORTED;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return DGX_ERR_CUDA;
-  if (!g_scratch_ptr[dev]) {
-    double* p = nullptr;
-    if (cudaGetSymbolAddress((void**)&p, g_scratch) != cudaSuccess || !p) return DGX_ERR_CUDA;
-    g_scratch_ptr[dev] = p;
-  }
-  double* base = g_scratch_ptr[dev];
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) { set_err("dgx_divergence_rms_static: no device"); return DGX_ERR_CUDA; }
+  dgx::SpecLaunch L = dgx::spec_launch(cells[0], cells[1], cells[2], sizeof(double2));
+  if (!dgx::spec_prepare(L, false)) { set_err("dgx_divergence_rms_static: FFT line tiles exceed shared memory"); return DGX_ERR_UNSUPPORTED; }
+  double* base = scratch_address(dev);
+  if (!base) { set_err("dgx_divergence_rms_static: cudaGetSymbolAddress failed"); return DGX_ERR_CUDA; }
   cudaStream_t st = (cudaStream_t)stream;
-  // divergence correction of the reference (MechBase::base_init)
   double scaled[3];
-  {
-    int idx[3] = {0, 1, 2};
-    if (divergence_correction == 1 || divergence_correction == 2) {
-      double key[3];
-      for (int i = 0; i < 3; ++i) key[i] = divergence_correction == 1 ? size[i] : size[i] / (double)cells[i];
-      for (int a = 1; a < 3; ++a)
-        for (int b = a; b > 0 && key[idx[b]] < key[idx[b - 1]]; --b) { int t = idx[b]; idx[b] = idx[b - 1]; idx[b - 1] = t; }
-      for (int j = 0; j < 3; ++j)
-        scaled[j] = divergence_correction == 1 ? size[j] / size[idx[1]] : size[j] / size[idx[1]] * cells[idx[1]];
-    } else {
-      for (int j = 0; j < 3; ++j) scaled[j] = size[j];
-    }
-  }
+  dgx::scaled_geometry(cells, size, divergence_correction, scaled);
   double* planes = base + OFF_PLANAR;
   double* spec = base + OFF_SPEC;
   double* xi[3];
+  // twiddle and frequency tables: the same host tables as the regular entry point,
+  // copied from host memory into the static array (no device allocation)
   for (int i = 0; i < 3; ++i) {
     double2* tw = reinterpret_cast<double2*>(base + OFF_TW + 3 * TW_LEN * i);
     float2* twf = reinterpret_cast<float2*>(base + OFF_TW + 3 * TW_LEN * i + 2 * TW_LEN);
     xi[i] = base + OFF_XI + TW_LEN * i;
-    int nxi = i == 0 ? cells[0] / 2 + 1 : cells[i];
-    k_axis_tables<<<64, 256, 0, st>>>(cells[i], nxi, i == 0, size[i], derivative, tw, twf, xi[i]);
+    std::vector<double2> h_tw;
+    std::vector<float2> h_twf;
+    std::vector<double> h_xi;
+    dgx::axis_tables(cells[i], h_tw, h_twf);
+    dgx::xi_axis(i, cells, size, derivative, h_xi);
+    if (cudaMemcpyAsync(tw, h_tw.data(), sizeof(double2) * h_tw.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(twf, h_twf.data(), sizeof(float2) * h_twf.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(xi[i], h_xi.data(), sizeof(double) * h_xi.size(), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+      set_err("dgx_divergence_rms_static: table upload: %s", cudaGetErrorString(cudaGetLastError()));
+      return DGX_ERR_CUDA;
+    }
     plan[i].tw = tw;
     plan[i].twf = twf;
   }
   k_interleaved_to_planes<<<(int)((9 * N + 255) / 256), 256, 0, st>>>(P_device, N, planes);
-  dgx::spec_prepare(L, false);
   dgx::GammaArgs ga{};
   ga.xi_x = xi[0]; ga.xi_y = xi[1]; ga.xi_z = xi[2];
   for (int i = 0; i < 3; ++i) ga.resc[i] = size[i] / scaled[i];
@@ -150,5 +141,7 @@ extern "C" dgx_status dgx_divergence_rms_static(const int32_t cells[3], const do
   ga.div_part = base + OFF_PART;
   dgx::spec_convolve(L, false, plan[0], plan[1], plan[2], planes, planes, N, spec, ga, st);
   dgx::spec_div_finish(ga.div_part, L.ndiv, std::pow((double)N, -1.0), cells[0], rms_device, st);
-  return cudaGetLastError() == cudaSuccess ? DGX_OK : DGX_ERR_CUDA;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_err("dgx_divergence_rms_static: launch: %s", cudaGetErrorString(e)); return DGX_ERR_CUDA; }
+  return DGX_OK;
 }

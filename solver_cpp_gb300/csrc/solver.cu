@@ -677,18 +677,7 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
         if (r->mp.P[a][k + 3 * l] != sg * r->mp.pval) { set_err("Schmid table mismatch"); delete r; return DGX_ERR_STATE; }
       }
   // divergence correction (MechBase::base_init, mech_base.cpp:11-43)
-  {
-    int idx[3] = {0, 1, 2};
-    int dc = num->divergence_correction;
-    if (dc == 1 || dc == 2) {
-      double key[3];
-      for (int i = 0; i < 3; ++i) key[i] = dc == 1 ? size[i] : size[i] / (double)cells[i];
-      for (int a = 1; a < 3; ++a) for (int b = a; b > 0 && key[idx[b]] < key[idx[b - 1]]; --b) std::swap(idx[b], idx[b - 1]);
-      for (int j = 0; j < 3; ++j) r->scaled[j] = dc == 1 ? size[j] / size[idx[1]] : size[j] / size[idx[1]] * cells[idx[1]];
-    } else {
-      for (int j = 0; j < 3; ++j) r->scaled[j] = size[j];
-    }
-  }
+  scaled_geometry(cells, size, num->divergence_correction, r->scaled);
   cudaError_t ce = cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking);
   if (ce != cudaSuccess) { set_err("cudaStreamCreate: %s", cudaGetErrorString(ce)); delete r; return DGX_ERR_CUDA; }
   r->owns_stream = true;
@@ -699,21 +688,17 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
   bool fp32 = num->precision == 1;
   for (int i = 0; i < 3; ++i)
     if (!axis_create(&r->ax[i], cells[i])) { set_err("FFT plan for length %d failed", cells[i]); dgx_rve_destroy(r); return DGX_ERR_UNSUPPORTED; }
-  spec_prepare(r->sl, fp32);
+  if (!spec_prepare(r->sl, fp32)) {
+    set_err("grid %dx%dx%d: FFT line tiles exceed the device's shared memory", cells[0], cells[1], cells[2]);
+    dgx_rve_destroy(r); return DGX_ERR_UNSUPPORTED;
+  }
   // xi1st per axis (imaginary parts; continuous or central difference)
   {
-    const double TAU = 6.283185307179586476925286766559;
-    int lens[3] = {cells[0] / 2 + 1, cells[1], cells[2]};
     double* dst[3] = {r->d_xi_x, r->d_xi_y, r->d_xi_z};
     for (int p = 0; p < 3; ++p) {
-      std::vector<double> v(lens[p]);
-      for (int i = 0; i < lens[p]; ++i) {
-        int k = (p == 0) ? i : (i > cells[p] / 2 ? i - cells[p] : i);
-        double val = num->derivative == 0 ? TAU * k / size[p] : std::sin(TAU * k / cells[p]) / (2.0 * size[p] / cells[p]);
-        bool nyq = (cells[p] % 2 == 0) && (i == cells[p] / 2) && num->derivative == 0;
-        v[i] = nyq ? 0.0 : val;
-      }
-      if (cudaMemcpy(dst[p], v.data(), sizeof(double) * lens[p], cudaMemcpyHostToDevice) != cudaSuccess) {
+      std::vector<double> v;
+      xi_axis(p, cells, size, num->derivative, v);
+      if (cudaMemcpy(dst[p], v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
         set_err("xi upload failed"); dgx_rve_destroy(r); return DGX_ERR_CUDA;
       }
     }

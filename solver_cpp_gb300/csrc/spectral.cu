@@ -91,6 +91,18 @@ __device__ typename cpx<R>::t* block_fft(typename cpx<R>::t* a, typename cpx<R>:
         y1.x = d02.x + rot.x; y1.y = d02.y + rot.y;
         y3.x = d02.x - rot.x; y3.y = d02.y - rot.y;
         out[od] = y0; out[od + Ls] = y1; out[od + 2 * Ls] = y2; out[od + 3 * Ls] = y3;
+      } else if (r > 16) {
+        // a prime factor above 16: each of the r outputs is a direct DFT sum over the
+        // r inputs, read from shared memory (no per-thread array)
+        for (int s2 = 0; s2 < r; ++s2) {
+          C acc = in[j];
+          for (int q = 1; q < r; ++q) {
+            const C vq = cmul(in[j + q * m], twid<R>(p, q * twstep, sign));
+            const C t2 = cmul(vq, twid<R>(p, (int)(((long)q * s2 * m) % n), sign));
+            acc.x += t2.x; acc.y += t2.y;
+          }
+          out[od + s2 * Ls] = acc;
+        }
       } else {
         C v[16];
         for (int q = 0; q < r; ++q) v[q] = cmul(in[j + q * m], twid<R>(p, q * twstep, sign));
@@ -480,8 +492,11 @@ __global__ void k_div_finish(const double* __restrict__ part, int nb, double wgt
 
 // ------------------------------------------------------------------ host side
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 namespace dgx {
@@ -506,34 +521,76 @@ void twiddle(long j, long n, double* c, double* s) {
 
 int factorize(int n, int* rad) {
   int ns = 0, m = n;
-  while (m % 4 == 0) { rad[ns++] = 4; m /= 4; }
-  while (m % 2 == 0) { rad[ns++] = 2; m /= 2; }
+  while (m % 4 == 0 && ns < 16) { rad[ns++] = 4; m /= 4; }
+  while (m % 2 == 0 && ns < 16) { rad[ns++] = 2; m /= 2; }
   for (int r = 3; m > 1 && ns < 16; r += 2)
-    while (m % r == 0) { rad[ns++] = r; m /= r; }
+    while (m % r == 0 && ns < 16) { rad[ns++] = r; m /= r; }
   return m == 1 ? ns : -1;
 }
 
-bool axis_create(AxisHost* ax, int n) {
-  ax->plan.n = n;
-  int ns = factorize(n, ax->plan.radix);
-  if (ns < 0) return false;
-  for (int s = 0; s < ns; ++s) if (ax->plan.radix[s] > 16) return false;
-  ax->plan.nstages = ns;
-  std::vector<double2> tw(n);
-  std::vector<float2> twf(n);
+void axis_tables(int n, std::vector<double2>& tw, std::vector<float2>& twf) {
+  tw.resize(n);
+  twf.resize(n);
   for (int j = 0; j < n; ++j) {
     double c, s;
     twiddle(j, n, &c, &s);
     tw[j] = make_double2(c, -s);
     twf[j] = make_float2((float)c, (float)-s);
   }
+}
+
+bool axis_plan(int n, AxisPlan* p) {
+  p->n = n;
+  p->nstages = factorize(n, p->radix);
+  p->tw = nullptr;
+  p->twf = nullptr;
+  return p->nstages >= 0;
+}
+
+bool axis_create(AxisHost* ax, int n) {
+  if (!axis_plan(n, &ax->plan)) return false;
+  std::vector<double2> tw;
+  std::vector<float2> twf;
+  axis_tables(n, tw, twf);
   if (cudaMalloc(&ax->d_tw, sizeof(double2) * n) != cudaSuccess) return false;
   if (cudaMalloc(&ax->d_twf, sizeof(float2) * n) != cudaSuccess) return false;
-  cudaMemcpy(ax->d_tw, tw.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
-  cudaMemcpy(ax->d_twf, twf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
+  if (cudaMemcpy(ax->d_tw, tw.data(), sizeof(double2) * n, cudaMemcpyHostToDevice) != cudaSuccess) return false;
+  if (cudaMemcpy(ax->d_twf, twf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice) != cudaSuccess) return false;
   ax->plan.tw = ax->d_tw;
   ax->plan.twf = ax->d_twf;
   return true;
+}
+
+void scaled_geometry(const int cells[3], const double size[3], int divergence_correction, double out[3]) {
+  // MechBase::base_init (mech_base.cpp:11-43): 1 size, 2 size + grid, else none
+  int idx[3] = {0, 1, 2};
+  const int dc = divergence_correction;
+  if (dc == 1 || dc == 2) {
+    double key[3];
+    for (int i = 0; i < 3; ++i) key[i] = dc == 1 ? size[i] : size[i] / (double)cells[i];
+    for (int a = 1; a < 3; ++a)
+      for (int b = a; b > 0 && key[idx[b]] < key[idx[b - 1]]; --b) std::swap(idx[b], idx[b - 1]);
+    for (int j = 0; j < 3; ++j) out[j] = dc == 1 ? size[j] / size[idx[1]] : size[j] / size[idx[1]] * cells[idx[1]];
+  } else {
+    for (int j = 0; j < 3; ++j) out[j] = size[j];
+  }
+}
+
+void xi_axis(int axis, const int cells[3], const double size[3], int derivative, std::vector<double>& v) {
+  // imaginary part of xi1st along one axis (Spectral::init / get_freq_derivative,
+  // spectral.cpp:53-130): continuous 2 pi k / size with the Nyquist frequency zeroed
+  // (per component), central difference sin(2 pi k / n) / (2 size / n); x holds the
+  // N0/2+1 non-negative frequencies, y and z all n in FFT order
+  const double TAU = 6.283185307179586476925286766559;
+  const int n = cells[axis];
+  const int len = axis == 0 ? n / 2 + 1 : n;
+  v.resize(len);
+  for (int i = 0; i < len; ++i) {
+    const int k = axis == 0 ? i : (i > n / 2 ? i - n : i);
+    const double val = derivative == 0 ? TAU * k / size[axis] : std::sin(TAU * k / n) / (2.0 * size[axis] / n);
+    const bool nyq = (n % 2 == 0) && (i == n / 2) && derivative == 0;
+    v[i] = nyq ? 0.0 : val;
+  }
 }
 
 void axis_destroy(AxisHost* ax) {
@@ -567,8 +624,25 @@ SpecLaunch spec_launch_tiles(int N0, int N1, int N2, size_t csize, int LX, int T
   return L;
 }
 
+// opt-in shared memory per block of the current device (queried once per device)
+static std::mutex g_dev_mu;
+static std::map<int, size_t> g_smem_optin;
+
+size_t smem_optin_limit() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 48 * 1024;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  auto it = g_smem_optin.find(dev);
+  if (it != g_smem_optin.end()) return it->second;
+  int v = 0;
+  size_t lim = 48 * 1024;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess && v > 0) lim = (size_t)v;
+  g_smem_optin[dev] = lim;
+  return lim;
+}
+
 bool spec_launch_fits(const SpecLaunch& L) {
-  const size_t mx = 227 * 1024;
+  const size_t mx = smem_optin_limit();
   return L.smx <= mx && L.smy <= mx && L.smz <= mx;
 }
 
@@ -582,24 +656,38 @@ SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize) {
   return spec_launch_tiles(N0, N1, N2, csize, LX, TIy, TIz);
 }
 
-// The dynamic shared-memory limit is a property of the kernel, shared by every
-// RVE: raise it to the largest request seen so far (never lower it, or an RVE
-// created earlier with a larger grid could no longer launch).
+// The dynamic shared-memory limit is a property of the kernel on one device, shared by
+// every RVE on that device: raise it to the largest request seen so far on the current
+// device (never lower it, or an RVE created earlier with a larger grid could no longer
+// launch).  Limits are kept per device and per precision, under a lock (RVEs may be
+// created from several host threads).
 template <typename R>
-static void set_smem_limits(const SpecLaunch& L) {
-  static size_t mx = 0, my = 0, mz = 0;
-  if (L.smz > mz) { mz = L.smz; cudaFuncSetAttribute(k_zpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mz); }
-  if (L.smy > my) { my = L.smy; cudaFuncSetAttribute(k_ypass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)my); }
-  if (L.smx > mx) {
-    mx = L.smx;
-    cudaFuncSetAttribute(k_xfwd<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
-    cudaFuncSetAttribute(k_xinv<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
+static bool set_smem_limits(const SpecLaunch& L) {
+  static std::map<int, std::array<size_t, 3>> lim;   // device -> x, y, z pass limits
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  std::array<size_t, 3>& m = lim[dev];
+  bool ok = true;
+  if (L.smz > m[2]) {
+    ok &= cudaFuncSetAttribute(k_zpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smz) == cudaSuccess;
+    if (ok) m[2] = L.smz;
   }
+  if (L.smy > m[1]) {
+    ok &= cudaFuncSetAttribute(k_ypass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smy) == cudaSuccess;
+    if (ok) m[1] = L.smy;
+  }
+  if (L.smx > m[0]) {
+    ok &= cudaFuncSetAttribute(k_xfwd<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smx) == cudaSuccess;
+    ok &= cudaFuncSetAttribute(k_xinv<R, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smx) == cudaSuccess;
+    if (ok) m[0] = L.smx;
+  }
+  return ok;
 }
 
-void spec_prepare(const SpecLaunch& L, bool fp32) {
-  if (fp32) set_smem_limits<float>(L);
-  else set_smem_limits<double>(L);
+bool spec_prepare(const SpecLaunch& L, bool fp32) {
+  if (!spec_launch_fits(L)) return false;
+  return fp32 ? set_smem_limits<float>(L) : set_smem_limits<double>(L);
 }
 
 // full convolution of 9 real planes: forward x, y, z passes, div-RMS partials and

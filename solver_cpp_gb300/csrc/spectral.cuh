@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <vector>
 
 namespace dgx {
 
@@ -60,15 +61,27 @@ struct SpecItem {
 
 // cos/sin of 2 pi j / n with the argument reduced to the first octant
 void twiddle(long j, long n, double* c, double* s);
-// radix factorisation (4, 2, then odd primes <= 16); number of stages or -1
+// radix factorisation (4, 2, then odd primes in increasing order); number of stages or -1
 int factorize(int n, int* rad);
+// twiddle tables exp(-2 pi i j / n), j < n, in FP64 and FP32
+void axis_tables(int n, std::vector<double2>& tw, std::vector<float2>& twf);
+// plan of one axis without tables (tw / twf null); false if n has more than 16 factors
+bool axis_plan(int n, AxisPlan* p);
 bool axis_create(AxisHost* ax, int n);
+// MechBase::base_init divergence correction: scaled geometry for 0 none, 1 size, 2 size+grid
+void scaled_geometry(const int cells[3], const double size[3], int divergence_correction, double out[3]);
+// imaginary parts of xi1st along one axis (continuous 0 / central difference 1)
+void xi_axis(int axis, const int cells[3], const double size[3], int derivative, std::vector<double>& v);
+// opt-in dynamic shared memory per block of the current device
+size_t smem_optin_limit();
 void axis_destroy(AxisHost* ax);
 SpecLaunch spec_launch(int N0, int N1, int N2, size_t csize);
 // explicit tile shape (autotuner); spec_launch_fits: shared memory within the limit
 SpecLaunch spec_launch_tiles(int N0, int N1, int N2, size_t csize, int LX, int TIy, int TIz);
 bool spec_launch_fits(const SpecLaunch& L);
-void spec_prepare(const SpecLaunch& L, bool fp32);
+// raise the kernels' dynamic shared-memory limits on the current device for L; false if
+// L does not fit the device or the attribute could not be set
+bool spec_prepare(const SpecLaunch& L, bool fp32);
 void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                    const double* in, double* field, long long ld, void* spec, const GammaArgs& ga, cudaStream_t st);
 // Displacements of the deformed grid from the deformation gradient planes F (ld):

@@ -49,3 +49,28 @@ def microstructure(cells, n_grains, seed, size=(1.0, 1.0, 1.0)):
     mat = voronoi(cells, size, n_grains, seed)
     q = random_quaternions(n_grains, seed + 7919)
     return mat, q
+
+
+# the batched configuration: grids uniform in {8,16,32,48}^3, 8-200 grains, load case
+# uniform in tension x / y / z and shear xy (1e-3/s), per-RVE seeds 1000 + k
+BATCH_SIZES = (8, 16, 32, 48)
+BATCH_KINDS = ("tensionX", "tensionY", "tensionZ", "shearXY")
+
+
+def batch_member(k, seed=1000):
+    """Member k of the batched population: (cells, grains, load kind, material_at, orientations)."""
+    rng = np.random.default_rng(seed + k)
+    c = int(BATCH_SIZES[rng.integers(len(BATCH_SIZES))])
+    ng = int(rng.integers(8, 201))
+    kind = BATCH_KINDS[rng.integers(len(BATCH_KINDS))]
+    mat, q = microstructure((c, c, c), ng, seed + k)
+    return (c, c, c), ng, kind, mat, q
+
+
+def batch_population(count, seed=1000):
+    return [batch_member(k, seed) for k in range(count)]
+
+
+def batch_member_sizes(count, seed=1000):
+    """Grid edge of each member without building the microstructures."""
+    return [int(BATCH_SIZES[np.random.default_rng(seed + k).integers(len(BATCH_SIZES))]) for k in range(count)]

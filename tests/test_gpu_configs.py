@@ -1,0 +1,205 @@
+"""GPU parity at the benchmark configurations, through the C ABI, against the CPU oracle.
+
+* 16^3 grid, 20 seeded Voronoi grains, tension x, 20 increments over 20 s (the
+  CPU-runnable configuration): every increment's P_av / F_av and iteration count,
+  and the final F, P, F_p, xi fields, FP64 form within 1e-8; the mixed form within
+  1e-5 of the oracle's P_av in every increment.
+* 64^3 grid, 200 grains (seed 42, the benchmark workload), tension x at 1e-3/s: the
+  first three increments (dt = 1 s, as in the 40-increment load case), P_av / F_av
+  and the F, P, F_p fields within 1e-8; the mixed form's P_av within 1e-5 of the
+  oracle; the FP32-spectrum divergence RMS of the converged stress field against the
+  FP64 one, relative to the divergence tolerance.
+* one 32^3 and one 48^3 member of the batched population (two increments of their own
+  load case) run in a dgx batch: FP64 members within 1e-8 of the oracle, mixed members
+  within 1e-5.
+* dgx_fft_forward against numpy.fft.rfftn at 48^3, 96^3, 128^3.
+The reference path restated by the oracle: src/grid/spectral.cpp:132-219,
+src/grid/mech_solver_basic.cpp:110-339, src/phase_mechanical.f90:380-693.
+"""
+import numpy as np
+import pytest
+
+from oracle import dgo
+from solver_cpp_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-8           # plain FP64 form against the oracle
+TOL_MIXED = 1e-5     # mixed form against the oracle (volume-averaged P)
+SEED16 = 16          # Voronoi seed of the 16^3 / 20-grain configuration
+SEED64 = 42          # Voronoi seed of the 64^3 / 200-grain benchmark workload
+
+
+def rel(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import solver_cpp_gb300 as g
+    from solver_cpp_gb300 import build
+    build.build()
+    return g
+
+
+def _oracle(cells, mat_at, q, steps, fields=("F", "P", "Fp", "xi")):
+    s = dgo.Solver(cells, (1.0, 1.0, 1.0), mat_at, q)
+    recs = s.run(steps)
+    return recs, {k: s.get(k) for k in fields}
+
+
+@pytest.fixture(scope="module")
+def config16():
+    cells = (16, 16, 16)
+    mat_at, q = synthetic.microstructure(cells, 20, SEED16)
+    recs, fields = _oracle(cells, mat_at, q, [dgo.loadstep("tensionX", t=20.0, N=20)])
+    return cells, mat_at, q, recs, fields
+
+
+@pytest.fixture(scope="module")
+def config64():
+    cells = (64, 64, 64)
+    mat_at, q = synthetic.microstructure(cells, 200, SEED64)
+    # the first three increments of the 40-increment / 40-s load case (dt = 1 s; the
+    # stress aim is zero throughout, so the remaining time does not enter)
+    recs, fields = _oracle(cells, mat_at, q, [dgo.loadstep("tensionX", t=3.0, N=3)], ("F", "P", "Fp"))
+    return cells, mat_at, q, recs, fields
+
+
+def _check_records(recs_g, recs_o, tol, iterations=True):
+    assert len(recs_g) == len(recs_o)
+    worst = 0.0
+    for rg, ro in zip(recs_g, recs_o):
+        e = rel(rg["P_av"], dgo.from_fortran9(ro["P_av"]))
+        assert e < tol
+        assert rel(rg["F_av"], dgo.from_fortran9(ro["F_av"])) < tol
+        if iterations:
+            assert rg["iterations"] == ro["iterations"]
+        worst = max(worst, e)
+    return worst
+
+
+def test_config16_fp64_20_increments_vs_oracle(gpu, config16):
+    cells, mat_at, q, ro, fo = config16
+    rve = gpu.RVE(cells, (1, 1, 1), mat_at, q)
+    recs = rve.loop_over_loadcase([gpu.load_step("tensionX", t=20.0, N=20)])
+    assert len(recs) == 20
+    _check_records(recs, ro, TOL)
+    for key in ("F", "P", "Fp"):
+        assert rel(rve.get(key), dgo.from_fortran9(fo[key])) < TOL, key
+    assert rel(rve.get("xi"), fo["xi"]) < TOL
+    rve.close()
+
+
+def test_config16_mixed_vs_oracle(gpu, config16):
+    cells, mat_at, q, ro, _ = config16
+    rve = gpu.RVE(cells, (1, 1, 1), mat_at, q, num=gpu.numerics(precision="mixed"))
+    recs = rve.loop_over_loadcase([gpu.load_step("tensionX", t=20.0, N=20)])
+    worst = _check_records(recs, ro, TOL_MIXED, iterations=False)
+    print(f"16^3 mixed vs oracle: max rel P_av error {worst:.2e}")
+    rve.close()
+
+
+def test_config64_fp64_first_increments_vs_oracle(gpu, config64):
+    cells, mat_at, q, ro, fo = config64
+    rve = gpu.RVE(cells, (1, 1, 1), mat_at, q)
+    step = gpu.load_step("tensionX", t=40.0, N=40)
+    rve.init()
+    recs = [rve.run_increment(step, 0, i) for i in range(3)]
+    _check_records(recs, ro, TOL)
+    for key in ("F", "P", "Fp"):
+        assert rel(rve.get(key), dgo.from_fortran9(fo[key])) < TOL, key
+    # the FP32-spectrum divergence RMS of the converged stress field: its difference from
+    # the FP64 value, relative to the divergence tolerance of the solve, is the noise
+    # floor the mixed form's convergence test works above
+    P = rve.get("P")
+    rms64 = rve.calculate_divergence_rms(P)
+    mixed = gpu.RVE(cells, (1, 1, 1), mat_at, q, num=gpu.numerics(precision="mixed"))
+    rms32 = mixed.calculate_divergence_rms(P)
+    num = gpu.numerics()
+    div_tol = max(np.abs(recs[-1]["P_av"]).max() * num.eps_rel_div, num.eps_abs_div)
+    floor = abs(rms32 - rms64) / div_tol
+    print(f"64^3 divergence RMS: FP64 {rms64:.6e}, FP32 spectrum {rms32:.6e}, |diff| / divTol {floor:.2e}")
+    assert floor < 1e-2
+    mixed.close()
+    rve.close()
+
+
+def test_config64_mixed_first_increments_vs_oracle(gpu, config64):
+    cells, mat_at, q, ro, _ = config64
+    rve = gpu.RVE(cells, (1, 1, 1), mat_at, q, num=gpu.numerics(precision="mixed"))
+    step = gpu.load_step("tensionX", t=40.0, N=40)
+    rve.init()
+    recs = [rve.run_increment(step, 0, i) for i in range(3)]
+    worst = _check_records(recs, ro, TOL_MIXED, iterations=False)
+    print(f"64^3 mixed vs oracle: max rel P_av error {worst:.2e}")
+    rve.close()
+
+
+def _members(count=64):
+    """First 32^3 and first 48^3 member of the batched population."""
+    sizes = synthetic.batch_member_sizes(count)
+    return [synthetic.batch_member(sizes.index(c)) for c in (32, 48)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_members_32_48_vs_oracle(gpu, precision):
+    members = _members()
+    inc = 2
+    batch = gpu.Batch(len(members))
+    rves = []
+    for cells, ng, kind, mat, q in members:
+        r = gpu.RVE(cells, (1.0, 1.0, 1.0), mat, q, num=gpu.numerics(precision=precision))
+        rves.append((r, batch.add(r, [gpu.load_step(kind, t=float(inc), N=inc)])))
+    batch.run()
+    for (cells, ng, kind, mat, q), (r, slot) in zip(members, rves):
+        recs = batch.records(slot)
+        ro, fo = _oracle(cells, mat, q, [dgo.loadstep(kind, t=float(inc), N=inc)], ("F", "P", "Fp"))
+        if precision == "fp64":
+            _check_records(recs, ro, TOL)
+        else:
+            _check_records(recs, ro, TOL_MIXED, iterations=False)
+    batch.close()
+    for r, _ in rves:
+        r.close()
+
+
+def test_fft_forward_vs_numpy_benchmark_grids(gpu):
+    rng = np.random.default_rng(21)
+    for cells in [(48, 48, 48), (96, 96, 96), (128, 128, 128)]:
+        N0, N1, N2 = cells
+        rve = gpu.RVE(cells, (1, 1, 1), np.zeros(N0 * N1 * N2, int), [[1, 0, 0, 0]])
+        f = rng.standard_normal((N2, N1, N0, 3, 3))
+        spec = rve.fft_forward(f.reshape(-1, 3, 3))
+        ref = np.fft.rfftn(f, axes=(0, 1, 2))
+        assert rel(spec, np.transpose(ref, (1, 0, 2, 3, 4))) < 1e-13, cells
+        rve.close()
+
+
+def test_fft_prime_lengths_vs_numpy(gpu):
+    """Lengths with prime factors above 16 (FFTW plans any length, src/grid/fft.cpp:20-40)."""
+    rng = np.random.default_rng(22)
+    for cells in [(17, 6, 5), (19, 23, 3), (34, 7, 11), (6, 37, 4)]:
+        N0, N1, N2 = cells
+        rve = gpu.RVE(cells, (1, 1, 1), np.zeros(N0 * N1 * N2, int), [[1, 0, 0, 0]])
+        f = rng.standard_normal((N2, N1, N0, 3, 3))
+        spec = rve.fft_forward(f.reshape(-1, 3, 3))
+        ref = np.fft.rfftn(f, axes=(0, 1, 2))
+        assert rel(spec, np.transpose(ref, (1, 0, 2, 3, 4))) < 1e-13, cells
+        rve.close()
+
+
+def test_solver_prime_grid_vs_oracle(gpu):
+    """A 17 x 6 x 5 grid (prime factor 17) solved in both the device path and the oracle."""
+    cells = (17, 6, 5)
+    mat_at, q = synthetic.microstructure(cells, 5, 3)
+    size = (1.0, 6.0 / 17.0, 5.0 / 17.0)
+    rve = gpu.RVE(cells, size, mat_at, q)
+    recs = rve.loop_over_loadcase([gpu.load_step("tensionX", t=4.0, N=4)])
+    s = dgo.Solver(cells, size, mat_at, q)
+    ro = s.run([dgo.loadstep("tensionX", t=4.0, N=4)])
+    _check_records(recs, ro, TOL)
+    for key in ("F", "P", "Fp"):
+        assert rel(rve.get(key), dgo.from_fortran9(s.get(key))) < TOL, key
+    rve.close()
