@@ -103,6 +103,33 @@ int64_t dgx_rve_device_bytes(const dgx_rve* rve);
  * implementation evaluates whole RVEs: first must be 0 and count N. */
 dgx_status dgx_constitutive_response(dgx_rve* rve, const double* F, double dt, int32_t first, int32_t count,
                                      double* P, double* dPdF, int32_t* terminally_ill);
+/* Library-owned device fields in the reference layout, for a grid solver that keeps F,
+ * P and dPdF on the device.  Replaces f_homogenization_fetch_tensor_pointers
+ * (src/grid/spectral.h:17-19; homogenization.f90:491-510): F0 the committed deformation
+ * gradient (3,3,N), refreshed by every commit; F the deformation gradient (3,3,N) the
+ * caller writes before dgx_constitutive_response_fields; P (3,3,N) and dPdF
+ * (3,3,3,3,N, a[i+3j+9k+27l + 81*cell]; null unless requested) written by it;
+ * terminally_ill a device int32 (1: a cell failed), the reference's Fortran logical;
+ * stream the cudaStream_t the library works on (order your kernels on it, or
+ * synchronise).  All pointers are device pointers owned by the RVE (freed with it);
+ * the first call allocates them (F0 and F start as the committed F). */
+typedef struct dgx_field_ptrs {
+  int64_t n;
+  double* F0;
+  double* F;
+  double* P;
+  double* dPdF;
+  int32_t* terminally_ill;
+  void* stream;
+} dgx_field_ptrs;
+dgx_status dgx_fields(dgx_rve* rve, int32_t with_dPdF, dgx_field_ptrs* out);
+/* Constitutive response of the exported field F in place, no host copies of fields:
+ * P (and dPdF if want_dPdF) written to the exported buffers, terminally_ill set; P_av
+ * and the tangent averages available through dgx_averages.  Replaces
+ * f_homogenization_mechanical_response + _response2 as Spectral::constitutive_response
+ * calls them (src/grid/spectral.cpp:132-160).  Whole RVE only (first 0, count N);
+ * returns after the results are on the device. */
+dgx_status dgx_constitutive_response_fields(dgx_rve* rve, double dt, int32_t first, int32_t count, int32_t want_dPdF);
 /* Volume averages of the last response: replaces the reductions of
  * Spectral::constitutive_response (src/grid/spectral.cpp:160-217). */
 dgx_status dgx_averages(dgx_rve* rve, double P_av[9], double C_volAvg[81], double C_minMaxAvg[81]);
@@ -139,6 +166,20 @@ dgx_status dgx_fft_forward(dgx_rve* rve, const double* field, double* spectrum);
  * on the stream (the small FFT tables are staged from host memory first). */
 dgx_status dgx_divergence_rms_static(const int32_t cells[3], const double size[3], int32_t divergence_correction,
                                      int32_t derivative, const double* P_device, double* rms_device, void* stream);
+
+/* ---- Geometry input: VTK ImageData (.vti) content held in memory (host only).
+ * Replaces f_VTI_readCellsSizeOrigin (src/grid/discretization_grid.h:19-20): cells from
+ * WholeExtent, size = cells x Spacing, origin from Origin. */
+dgx_status dgx_vti_read_cells_size_origin(const char* content, int64_t length, int32_t cells[3], double size[3],
+                                          double origin[3]);
+/* Replaces f_VTI_readDataset_int (src/grid/discretization_grid.h:21-22): the integer
+ * cell-data array `label` (DAMASK: "material"), x fastest, into dataset.  On entry
+ * *dataset_size is the capacity of dataset, on return the number of values (N0*N1*N2);
+ * too small a capacity returns DGX_ERR_ARG with *dataset_size set to the count needed.
+ * ascii or inline base64 binary, raw or vtkZLibDataCompressor, UInt32/UInt64 headers,
+ * any integer element type within int32 range. */
+dgx_status dgx_vti_read_dataset_int(const char* content, int64_t length, const char* label, int32_t label_length,
+                                    int32_t* dataset, int64_t* dataset_size);
 
 /* Solver (MechSolverBasic + DamaskGrid, src/grid/mech_solver_basic.cpp, damask_grid.cpp) */
 dgx_status dgx_solver_init(dgx_rve* rve);                                   /* MechSolverBasic::init :19-108 */

@@ -16,7 +16,7 @@ from . import dgx as _d
 from .dgx import DgxError  # noqa: F401
 from .loadcase import load_step, parse_load_yaml, parse_numerics_yaml  # noqa: F401
 
-__all__ = ["RVE", "Batch", "Server", "footprint", "material", "numerics", "load_step", "DgxError"]
+__all__ = ["RVE", "Batch", "Server", "footprint", "material", "numerics", "load_step", "vti_read", "DgxError"]
 
 
 def material(**kw):
@@ -107,6 +107,21 @@ class RVE:
             # flat index i + 3j + 9k + 27l per cell -> array [cell][l][k][j][i]
             return Pn, np.transpose(d, (0, 4, 3, 2, 1))
         return Pn
+
+    def fields(self, with_dPdF=False):
+        """Library-owned device fields in the reference layout (dgx_fields): dict of
+        device pointers F0, F, P, dPdF (0 if not requested), terminally_ill, the stream
+        and the cell count n."""
+        fp = _d.FieldPtrs()
+        _d.check(_d.lib().dgx_fields(self.h, int(bool(with_dPdF)), C.byref(fp)), "dgx_fields")
+        return dict(n=fp.n, F0=fp.F0 or 0, F=fp.F or 0, P=fp.P or 0, dPdF=fp.dPdF or 0,
+                    terminally_ill=fp.terminally_ill or 0, stream=fp.stream or 0)
+
+    def constitutive_response_fields(self, dt, want_dPdF=False):
+        """Constitutive response of the exported device field F in place
+        (dgx_constitutive_response_fields); results in the exported P / dPdF."""
+        _d.check(_d.lib().dgx_constitutive_response_fields(self.h, float(dt), 0, self.N, int(bool(want_dPdF))),
+                 "dgx_constitutive_response_fields")
 
     def averages(self):
         P = np.zeros(9); Cv = np.zeros(81); Cm = np.zeros(81)
@@ -327,6 +342,20 @@ class Batch:
     @property
     def stream(self):
         return int(_d.lib().dgx_batch_stream(self.h) or 0)
+
+
+def vti_read(content, label="material"):
+    """(cells, size, origin, dataset) of VTI content through the library's reader
+    (dgx_vti_read_cells_size_origin / dgx_vti_read_dataset_int; host only)."""
+    b = content.encode() if isinstance(content, str) else bytes(content)
+    cells = (C.c_int32 * 3)(); size = (C.c_double * 3)(); origin = (C.c_double * 3)()
+    _d.check(_d.lib().dgx_vti_read_cells_size_origin(b, len(b), cells, size, origin), "dgx_vti_read_cells_size_origin")
+    n = C.c_int64(cells[0] * cells[1] * cells[2])
+    data = np.zeros(n.value, dtype=np.int32)
+    lb = label.encode()
+    _d.check(_d.lib().dgx_vti_read_dataset_int(b, len(b), lb, len(lb), data.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               C.byref(n)), "dgx_vti_read_dataset_int")
+    return np.array(cells[:]), np.array(size[:]), np.array(origin[:]), data[:n.value]
 
 
 def flop_model():

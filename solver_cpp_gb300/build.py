@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libdgx.so")
 SOURCES = ["constitutive.cu", "spectral.cu", "solver.cu", "peak.cu", "noalloc.cu", "batch.cu", "results.cu"]
-HOST_SOURCES = ["ref_stiffness.cpp", "server.cpp"]
+HOST_SOURCES = ["ref_stiffness.cpp", "server.cpp", "vti.cpp"]
 HEADERS = ["dgx_internal.cuh", "spectral.cuh", "rve.cuh", "h5lite.hpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

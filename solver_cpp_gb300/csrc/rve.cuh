@@ -39,6 +39,10 @@ struct dgx_rve {
   double* d_aos = nullptr;         // optional: 12 N doubles, device-side AoS staging of field reads
                                    // (allocated on the first read; not part of the creation footprint)
   double *d_un = nullptr, *d_up = nullptr, *d_Favg = nullptr;   // optional: coordinate update
+  // optional: library-owned fields in the reference layout (dgx_fields), allocated on
+  // the first dgx_fields call: F0 (committed F), F (written by the caller), P, dPdF
+  double *fx_F0 = nullptr, *fx_F = nullptr, *fx_P = nullptr, *fx_dPdF = nullptr;
+  int32_t* fx_ill = nullptr;
   dgx::BcBlock* d_bc = nullptr;    // stress BC of the current solve (device copy)
   int32_t* d_mat = nullptr;
   double* d_Rm = nullptr;

@@ -533,6 +533,10 @@ dgx_status commit(dgx_rve* r) {
   CK(cudaMemcpyAsync(r->ps.Lp0, r->ps.Lp, b9, cudaMemcpyDeviceToDevice, r->st));
   CK(cudaMemcpyAsync(r->ps.S0, r->ps.S, b9, cudaMemcpyDeviceToDevice, r->st));
   CK(cudaMemcpyAsync(r->ps.st0, r->ps.st, b24, cudaMemcpyDeviceToDevice, r->st));
+  if (r->fx_F0) {                     // exported committed F (dgx_fields), reference layout
+    k_planar2aos<<<nblk(9 * r->N), 256, 0, r->st>>>(r->ps.F0, r->N, 9, r->N, r->fx_F0);
+    r->n_launch++;
+  }
   return DGX_OK;
 }
 
@@ -765,6 +769,73 @@ extern "C" dgx_status dgx_constitutive_response(dgx_rve* r, const double* F, dou
     TRY(download_aos(r, r->d_dPdF, 81, dPdF));
   }
   if (terminally_ill) *terminally_ill = r->terminally_ill;
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_fields(dgx_rve* r, int32_t with_dPdF, dgx_field_ptrs* out) {
+  if (!r || !out) { set_err("dgx_fields: null argument"); return DGX_ERR_ARG; }
+  if (r->in_batch) { set_err("dgx_fields: the RVE is a batch member"); return DGX_ERR_STATE; }
+  const int64_t N = r->N;
+  if (!r->fx_F) {
+    double* ill = nullptr;
+    TRY(dalloc(r, &r->fx_F0, 9 * N));
+    TRY(dalloc(r, &r->fx_F, 9 * N));
+    TRY(dalloc(r, &r->fx_P, 9 * N));
+    TRY(dalloc(r, &ill, 1));
+    r->fx_ill = reinterpret_cast<int32_t*>(ill);
+    // F0 and F start as the committed deformation gradient, P as the last stress
+    k_planar2aos<<<nblk(9 * N), 256, 0, r->st>>>(r->ps.F0, N, 9, N, r->fx_F0);
+    k_planar2aos<<<nblk(9 * N), 256, 0, r->st>>>(r->ps.F0, N, 9, N, r->fx_F);
+    k_planar2aos<<<nblk(9 * N), 256, 0, r->st>>>(r->ps.P, N, 9, N, r->fx_P);
+    r->n_launch += 3;
+    CK(cudaMemsetAsync(r->fx_ill, 0, sizeof(int32_t), r->st));
+  }
+  if (with_dPdF && !r->fx_dPdF) {
+    TRY(dalloc(r, &r->fx_dPdF, 81 * N));
+    CK(cudaMemsetAsync(r->fx_dPdF, 0, sizeof(double) * 81 * N, r->st));
+  }
+  CK(cudaStreamSynchronize(r->st));
+  CK(cudaGetLastError());
+  out->n = N;
+  out->F0 = r->fx_F0;
+  out->F = r->fx_F;
+  out->P = r->fx_P;
+  out->dPdF = r->fx_dPdF;
+  out->terminally_ill = r->fx_ill;
+  out->stream = (void*)r->st;
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_constitutive_response_fields(dgx_rve* r, double dt, int32_t first, int32_t count,
+                                                       int32_t want_dPdF) {
+  if (!r) { set_err("null argument"); return DGX_ERR_ARG; }
+  if (!r->fx_F) { set_err("dgx_constitutive_response_fields: call dgx_fields first"); return DGX_ERR_STATE; }
+  if (r->in_batch) { set_err("dgx_constitutive_response_fields: the RVE is a batch member"); return DGX_ERR_STATE; }
+  if (first != 0 || count != r->N) { set_err("dgx_constitutive_response_fields: whole RVE only (first=0, count=N)"); return DGX_ERR_UNSUPPORTED; }
+  if (want_dPdF && !r->fx_dPdF) { set_err("dgx_constitutive_response_fields: dgx_fields was called without dPdF"); return DGX_ERR_STATE; }
+  const int64_t N = r->N;
+  // the caller's F (reference layout, library-owned) -> planes, on the RVE's stream
+  k_aos2planar<<<nblk(9 * N), 256, 0, r->st>>>(r->fx_F, 9, N, r->XA, N);
+  r->n_launch++;
+  r->terminally_ill = 0;
+  TRY(constitutive_response(r, r->XA, dt, true));
+  k_planar2aos<<<nblk(9 * N), 256, 0, r->st>>>(r->ps.P, N, 9, N, r->fx_P);
+  r->n_launch++;
+  if (want_dPdF) {
+    if (!r->d_dPdF) {
+      double* d = nullptr;
+      TRY(dalloc(r, &d, 81 * N));
+      r->d_dPdF = d;
+    }
+    launch_tangent(r->mp, r->ps, dt, r->d_dPdF, N, r->d_tpart, r->st);
+    launch_tangent_finish(r->d_tpart, r->nb_tan, r->wgt, r->d_Cvol, r->d_Cmm, r->st);
+    k_planar2aos<<<nblk(81 * N), 256, 0, r->st>>>(r->d_dPdF, N, 81, N, r->fx_dPdF);
+    r->n_launch += 3;
+  }
+  const int32_t ill = r->terminally_ill ? 1 : 0;
+  CK(cudaMemcpyAsync(r->fx_ill, &ill, sizeof(int32_t), cudaMemcpyHostToDevice, r->st));
+  CK(cudaStreamSynchronize(r->st));
+  CK(cudaGetLastError());
   return DGX_OK;
 }
 

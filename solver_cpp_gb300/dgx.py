@@ -77,7 +77,13 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_update_coords", "dgx_result_open", "dgx_result_add_setup", "dgx_result_write_increment",
            "dgx_result_close", "dgx_restart_write", "dgx_restart_read", "dgx_run_loadcase_output", "dgx_batch_tuning", "dgx_flop_model", "dgx_flop_model_mixed",
            "dgx_batch_set_round_points",
-           "dgx_server_set_round_points", "dgx_device_math"]
+           "dgx_server_set_round_points", "dgx_device_math", "dgx_fields", "dgx_constitutive_response_fields",
+           "dgx_vti_read_cells_size_origin", "dgx_vti_read_dataset_int"]
+
+
+class FieldPtrs(C.Structure):
+    _fields_ = [("n", C.c_int64), ("F0", C.c_void_p), ("F", C.c_void_p), ("P", C.c_void_p), ("dPdF", C.c_void_p),
+                ("terminally_ill", C.c_void_p), ("stream", C.c_void_p)]
 
 
 class DgxError(RuntimeError):
@@ -161,6 +167,10 @@ def lib():
     L.dgx_server_release.argtypes = [vp, C.c_int64]
     L.dgx_server_stats.argtypes = [vp, C.POINTER(ServerInfo)]
     L.dgx_divergence_rms_static.argtypes = [ip, dp, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.dgx_fields.argtypes = [vp, C.c_int32, C.POINTER(FieldPtrs)]
+    L.dgx_constitutive_response_fields.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, C.c_int32]
+    L.dgx_vti_read_cells_size_origin.argtypes = [C.c_char_p, C.c_int64, ip, dp, dp]
+    L.dgx_vti_read_dataset_int.argtypes = [C.c_char_p, C.c_int64, C.c_char_p, C.c_int32, ip, i64p]
     for name in SYMBOLS:
         f = getattr(L, name)
         if name not in ("dgx_material_default", "dgx_numerics_default", "dgx_rve_destroy", "dgx_last_error",

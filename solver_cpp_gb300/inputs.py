@@ -43,8 +43,14 @@ def _decode_binary(data, header_type, compressed, dtype):
     hfmt = "<I" if hsz == 4 else "<Q"
     data = re.sub(r"\s+", "", data)
     if not compressed:
-        n = struct.unpack(hfmt, base64.b64decode(data[:((hsz + 2) // 3) * 4])[:hsz])[0]
-        raw = base64.b64decode(data)[hsz:hsz + n]
+        # the byte-count header and the data are base64-encoded either as one stream or
+        # each on its own (then the header's encoding ends in '=' padding)
+        hchars = ((hsz + 2) // 3) * 4
+        n = struct.unpack(hfmt, base64.b64decode(data[:hchars])[:hsz])[0]
+        if "=" in data[:hchars]:
+            raw = base64.b64decode(data[hchars:])[:n]
+        else:
+            raw = base64.b64decode(data)[hsz:hsz + n]
         return np.frombuffer(raw, dtype=dtype)
     nb = struct.unpack(hfmt, base64.b64decode(data[:((hsz + 2) // 3) * 4])[:hsz])[0]
     hlen = hsz * (3 + nb)
