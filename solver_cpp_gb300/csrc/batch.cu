@@ -397,6 +397,7 @@ static std::string plan_signature(const RoundPlan& p) {
     s.put(L.nbx); s.put(L.nby); s.put(L.nbz); s.put(L.ndiv);
     const GammaArgs& a = g.ga;
     s.put(a.xi_x); s.put(a.xi_y); s.put(a.xi_z); s.raw(a.resc, sizeof(a.resc)); s.put(a.C_ref); s.put(a.aim);
+    s.put(a.fw[0]); s.put(a.fw[1]); s.put(a.fw[2]); s.raw(a.fw_h4, sizeof(a.fw_h4)); s.put(a.gtab);
     s.put(a.do_gamma); s.put(a.do_div); s.put(a.store_fwd); s.put(a.zsign); s.put(a.div_part);
     for (int k = 0; k < 3; ++k) {
       const AxisPlan& ap = g.r0->ax[k].plan;
@@ -618,7 +619,7 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
       for (int i : kv.second) {
         dgx_rve* r = q[i].r;
         SpecItem& it = e->h_spec[off++];
-        it.in = r->ps.P; it.out = q[i].out; it.spec = r->spec; it.C_ref = r->d_Cref; it.aim = e->d_aim + 9 * i;
+        it.in = r->ps.P; it.out = q[i].out; it.spec = r->spec; it.gtab = r->d_gtab; it.aim = e->d_aim + 9 * i;
         it.div_part = r->d_divpart; it.rms = e->d_rms + i;
       }
     }

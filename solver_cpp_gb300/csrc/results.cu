@@ -335,7 +335,8 @@ extern "C" dgx_status dgx_restart_read(dgx_rve* r, const char* path) {
   r->total_iter = iv[5];
   if (!need("solver/stress_mask", 9 * 4)) return DGX_ERR_ARG;
   memcpy(r->stress_mask, b.data(), sizeof(r->stress_mask));
-  CK(cudaMemcpy(r->d_Cref, r->C_ref, 81 * sizeof(double), cudaMemcpyHostToDevice));
+  TRY(set_reference_stiffness(r));
+  CK(cudaStreamSynchronize(r->st));
   r->tangent_fresh = false;
   r->initialized = true;
   return DGX_OK;

@@ -35,6 +35,8 @@ struct dgx_rve {
   int* d_ill = nullptr;
   dgx::ConsCounters* d_cnt = nullptr;
   double *d_xi_x = nullptr, *d_xi_y = nullptr, *d_xi_z = nullptr;
+  double* d_fw[3] = {nullptr, nullptr, nullptr};   // FWBW derivative: per-axis (D, E) factors
+  double* d_gtab = nullptr;        // K^-1 of C_ref per frequency (gamma_table), rebuilt with C_ref
   double* d_dPdF = nullptr;        // optional (81 planes) for the boundary call
   double* d_aos = nullptr;         // optional: 12 N doubles, device-side AoS staging of field reads
                                    // (allocated on the first read; not part of the creation footprint)
@@ -128,6 +130,9 @@ void solve_epilogue(dgx_rve* r, int reason, int32_t* conv, int32_t* iterations, 
 // volume average of F (the record of an increment)
 dgx_status field_average(dgx_rve* r, const double* X, double out[9]);
 GammaArgs gamma_args(dgx_rve* r, bool gamma, bool div);
+// upload r->C_ref (MechBase::update_gamma, mech_base.cpp:156-157) and rebuild the
+// per-frequency K^-1 table of the Gamma operator from it, on the RVE's stream
+dgx_status set_reference_stiffness(dgx_rve* r);
 void launch_axpy(double* z, const double* x, double a, const double* y, int64_t n, cudaStream_t st);
 void launch_combine(double* XA, const double* XM, const VecList& Xd, int l, double c0, const double* beta, int64_t n,
                     int nb, cudaStream_t st);

@@ -451,11 +451,23 @@ dgx_status ensure_tangent(dgx_rve* r) {
 GammaArgs gamma_args(dgx_rve* r, bool gamma, bool div) {
   GammaArgs ga{};
   ga.xi_x = r->d_xi_x; ga.xi_y = r->d_xi_y; ga.xi_z = r->d_xi_z;
-  for (int i = 0; i < 3; ++i) ga.resc[i] = r->geom[i] / r->scaled[i];
-  ga.C_ref = r->d_Cref; ga.aim = r->d_aim;
+  for (int i = 0; i < 3; ++i) {
+    ga.resc[i] = r->geom[i] / r->scaled[i];
+    ga.fw[i] = r->d_fw[i];
+    ga.fw_h4[i] = 4.0 * r->geom[i] / r->cells[i];
+  }
+  ga.C_ref = r->d_Cref; ga.gtab = r->d_gtab; ga.aim = r->d_aim;
   ga.do_gamma = gamma; ga.do_div = div; ga.store_fwd = 0;
   ga.div_part = r->d_divpart;
   return ga;
+}
+
+dgx_status set_reference_stiffness(dgx_rve* r) {
+  CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
+  gamma_table(r->sl.g, r->num.precision == 1, gamma_args(r, true, false), r->d_gtab, r->st);
+  r->n_launch++;
+  CK(cudaGetLastError());
+  return DGX_OK;
 }
 
 int converged(dgx_rve* r) {
@@ -474,7 +486,7 @@ dgx_status solve_prologue(dgx_rve* r) {
   masked_compliance(r->C_volAvg, r->rot_q, r->stress_mask, r->S);
   if (r->num.update_gamma) {
     for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
-    CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
+    TRY(set_reference_stiffness(r));
   }
   // the BC state the device updates during the solve (same values as the host copy)
   BcBlock bc;
@@ -645,6 +657,10 @@ static dgx_status allocate_buffers(dgx_rve* r, const int32_t cells[3], const dgx
   AL(&r->d_Pav, 9); AL(&r->d_Cvol, 81); AL(&r->d_Cmm, 81); AL(&r->d_Cref, 81); AL(&r->d_aim, 9); AL(&r->d_rms, 1);
   AL(&r->d_ill, 1); AL(&r->d_cnt, 1);
   AL(&r->d_xi_x, cells[0] / 2 + 1); AL(&r->d_xi_y, cells[1]); AL(&r->d_xi_z, cells[2]);
+  if (num->derivative == 2) {
+    AL(&r->d_fw[0], 4 * (cells[0] / 2 + 1)); AL(&r->d_fw[1], 4 * cells[1]); AL(&r->d_fw[2], 4 * cells[2]);
+  }
+  AL(&r->d_gtab, (gamma_table_bytes(r->sl.g, fp32, num->derivative == 2) + 7) / 8);
   AL(&r->d_mat, N); AL(&r->d_Rm, 9 * (int64_t)n_materials);
 #undef AL
   return DGX_OK;
@@ -657,7 +673,8 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
     set_err("dgx_rve_create: null argument"); return DGX_ERR_ARG;
   }
   for (int i = 0; i < 3; ++i) if (cells[i] < 1 || !(size[i] > 0.0)) { set_err("dgx_rve_create: bad cells/size"); return DGX_ERR_ARG; }
-  if (num->derivative == 2) { set_err("FWBW_difference derivative is not implemented on the device path"); return DGX_ERR_UNSUPPORTED; }
+  if (num->derivative < 0 || num->derivative > 2) { set_err("derivative must be 0, 1 or 2"); return DGX_ERR_ARG; }
+  if (num->divergence_correction < 0 || num->divergence_correction > 2) { set_err("divergence_correction must be 0, 1 or 2"); return DGX_ERR_ARG; }
   if (num->ngmres_m < 1 || num->ngmres_m > 30) { set_err("ngmres_m must be in [1, 30]"); return DGX_ERR_ARG; }
   for (int i = 0; i < 3; ++i) if (cells[i] > 4096) { set_err("cells > 4096"); return DGX_ERR_ARG; }
   dgx_rve* r = new dgx_rve();
@@ -701,9 +718,15 @@ extern "C" dgx_status dgx_rve_create(const int32_t cells[3], const double size[3
     double* dst[3] = {r->d_xi_x, r->d_xi_y, r->d_xi_z};
     for (int p = 0; p < 3; ++p) {
       std::vector<double> v;
-      xi_axis(p, cells, size, num->derivative, v);
+      xi_axis(p, cells, size, num->derivative == 2 ? 0 : num->derivative, v);
       if (cudaMemcpy(dst[p], v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
         set_err("xi upload failed"); dgx_rve_destroy(r); return DGX_ERR_CUDA;
+      }
+      if (num->derivative == 2) {
+        fw_axis(p, cells, v);
+        if (cudaMemcpy(r->d_fw[p], v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+          set_err("xi upload failed"); dgx_rve_destroy(r); return DGX_ERR_CUDA;
+        }
       }
     }
   }
@@ -858,7 +881,7 @@ extern "C" dgx_status dgx_commit_increment(dgx_rve* r) {
 extern "C" dgx_status dgx_update_gamma(dgx_rve* r, const double C[81]) {
   if (!r || !C) return DGX_ERR_ARG;
   for (int k = 0; k < 81; ++k) r->C_ref[k] = C[k] / r->wgt;
-  CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
+  TRY(set_reference_stiffness(r));
   return DGX_OK;
 }
 
@@ -933,7 +956,7 @@ extern "C" dgx_status dgx_solver_init(dgx_rve* r) {
     set_err("reference stiffness selection failed"); return DGX_ERR_STATE;
   }
   for (int k = 0; k < 81; ++k) r->C_ref[k] = r->C_minMaxAvg[k] / r->wgt;
-  CK(h2d(r, r->d_Cref, r->C_ref, 81 * sizeof(double)));
+  TRY(set_reference_stiffness(r));
   memcpy(r->C_minMaxAvgLastInc, r->C_minMaxAvg, sizeof(r->C_minMaxAvg));
   memcpy(r->C_volAvgLastInc, r->C_volAvg, sizeof(r->C_volAvg));
   r->initialized = true;
@@ -1046,7 +1069,8 @@ dgx_status dgx::update_coords_impl(dgx_rve* r, double* u_n, double* u_p) {
     TRY(dalloc(r, &r->d_Favg, 9));
   }
   spec_update_coords(r->sl, r->num.precision == 1, r->ax[0].plan, r->ax[1].plan, r->ax[2].plan, r->X, r->N, r->spec,
-                     r->XA, r->geom, r->num.derivative, r->wgt, r->d_Favg, r->d_un, r->d_up, r->st);
+                     r->XA, r->geom, r->num.derivative, gamma_args(r, false, false), r->wgt, r->d_Favg, r->d_un,
+                     r->d_up, r->st);
   r->n_launch += 8;
   if (u_n) CK(d2h(r, u_n, r->d_un, sizeof(double) * 3 * Nn));
   if (u_p) CK(d2h(r, u_p, r->d_up, sizeof(double) * 3 * r->N));

@@ -249,29 +249,166 @@ __global__ void k_ypass(SpecGeom g, AxisPlan py, typename cpx<R>::t* __restrict_
 
 // ---------------------------------------------------------------- z pass + Gamma + div
 
-// 2 blocks of 256 threads per SM (register cap 128): the per-frequency Gamma work
-// otherwise takes every register and leaves one block per SM
-template <typename R>
+// xi of one frequency for the forward/backward difference: xi_p = D_p E_q E_r / (4 h_p)
+// (q, r the next two axes, cyclically), the complex factors from the per-axis tables
+__device__ __forceinline__ void fw_xi(const GammaArgs& ga, int ix, int y, int z, double2 xi[3]) {
+  const double* t[3] = {ga.fw[0] + 4 * ix, ga.fw[1] + 4 * y, ga.fw[2] + 4 * z};
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const double* a = t[p];
+    const double* b = t[(p + 1) % 3];
+    const double* c = t[(p + 2) % 3];
+    const double abr = a[0] * b[2] - a[1] * b[3], abi = a[0] * b[3] + a[1] * b[2];
+    const double xr = abr * c[2] - abi * c[3], xim = abr * c[3] + abi * c[2];
+    xi[p] = make_double2(xr / ga.fw_h4[p], xim / ga.fw_h4[p]);
+  }
+}
+
+// Number of entries per frequency of the Gamma table.
+__host__ __device__ constexpr int gtab_entries(bool fp32, bool fw) { return fw ? 18 : (fp32 ? 6 : 9); }
+
+// K^-1(xi) per half-spectrum frequency (the spectral operator's only dependence on the
+// reference stiffness), evaluated once per reference-stiffness update.  Continuous and
+// central derivative: xi = i a (a real), K_lm = -sum_no C_ref(l,n,m,o) a_n a_o real;
+// |det K| <= 1e-16 (and xi = 0) gives a zero operator.  FWBW: K_lm = sum_no
+// C_ref(l,n,m,o) conj(-xi_n) xi_o (Hermitian), the determinant test on Re K, and the
+// operator uses the inverse of conj(K), as the real 6x6 form [[Re K, Im K],
+// [-Im K, Re K]] of the reference's update_gamma (mech_base.cpp:164-205) inverts it.
+template <typename R, bool FW>
+__global__ void k_gamma_table(SpecGeom g, GammaArgs ga, R* __restrict__ tab) {
+  __shared__ double s_C[81];
+  for (int k = threadIdx.x; k < 81; k += blockDim.x) s_C[k] = ga.C_ref[k];
+  __syncthreads();                      // every thread of the block reaches this barrier
+  const long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (f >= g.Nh) return;
+  const int z = (int)(f % g.N2);
+  const long long xy = f / g.N2;
+  const int ix = (int)(xy % g.N0r), y = (int)(xy / g.N0r);
+  constexpr int NE = gtab_entries(sizeof(R) == 4, FW);
+  R out[NE];
+#pragma unroll
+  for (int k = 0; k < NE; ++k) out[k] = R(0);
+  if constexpr (!FW) {
+    const double av[3] = {ga.xi_x[ix], ga.xi_y[y], ga.xi_z[z]};
+    double K[9];
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        double s = 0.0;
+#pragma unroll
+        for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+          for (int o = 0; o < 3; ++o) s = fma(s_C[l + 3 * nn + 9 * m + 27 * o], av[nn] * av[o], s);
+        K[l + 3 * m] = -s;
+      }
+    double c0 = K[4] * K[8] - K[7] * K[5], c1 = -K[1] * K[8] + K[7] * K[2], c2 = K[1] * K[5] - K[4] * K[2];
+    double det = K[0] * c0 + K[3] * c1 + K[6] * c2;
+    if (f != 0 && fabs(det) > 1e-16) {
+      double r = 1.0 / det;
+      double Ki[9] = {c0 * r, c1 * r, c2 * r,
+                      (-K[3] * K[8] + K[6] * K[5]) * r, (K[0] * K[8] - K[6] * K[2]) * r, (-K[0] * K[5] + K[3] * K[2]) * r,
+                      (K[3] * K[7] - K[6] * K[4]) * r, (-K[0] * K[7] + K[6] * K[1]) * r, (K[0] * K[4] - K[3] * K[1]) * r};
+      if constexpr (sizeof(R) == 8) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) out[k] = Ki[k];
+      } else {
+        // symmetric: 00 11 22 01 02 12
+        out[0] = (R)Ki[0]; out[1] = (R)Ki[4]; out[2] = (R)Ki[8];
+        out[3] = (R)Ki[3]; out[4] = (R)Ki[6]; out[5] = (R)Ki[7];
+      }
+    }
+  } else {
+    double2 xi[3];
+    fw_xi(ga, ix, y, z, xi);
+    // dyad(n, o) = conj(-xi_n) xi_o
+    double dr[9], di[9];
+#pragma unroll
+    for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+      for (int o = 0; o < 3; ++o) {
+        const double ar = -xi[nn].x, ai = xi[nn].y;     // conj(-xi_n)
+        dr[nn + 3 * o] = ar * xi[o].x - ai * xi[o].y;
+        di[nn + 3 * o] = ar * xi[o].y + ai * xi[o].x;
+      }
+    double Kr[9], Kim[9];
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        double sr = 0.0, si = 0.0;
+#pragma unroll
+        for (int nn = 0; nn < 3; ++nn)
+#pragma unroll
+          for (int o = 0; o < 3; ++o) {
+            const double c = s_C[l + 3 * nn + 9 * m + 27 * o];
+            sr = fma(c, dr[nn + 3 * o], sr);
+            si = fma(c, di[nn + 3 * o], si);
+          }
+        Kr[l + 3 * m] = sr; Kim[l + 3 * m] = si;
+      }
+    const double detr = Kr[0] * (Kr[4] * Kr[8] - Kr[7] * Kr[5]) - Kr[3] * (Kr[1] * Kr[8] - Kr[7] * Kr[2]) +
+                        Kr[6] * (Kr[1] * Kr[5] - Kr[4] * Kr[2]);
+    if (f != 0 && fabs(detr) > 1e-16) {
+      // M = conj(K): complex adjugate over the complex determinant
+      double Mr[9], Mi[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) { Mr[k] = Kr[k]; Mi[k] = -Kim[k]; }
+      auto cm = [](double ar, double ai, double br, double bi, double& r, double& i) { r = ar * br - ai * bi; i = ar * bi + ai * br; };
+      // cofactor C(i,j) of M, stored as adj(j,i)
+      double Ar[9], Ai[9];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+          double pr, pi, qr, qi;
+          cm(Mr[i1 + 3 * j1], Mi[i1 + 3 * j1], Mr[i2 + 3 * j2], Mi[i2 + 3 * j2], pr, pi);
+          cm(Mr[i1 + 3 * j2], Mi[i1 + 3 * j2], Mr[i2 + 3 * j1], Mi[i2 + 3 * j1], qr, qi);
+          Ar[j + 3 * i] = pr - qr; Ai[j + 3 * i] = pi - qi;
+        }
+      double dr_ = 0.0, di_ = 0.0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {       // det = sum_j M(0,j) C(0,j) = sum_j M(0,j) adj(j,0)
+        double pr, pi;
+        cm(Mr[3 * j], Mi[3 * j], Ar[j], Ai[j], pr, pi);
+        dr_ += pr; di_ += pi;
+      }
+      const double n2 = dr_ * dr_ + di_ * di_;
+      const double ir = dr_ / n2, ii = -di_ / n2;          // 1 / det
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        double r, i;
+        cm(Ar[k], Ai[k], ir, ii, r, i);
+        out[2 * k] = (R)r; out[2 * k + 1] = (R)i;
+      }
+    }
+  }
+  const long long gi = ((long long)y * g.N0r + ix) * g.N2 + z;
+#pragma unroll
+  for (int k = 0; k < NE; ++k) tab[k * g.Nh + gi] = out[k];
+}
+
+// 2 blocks of 256 threads per SM (register cap 128)
+template <typename R, bool FW>
 __global__ void __launch_bounds__(256, 2) k_zpass(SpecGeom g, AxisPlan pz, typename cpx<R>::t* __restrict__ spec, int TI, GammaArgs ga,
                         const SpecItem* __restrict__ items) {
   typedef typename cpx<R>::t C;
   if (items) {
     const SpecItem& it = items[blockIdx.y];
-    spec = (C*)it.spec; ga.C_ref = it.C_ref; ga.aim = it.aim; ga.div_part = it.div_part;
+    spec = (C*)it.spec; ga.gtab = it.gtab; ga.aim = it.aim; ga.div_part = it.div_part;
   }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int per = TI * g.N2;                       // lines x length per component
   C* a = reinterpret_cast<C*>(smem_raw);
   C* b = a + 9L * per;
   double* s_val = reinterpret_cast<double*>(b + 9L * per);   // weighted |div|^2 per frequency of the tile
-  __shared__ double s_C[81];
   const int ntile = (g.N0r + TI - 1) / TI;
   const int tile = blockIdx.x % ntile;
   const int y = blockIdx.x / ntile;
   const int i0 = tile * TI;
   const int ti = min(TI, g.N0r - i0);
   const long long zs = (long long)g.N1 * g.N0r;
-  for (int k = threadIdx.x; k < 81; k += blockDim.x) s_C[k] = ga.do_gamma ? ga.C_ref[k] : 0.0;
   // load: line (c, i) at a + (c*ti + i) * N2
   for (int t = threadIdx.x; t < 9 * ti * g.N2; t += blockDim.x) {
     int c = t / (ti * g.N2), rem = t - c * ti * g.N2;
@@ -281,68 +418,108 @@ __global__ void __launch_bounds__(256, 2) k_zpass(SpecGeom g, AxisPlan pz, typen
   __syncthreads();
   C* res = block_fft<R>(a, b, 9 * ti, pz, (ga.store_fwd && !ga.do_gamma && ga.zsign > 0) ? +1 : -1);
   C* other = (res == a) ? b : a;
+  const R* gt = reinterpret_cast<const R*>(ga.gtab);
   for (int t = threadIdx.x; (ga.do_div || ga.do_gamma) && t < ti * g.N2; t += blockDim.x) {
     int i = t / g.N2, z = t - i * g.N2;
     int ix = i0 + i;
-    double ax = ga.xi_x[ix], ay = ga.xi_y[y], az = ga.xi_z[z];
     C Ph[9];
 #pragma unroll
     for (int c = 0; c < 9; ++c) Ph[c] = res[((long)c * ti + i) * g.N2 + z];
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    double2 xi[3];
+    if constexpr (FW) fw_xi(ga, ix, y, z, xi);
+    else { ax = ga.xi_x[ix]; ay = ga.xi_y[y]; az = ga.xi_z[z]; }
     if (ga.do_div) {
       double wgt = (ix == 0 ? 1.0 : 0.0) + (ix == g.N0r - 1 ? 1.0 : 0.0) + ((ix > 0 && ix < g.N0r - 1) ? 2.0 : 0.0);
-      double bx = ax * ga.resc[0], by = ay * ga.resc[1], bz = az * ga.resc[2];
       double s = 0.0;
+      if constexpr (!FW) {
+        double bx = ax * ga.resc[0], by = ay * ga.resc[1], bz = az * ga.resc[2];
 #pragma unroll
-      for (int l = 0; l < 3; ++l) {
-        double ur = (double)Ph[l].x * bx + (double)Ph[l + 3].x * by + (double)Ph[l + 6].x * bz;
-        double ui = (double)Ph[l].y * bx + (double)Ph[l + 3].y * by + (double)Ph[l + 6].y * bz;
-        s += ur * ur + ui * ui;
+        for (int l = 0; l < 3; ++l) {
+          double ur = (double)Ph[l].x * bx + (double)Ph[l + 3].x * by + (double)Ph[l + 6].x * bz;
+          double ui = (double)Ph[l].y * bx + (double)Ph[l + 3].y * by + (double)Ph[l + 6].y * bz;
+          s += ur * ur + ui * ui;
+        }
+      } else {
+        // prod_l = sum_n P(l, n) conj(-xi_n) resc_n
+        double vr[3], vi[3];
+#pragma unroll
+        for (int nn = 0; nn < 3; ++nn) { vr[nn] = -xi[nn].x * ga.resc[nn]; vi[nn] = xi[nn].y * ga.resc[nn]; }
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          double pr = 0.0, pi = 0.0;
+#pragma unroll
+          for (int nn = 0; nn < 3; ++nn) {
+            const double xr = (double)Ph[l + 3 * nn].x, xim = (double)Ph[l + 3 * nn].y;
+            pr += xr * vr[nn] - xim * vi[nn];
+            pi += xr * vi[nn] + xim * vr[nn];
+          }
+          s += pr * pr + pi * pi;
+        }
       }
       s_val[t] = wgt * s;
     }
     if (ga.do_gamma) {
       C out[9];
+      const long long gi = ((long long)y * g.N0r + ix) * g.N2 + z;
       if (ix == 0 && y == 0 && z == 0) {
 #pragma unroll
         for (int c = 0; c < 9; ++c) { out[c].x = (R)ga.aim[c]; out[c].y = 0; }
+      } else if constexpr (!FW) {
+        // Gamma:P with K^-1 from the table, in the spectrum's precision:
+        // v(n) = sum_o a_o P(n,o); w(l) = sum_n Kinv(l,n) v(n); out(l,m) = -a_m w(l)
+        R Ki[9];
+        if constexpr (sizeof(R) == 8) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Ki[k] = gt[k * g.Nh + gi];
+        } else {
+          const R k00 = gt[gi], k11 = gt[g.Nh + gi], k22 = gt[2 * g.Nh + gi];
+          const R k01 = gt[3 * g.Nh + gi], k02 = gt[4 * g.Nh + gi], k12 = gt[5 * g.Nh + gi];
+          Ki[0] = k00; Ki[4] = k11; Ki[8] = k22; Ki[1] = Ki[3] = k01; Ki[2] = Ki[6] = k02; Ki[5] = Ki[7] = k12;
+        }
+        const R av[3] = {(R)ax, (R)ay, (R)az};
+        R vr[3], vi[3];
+#pragma unroll
+        for (int nn = 0; nn < 3; ++nn) {
+          vr[nn] = av[0] * Ph[nn].x + av[1] * Ph[nn + 3].x + av[2] * Ph[nn + 6].x;
+          vi[nn] = av[0] * Ph[nn].y + av[1] * Ph[nn + 3].y + av[2] * Ph[nn + 6].y;
+        }
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          R wr = Ki[l] * vr[0] + Ki[l + 3] * vr[1] + Ki[l + 6] * vr[2];
+          R wi = Ki[l] * vi[0] + Ki[l + 3] * vi[1] + Ki[l + 6] * vi[2];
+#pragma unroll
+          for (int m = 0; m < 3; ++m) { out[l + 3 * m].x = -av[m] * wr; out[l + 3 * m].y = -av[m] * wi; }
+        }
       } else {
-        double av[3] = {ax, ay, az};
-        double K[9];
+        // complex: v(n) = sum_o conj(-xi_o) P(n,o); w(l) = sum_n N(l,n) v(n); out(l,m) = xi_m w(l)
+        R vr[3], vi[3];
 #pragma unroll
-        for (int l = 0; l < 3; ++l)
+        for (int nn = 0; nn < 3; ++nn) {
+          R sr = 0, si = 0;
 #pragma unroll
-          for (int m = 0; m < 3; ++m) {
-            double s = 0.0;
-#pragma unroll
-            for (int nn = 0; nn < 3; ++nn)
-#pragma unroll
-              for (int o = 0; o < 3; ++o) s = fma(s_C[l + 3 * nn + 9 * m + 27 * o], av[nn] * av[o], s);
-            K[l + 3 * m] = -s;
+          for (int o = 0; o < 3; ++o) {
+            const R cr = (R)(-xi[o].x), ci = (R)xi[o].y;          // conj(-xi_o)
+            sr += cr * Ph[nn + 3 * o].x - ci * Ph[nn + 3 * o].y;
+            si += cr * Ph[nn + 3 * o].y + ci * Ph[nn + 3 * o].x;
           }
-        double c0 = K[4] * K[8] - K[7] * K[5], c1 = -K[1] * K[8] + K[7] * K[2], c2 = K[1] * K[5] - K[4] * K[2];
-        double det = K[0] * c0 + K[3] * c1 + K[6] * c2;
-        if (fabs(det) > 1e-16) {
-          double r = 1.0 / det;
-          double Ki[9] = {c0 * r, c1 * r, c2 * r,
-                          (-K[3] * K[8] + K[6] * K[5]) * r, (K[0] * K[8] - K[6] * K[2]) * r, (-K[0] * K[5] + K[3] * K[2]) * r,
-                          (K[3] * K[7] - K[6] * K[4]) * r, (-K[0] * K[7] + K[6] * K[1]) * r, (K[0] * K[4] - K[3] * K[1]) * r};
-          // v(n) = sum_o a_o P(n,o); w(l) = sum_n Kinv(l,n) v(n); out(l,m) = -a_m w(l)
-          double vr[3], vi[3];
+          vr[nn] = sr; vi[nn] = si;
+        }
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          R wr = 0, wi = 0;
 #pragma unroll
           for (int nn = 0; nn < 3; ++nn) {
-            vr[nn] = ax * (double)Ph[nn].x + ay * (double)Ph[nn + 3].x + az * (double)Ph[nn + 6].x;
-            vi[nn] = ax * (double)Ph[nn].y + ay * (double)Ph[nn + 3].y + az * (double)Ph[nn + 6].y;
+            const R nr = gt[(2 * (l + 3 * nn)) * g.Nh + gi], ni = gt[(2 * (l + 3 * nn) + 1) * g.Nh + gi];
+            wr += nr * vr[nn] - ni * vi[nn];
+            wi += nr * vi[nn] + ni * vr[nn];
           }
 #pragma unroll
-          for (int l = 0; l < 3; ++l) {
-            double wr = Ki[l] * vr[0] + Ki[l + 3] * vr[1] + Ki[l + 6] * vr[2];
-            double wi = Ki[l] * vi[0] + Ki[l + 3] * vi[1] + Ki[l + 6] * vi[2];
-#pragma unroll
-            for (int m = 0; m < 3; ++m) { out[l + 3 * m].x = (R)(-av[m] * wr); out[l + 3 * m].y = (R)(-av[m] * wi); }
+          for (int m = 0; m < 3; ++m) {
+            const R xr = (R)xi[m].x, xim = (R)xi[m].y;
+            out[l + 3 * m].x = xr * wr - xim * wi;
+            out[l + 3 * m].y = xr * wi + xim * wr;
           }
-        } else {
-#pragma unroll
-          for (int c = 0; c < 9; ++c) { out[c].x = 0; out[c].y = 0; }
         }
       }
 #pragma unroll
@@ -380,12 +557,13 @@ __global__ void __launch_bounds__(256, 2) k_zpass(SpecGeom g, AxisPlan pz, typen
 }
 
 // ---------------------------------------------------------------- coordinates
-// per half-spectrum frequency: u^ = F^ xi2nd / sum conj(-xi2nd) xi2nd (xi2nd = i a,
-// purely imaginary for the continuous and central derivatives: u^_l = -i (F^ a)_l / |a|^2),
-// zero at the zero frequency, whose real part gives Favg; components 3..8 cleared
+// per half-spectrum frequency: u^ = F^ xi2nd / sum conj(-xi2nd) xi2nd, zero at the zero
+// frequency (whose real part gives Favg) and where xi2nd = 0; components 3..8 cleared.
+// Continuous and central derivative: xi2nd = i a purely imaginary, u^_l = -i (F^ a)_l / |a|^2;
+// FWBW: xi2nd complex from the per-axis factor tables (ga.fw), u^_l = -(F^ xi)_l / |xi|^2.
 template <typename R>
 __global__ void k_coords_freq(SpecGeom g, typename cpx<R>::t* __restrict__ spec, double s0, double s1, double s2,
-                              int derivative, double wgt, double* __restrict__ Favg) {
+                              int derivative, GammaArgs ga, double wgt, double* __restrict__ Favg) {
   typedef typename cpx<R>::t C;
   const long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (f >= g.Nh) return;
@@ -393,15 +571,6 @@ __global__ void k_coords_freq(SpecGeom g, typename cpx<R>::t* __restrict__ spec,
   const int i = (int)(f % g.N0r);
   const long long yz = f / g.N0r;
   const int y = (int)(yz % g.N1), z = (int)(yz / g.N1);
-  const int k[3] = {i, y > g.N1 / 2 ? y - g.N1 : y, z > g.N2 / 2 ? z - g.N2 : z};
-  const int n[3] = {g.N0, g.N1, g.N2};
-  const double sz[3] = {s0, s1, s2};
-  double a[3], a2 = 0.0;
-#pragma unroll
-  for (int p = 0; p < 3; ++p) {
-    a[p] = derivative == 0 ? TAU * k[p] / sz[p] : sin(TAU * k[p] / n[p]) / (2.0 * sz[p] / n[p]);
-    a2 += a[p] * a[p];
-  }
   C Fh[9];
 #pragma unroll
   for (int c = 0; c < 9; ++c) Fh[c] = spec[c * g.Nh + f];
@@ -410,15 +579,44 @@ __global__ void k_coords_freq(SpecGeom g, typename cpx<R>::t* __restrict__ spec,
     for (int c = 0; c < 9; ++c) Favg[c] = (double)Fh[c].x * wgt;
   }
   C out[3];
+  if (derivative == 2) {
+    double2 xi[3];
+    fw_xi(ga, i, y, z, xi);
+    const double a2 = xi[0].x * xi[0].x + xi[0].y * xi[0].y + xi[1].x * xi[1].x + xi[1].y * xi[1].y +
+                      xi[2].x * xi[2].x + xi[2].y * xi[2].y;
+    const bool zero = (f == 0) || !(a2 > 0.0);
 #pragma unroll
-  for (int l = 0; l < 3; ++l) {
-    double nr = 0.0, ni = 0.0;
+    for (int l = 0; l < 3; ++l) {
+      double nr = 0.0, ni = 0.0;
 #pragma unroll
-    for (int m = 0; m < 3; ++m) { nr += (double)Fh[l + 3 * m].x * a[m]; ni += (double)Fh[l + 3 * m].y * a[m]; }
-    // -i (nr + i ni) / a2 = (ni - i nr) / a2
-    bool zero = (f == 0) || !(a2 > 0.0);
-    out[l].x = zero ? (R)0 : (R)(ni / a2);
-    out[l].y = zero ? (R)0 : (R)(-nr / a2);
+      for (int m = 0; m < 3; ++m) {
+        const double fr = (double)Fh[l + 3 * m].x, fi = (double)Fh[l + 3 * m].y;
+        nr += fr * xi[m].x - fi * xi[m].y;
+        ni += fr * xi[m].y + fi * xi[m].x;
+      }
+      out[l].x = zero ? (R)0 : (R)(-nr / a2);
+      out[l].y = zero ? (R)0 : (R)(-ni / a2);
+    }
+  } else {
+    const int k[3] = {i, y > g.N1 / 2 ? y - g.N1 : y, z > g.N2 / 2 ? z - g.N2 : z};
+    const int n[3] = {g.N0, g.N1, g.N2};
+    const double sz[3] = {s0, s1, s2};
+    double a[3], a2 = 0.0;
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+      a[p] = derivative == 0 ? TAU * k[p] / sz[p] : sin(TAU * k[p] / n[p]) / (2.0 * sz[p] / n[p]);
+      a2 += a[p] * a[p];
+    }
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+      double nr = 0.0, ni = 0.0;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) { nr += (double)Fh[l + 3 * m].x * a[m]; ni += (double)Fh[l + 3 * m].y * a[m]; }
+      // -i (nr + i ni) / a2 = (ni - i nr) / a2
+      bool zero = (f == 0) || !(a2 > 0.0);
+      out[l].x = zero ? (R)0 : (R)(ni / a2);
+      out[l].y = zero ? (R)0 : (R)(-nr / a2);
+    }
   }
 #pragma unroll
   for (int c = 0; c < 9; ++c) {
@@ -670,7 +868,8 @@ static bool set_smem_limits(const SpecLaunch& L) {
   std::array<size_t, 3>& m = lim[dev];
   bool ok = true;
   if (L.smz > m[2]) {
-    ok &= cudaFuncSetAttribute(k_zpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smz) == cudaSuccess;
+    ok &= cudaFuncSetAttribute(k_zpass<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smz) == cudaSuccess;
+    ok &= cudaFuncSetAttribute(k_zpass<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smz) == cudaSuccess;
     if (ok) m[2] = L.smz;
   }
   if (L.smy > m[1]) {
@@ -701,7 +900,8 @@ static void convolve_impl(const SpecLaunch& L, const AxisPlan& px, const AxisPla
   const unsigned ny = items ? (unsigned)nitems : 1u;
   k_xfwd<R, double><<<dim3(L.nbx, ny), 256, L.smx, st>>>(L.g, px, in, ld, (C*)spec, L.LX, items);
   k_ypass<R><<<dim3(L.nby, ny), 256, L.smy, st>>>(L.g, py, (C*)spec, L.TIy, -1, items);
-  k_zpass<R><<<dim3(L.nbz, ny), 256, L.smz, st>>>(L.g, pz, (C*)spec, L.TIz, ga, items);
+  if (ga.fw[0]) k_zpass<R, true><<<dim3(L.nbz, ny), 256, L.smz, st>>>(L.g, pz, (C*)spec, L.TIz, ga, items);
+  else k_zpass<R, false><<<dim3(L.nbz, ny), 256, L.smz, st>>>(L.g, pz, (C*)spec, L.TIz, ga, items);
   if (ga.do_gamma) {
     k_ypass<R><<<dim3(L.nby, ny), 256, L.smy, st>>>(L.g, py, (C*)spec, L.TIy, +1, items);
     k_xinv<R, double><<<dim3(L.nbx, ny), 256, L.smx, st>>>(L.g, px, (const C*)spec, field, ld, L.LX, items);
@@ -722,7 +922,8 @@ void spec_convolve_batch(const SpecLaunch& L, bool fp32, const AxisPlan& px, con
 
 void spec_update_coords(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                         const double* F, long long ld, void* spec, double* scratch, const double size[3],
-                        int derivative, double wgt, double* Favg, double* u_n, double* u_p, cudaStream_t st) {
+                        int derivative, const GammaArgs& xi, double wgt, double* Favg, double* u_n, double* u_p,
+                        cudaStream_t st) {
   GammaArgs ga{};
   ga.store_fwd = 1; ga.zsign = -1;
   const SpecGeom& g = L.g;
@@ -731,22 +932,52 @@ void spec_update_coords(const SpecLaunch& L, bool fp32, const AxisPlan& px, cons
   if (fp32) {
     typedef float2 C;
     convolve_impl<float>(L, px, py, pz, F, nullptr, ld, spec, ga, nullptr, 1, st);
-    k_coords_freq<float><<<nbf, 256, 0, st>>>(g, (C*)spec, size[0], size[1], size[2], derivative, wgt, Favg);
+    k_coords_freq<float><<<nbf, 256, 0, st>>>(g, (C*)spec, size[0], size[1], size[2], derivative, xi, wgt, Favg);
     ga.zsign = +1;
-    k_zpass<float><<<L.nbz, 256, L.smz, st>>>(g, pz, (C*)spec, L.TIz, ga, nullptr);
+    k_zpass<float, false><<<L.nbz, 256, L.smz, st>>>(g, pz, (C*)spec, L.TIz, ga, nullptr);
     k_ypass<float><<<L.nby, 256, L.smy, st>>>(g, py, (C*)spec, L.TIy, +1, nullptr);
     k_xinv<float, double><<<L.nbx, 256, L.smx, st>>>(g, px, (const C*)spec, scratch, ld, L.LX, nullptr);
   } else {
     typedef double2 C;
     convolve_impl<double>(L, px, py, pz, F, nullptr, ld, spec, ga, nullptr, 1, st);
-    k_coords_freq<double><<<nbf, 256, 0, st>>>(g, (C*)spec, size[0], size[1], size[2], derivative, wgt, Favg);
+    k_coords_freq<double><<<nbf, 256, 0, st>>>(g, (C*)spec, size[0], size[1], size[2], derivative, xi, wgt, Favg);
     ga.zsign = +1;
-    k_zpass<double><<<L.nbz, 256, L.smz, st>>>(g, pz, (C*)spec, L.TIz, ga, nullptr);
+    k_zpass<double, false><<<L.nbz, 256, L.smz, st>>>(g, pz, (C*)spec, L.TIz, ga, nullptr);
     k_ypass<double><<<L.nby, 256, L.smy, st>>>(g, py, (C*)spec, L.TIy, +1, nullptr);
     k_xinv<double, double><<<L.nbx, 256, L.smx, st>>>(g, px, (const C*)spec, scratch, ld, L.LX, nullptr);
   }
   k_coords_out<<<nbo, 256, 0, st>>>(g, scratch, ld, wgt, Favg, size[0] / g.N0, size[1] / g.N1, size[2] / g.N2, u_n,
                                     u_p);
+}
+
+size_t gamma_table_bytes(const SpecGeom& g, bool fp32, bool fwbw) {
+  return (size_t)gtab_entries(fp32, fwbw) * (size_t)g.Nh * (fp32 ? sizeof(float) : sizeof(double));
+}
+
+void gamma_table(const SpecGeom& g, bool fp32, const GammaArgs& ga, void* gtab, cudaStream_t st) {
+  const int nb = (int)((g.Nh + 255) / 256);
+  const bool fw = ga.fw[0] != nullptr;
+  if (fp32) {
+    if (fw) k_gamma_table<float, true><<<nb, 256, 0, st>>>(g, ga, (float*)gtab);
+    else k_gamma_table<float, false><<<nb, 256, 0, st>>>(g, ga, (float*)gtab);
+  } else {
+    if (fw) k_gamma_table<double, true><<<nb, 256, 0, st>>>(g, ga, (double*)gtab);
+    else k_gamma_table<double, false><<<nb, 256, 0, st>>>(g, ga, (double*)gtab);
+  }
+}
+
+void fw_axis(int axis, const int cells[3], std::vector<double>& v) {
+  // D = e^(i theta) - 1, E = e^(i theta) + 1, theta = 2 pi k / n (k in FFT order), as
+  // the reference's forward/backward difference (spectral.cpp:115-124)
+  const double TAU = 6.283185307179586476925286766559;
+  const int n = cells[axis];
+  const int len = axis == 0 ? n / 2 + 1 : n;
+  v.assign(4 * (size_t)len, 0.0);
+  for (int i = 0; i < len; ++i) {
+    const int k = axis == 0 ? i : (i > n / 2 ? i - n : i);
+    const double c = std::cos(TAU * k / n), s = std::sin(TAU * k / n);
+    v[4 * i] = c - 1.0; v[4 * i + 1] = s; v[4 * i + 2] = c + 1.0; v[4 * i + 3] = s;
+  }
 }
 
 void spec_div_finish_batch(const SpecItem* items, int nitems, int nb, double wgt, int N0, cudaStream_t st) {

@@ -39,8 +39,14 @@ struct GammaArgs {
   const double* xi_x;     // N0r  (imaginary part of xi1st along x; continuous/central)
   const double* xi_y;     // N1
   const double* xi_z;     // N2
+  // forward/backward difference (FWBW): per axis and FFT index the complex factors
+  // D = e^(i theta) - 1 and E = e^(i theta) + 1 (4 doubles: D.re, D.im, E.re, E.im),
+  // xi_p = D_p E_q E_r / (4 h_p) with q, r the other two axes; null otherwise
+  const double* fw[3];
+  double fw_h4[3];        // 4 h_p = 4 size_p / cells_p
   double resc[3];         // geom / scaled_geom
-  const double* C_ref;    // 81, device
+  const double* C_ref;    // 81, device (gamma_table input)
+  const void* gtab;       // per-frequency K^-1 table of C_ref (gamma_table), spectrum precision
   const double* aim;      // 9, device (zero-frequency value), may be null when !gamma
   int do_gamma, do_div;
   int store_fwd;          // without gamma: write the z transform back (forward, or inverse if zsign > 0)
@@ -53,11 +59,20 @@ struct SpecItem {
   const double* in;       // 9 real planes, ld = N
   double* out;            // 9 real planes, ld = N (Gamma * in)
   void* spec;             // 9 Nh complex (FP64 or FP32)
-  const double* C_ref;    // 81
+  const void* gtab;       // the RVE's K^-1 table (gamma_table)
   const double* aim;      // 9, zero-frequency value
   double* div_part;       // ndiv partials of the divergence sum
   double* rms;            // divergence RMS out
 };
+
+// The Gamma operator depends on the frequency only through K^-1(xi) of the reference
+// stiffness, which stays fixed between reference-stiffness updates: gamma_table
+// evaluates it once per frequency (layout: entry planes of Nh, frequency index
+// (y N0r + x) N2 + z) into gtab, of gamma_table_bytes.  FP64 spectra: the 9 entries of
+// the real K^-1 (continuous / central difference) or of the complex (K^*)^-1 (FWBW, 18
+// reals); FP32 spectra: the same in FP32, the real one as its 6 symmetric entries.
+size_t gamma_table_bytes(const SpecGeom& g, bool fp32, bool fwbw);
+void gamma_table(const SpecGeom& g, bool fp32, const GammaArgs& ga, void* gtab, cudaStream_t st);
 
 // cos/sin of 2 pi j / n with the argument reduced to the first octant
 void twiddle(long j, long n, double* c, double* s);
@@ -89,7 +104,10 @@ void spec_convolve(const SpecLaunch& L, bool fp32, const AxisPlan& px, const Axi
 // scratch: 9 real planes (ld); Favg: 9 doubles out (device).
 void spec_update_coords(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                         const double* F, long long ld, void* spec, double* scratch, const double size[3],
-                        int derivative, double wgt, double* Favg, double* u_n, double* u_p, cudaStream_t st);
+                        int derivative, const GammaArgs& xi, double wgt, double* Favg, double* u_n, double* u_p,
+                        cudaStream_t st);
+// host table of the FWBW factors (D, E) of one axis in FFT index order (4 doubles each)
+void fw_axis(int axis, const int cells[3], std::vector<double>& v);
 // nitems RVEs of the same grid (and precision) in one launch per pass; items in device memory
 void spec_convolve_batch(const SpecLaunch& L, bool fp32, const AxisPlan& px, const AxisPlan& py, const AxisPlan& pz,
                          const SpecItem* items, int nitems, const GammaArgs& ga, cudaStream_t st);
