@@ -152,6 +152,22 @@ void dgo_fft_c2r(const int cells[3], int ncomp, const double* spec_, double* fie
 }
 
 /* ------------------------------------------------------------------ xi */
+/* cos/sin of 2 pi k / n for the forward/backward difference: exact at quarter turns
+ * (k / n a multiple of 1/4), where the factors e^(i theta) +- 1 vanish and xi with them;
+ * cos(2 pi k / n), sin(2 pi k / n) otherwise */
+static void fw_trig(int k, int n, double* c, double* s) {
+  long q4 = (4L * k) % n;
+  if (q4 == 0) {
+    long quarter = ((4L * k) / n) % 4;
+    if (quarter < 0) quarter += 4;
+    const double cc[4] = {1.0, 0.0, -1.0, 0.0}, ss[4] = {0.0, 1.0, 0.0, -1.0};
+    *c = cc[quarter]; *s = ss[quarter];
+    return;
+  }
+  *c = cos(TAU * k / n);
+  *s = sin(TAU * k / n);
+}
+
 static void freq_derivative(int derivative, const int cells[3], const double geom[3], const int ks[3], cplx out[3]) {
   for (int i = 0; i < 3; ++i) {
     switch (derivative) {
@@ -161,11 +177,16 @@ static void freq_derivative(int derivative, const int cells[3], const double geo
       case DGO_DERIV_CENTRAL:
         out[i] = (I * sin(TAU * ks[i] / cells[i])) / (2.0 * geom[i] / cells[i]);
         break;
-      default: {  /* forward/backward difference, Fortran form */
+      default: {  /* forward/backward difference (spectral.cpp:115-124 spells the factors out; as
+                     written there the statement ends in a comma operator and yields zero) */
         int j = (i + 1) % 3, k = (i + 2) % 3;
-        cplx a = (cos(TAU * ks[i] / cells[i]) - 1.0) + I * sin(TAU * ks[i] / cells[i]);
-        cplx b = (cos(TAU * ks[j] / cells[j]) + 1.0) + I * sin(TAU * ks[j] / cells[j]);
-        cplx c = (cos(TAU * ks[k] / cells[k]) + 1.0) + I * sin(TAU * ks[k] / cells[k]);
+        double ci, si, cj, sj, ck, sk;
+        fw_trig(ks[i], cells[i], &ci, &si);
+        fw_trig(ks[j], cells[j], &cj, &sj);
+        fw_trig(ks[k], cells[k], &ck, &sk);
+        cplx a = (ci - 1.0) + I * si;
+        cplx b = (cj + 1.0) + I * sj;
+        cplx c = (ck + 1.0) + I * sk;
         out[i] = a * b * c / (4.0 * geom[i] / cells[i]);
       }
     }
@@ -398,6 +419,7 @@ void dgo_update_coords(const int cells[3], const double geom[3], int derivative,
     if (f == 0) { uh[0] = uh[1] = uh[2] = 0.0; continue; }
     cplx den = 0.0;
     for (int m = 0; m < 3; ++m) den += conj(-xi[m]) * xi[m];
+    if (den == 0.0) { uh[3 * f] = uh[3 * f + 1] = uh[3 * f + 2] = 0.0; continue; }   /* xi = 0: no fluctuation */
     for (int l = 0; l < 3; ++l) {
       cplx s = 0.0;
       for (int m = 0; m < 3; ++m) s += Fh[9 * f + l + 3 * m] * xi[m];

@@ -18,6 +18,8 @@
 // Schmid signs of the cF slip systems are folded in at compile time; all of it is
 // algebraically identical to the reference's contractions.
 #include <algorithm>
+#include <mutex>
+#include <set>
 #include <type_traits>
 
 #include "../../include/dgx.h"
@@ -861,13 +863,34 @@ __device__ bool stress_outputs(const double* F, const double* invFp0, double dt,
   return false;
 }
 
-template <typename R>
-__device__ __forceinline__ R damper(const R* o0, const R* o1, const R* o2) {
+// Per-thread scratch of the state integration in shared memory (one record per thread
+// of the block, entry i of thread t at base[i * BS + t]): the damper's two previous
+// rates (FP64 in the plain form, FP32 in the mixed form).  Kept out of registers, as
+// they are touched once per fixed-point pass while the Lp Newton between passes needs
+// every register.
+template <typename DT>
+struct Hist {
+  DT* h;
+  int stride;
+  __device__ __forceinline__ DT& l1(int i) const { return h[i * stride]; }
+  __device__ __forceinline__ DT& l2(int i) const { return h[(2 * NSLIP + i) * stride]; }
+};
+
+// the committed state of the step's start: device planes (stride ld) or a local array
+struct StateRef {
+  const double* p;
+  int64_t ld;
+  __device__ __forceinline__ double operator[](int i) const { return p[i * ld]; }
+};
+
+template <typename R, typename DT>
+__device__ __forceinline__ R damper(const R* o0, const Hist<DT>& h) {
   R d12 = R(0), d22 = R(0), d01 = R(0);
 #pragma unroll
   for (int i = 0; i < 2 * NSLIP; ++i) {
-    R a = o0[i] - o1[i], b = o1[i] - o2[i];
-    d12 = fmx(a, b, d12); d22 = fmx(b, b, d22); d01 = fmx(o0[i], o1[i], d01);
+    const R o1 = h.l1(i), o2 = h.l2(i);
+    R a = o0[i] - o1, b = o1 - o2;
+    d12 = fmx(a, b, d12); d22 = fmx(b, b, d22); d01 = fmx(o0[i], o1, d01);
   }
   if (fmin(d01, d12) < R(0) && d22 > R(0)) return R(0.75) + R(0.25) * tanh(R(2) + R(4) * d12 * rcp(d22));
   return R(1);
@@ -877,27 +900,26 @@ __device__ __forceinline__ bool bad_rate(double x) { return nan_bits(x); }
 __device__ __forceinline__ bool bad_rate(float x) { return absbits(x) >= 0x7f800000; }
 
 // integrateStateFPI; returns true if broken.  S on entry: stress used for the
-// first dot state (restored committed stress); state in/out.  F and Fp0 are fixed for
-// the whole iteration, so Fp0^-1 and F Fp0^-1 are formed once.
+// first dot state (restored committed stress); state in/out; on success Lp, S and
+// the state are the converged ones and the caller forms P, Fp, Fe (stress_outputs).
+// A = F Fp0^-1 is fixed for the whole iteration.
 // guess (mixed form, may be null): a state (planes of stride gld) that replaces the
 // explicit predictor state0 + dot(S) dt as the iteration's start, with the rate it
 // implies, (guess - state0) / dt, as the first rate of the damper's history.  The
 // fixed point and its FP64 test are unchanged.
 template <bool MX>
-__device__ bool integrate_state(const MatParams& mp, const double* F, const double* Fp0, const double* state0,
-                                double dt, double* state, double* Lp, double* S, double* P, double* Fp,
-                                double* Fe, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
+__device__ bool integrate_state(const MatParams& mp, const double* F, const double* A, const double* invFp0,
+                                StateRef state0, double dt, double* state, double* Lp, double* S,
+                                const Hist<typename std::conditional<MX, float, double>::type>& hist,
+                                LpPredictor* pred_s, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
                                 unsigned* fpi_iters, const WarmPrev* wp = nullptr) {
-  // rates and their history: FP64 in the plain form, FP32 in the mixed form
+  // rates: FP64 in the plain form, FP32 in the mixed form
   using DT = typename std::conditional<MX, float, double>::type;
-  DT dot[2 * NSLIP], last1[2 * NSLIP], last2[2 * NSLIP];
+  DT dot[2 * NSLIP];
   double prxi[NSLIP], gdot[NSLIP];
-  LpPredictor pred;                  // mixed form: start of the next pass's Lp Newton
-  pred.valid = false;
+  // pred_s (mixed form only): start of the next pass's Lp Newton
+  if constexpr (MX) pred_s->valid = false;
   (*st_iters)++;
-  double invFp0[9], A[9];
-  if (!inv33(Fp0, invFp0)) return true;
-  mm(F, invFp0, A);
   bool seeded = false;
   if (MX && wp && dt > 0.0) {
     // the guess seeds the iteration only if its slip resistances are positive and its
@@ -966,14 +988,14 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
       for (int a = 0; a < NSLIP; ++a) {
         const float px = mp.pval_f * rcp(to_f32(state[a]));
         const float r = fabsf(tp[a]) * px;
-        pred.r[a] = r;
-        pred.prxi[a] = px;
-        pred.g[a] = mp.n_f * px * pow_nm1_f(r, mp) * dtt[a];
+        pred_s->r[a] = r;
+        pred_s->prxi[a] = px;
+        pred_s->g[a] = mp.n_f * px * pow_nm1_f(r, mp) * dtt[a];
       }
 #pragma unroll
-      for (int k = 0; k < 9; ++k) pred.Fe[k] = Fep[k];
-      pred.mode = 2;
-      pred.valid = true;
+      for (int k = 0; k < 9; ++k) pred_s->Fe[k] = Fep[k];
+      pred_s->mode = 2;
+      pred_s->valid = true;
     }
   }
   if (!seeded) {
@@ -993,15 +1015,13 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(to_f64(dot[i]), dt, state0[i]);
   }
-  bool broken = true;
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) { last2[i] = it > 1 ? last1[i] : DT(0); last1[i] = dot[i]; }
+    for (int i = 0; i < 2 * NSLIP; ++i) { hist.l2(i) = it > 1 ? hist.l1(i) : DT(0); hist.l1(i) = dot[i]; }
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
     (*fpi_iters)++;
-    broken = integrate_stress<MX>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters, MX ? &pred : nullptr);
-    if (broken) break;
+    if (integrate_stress<MX>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters, MX ? pred_s : nullptr)) return true;
     if constexpr (MX) {
       float gf[NSLIP];
 #pragma unroll
@@ -1013,12 +1033,12 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
     bool nan = false;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
-    if (nan) break;
-    const DT z = damper(dot, last1, last2);
+    if (nan) return true;
+    const DT z = damper(dot, hist);
     bool conv = true;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) {
-      const DT d = dot[i] * z + last1[i] * (DT(1) - z);
+      const DT d = dot[i] * z + hist.l1(i) * (DT(1) - z);
       double r = state[i] - state0[i] - to_f64(d) * dt;
       state[i] = state[i] - r;
       // |r| <= max(atol, eps |state|), compared exactly as integers (r and state are
@@ -1027,85 +1047,149 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
       conv &= absbits(r) <= max(atol, absbits(mp.eps_rel_state * state[i]));
       dot[i] = d;
       if constexpr (MX) {
-        if (i < NSLIP) pred.dxi[i] = to_f32(r);   // xi - xi' of this update
+        if (i < NSLIP) pred_s->dxi[i] = to_f32(r);   // xi - xi' of this update
       }
     }
-    if (conv) { broken = false; break; }
+    if (conv) return false;
   }
-  // P, Fp, Fe of the last stress integration (as the reference leaves them)
-  if (!broken) broken = stress_outputs(F, invFp0, dt, Lp, S, P, Fp, Fe);
-  return broken;
+  return true;
 }
 
 __device__ __forceinline__ double ldp(const double* p, int64_t ld, int c, int64_t e) { return p[c * ld + e]; }
 
+// F Fp0^-1 and Fp0^-1 of a sub-step (false if Fp0 is singular)
+__device__ __forceinline__ bool sub_step_maps(const double* Fsub, const double* Fp0, double* invFp0, double* A) {
+  if (!inv33(Fp0, invFp0)) return false;
+  mm(Fsub, invFp0, A);
+  return true;
+}
+
+// One sub-step of the cut-back driver: state integration, then P, Fp, Fe of its
+// converged stress integration (as the reference leaves them).  Returns true if the
+// sub-step converged.
+template <bool MX>
+__device__ __forceinline__ bool sub_step(const MatParams& mp, const double* Fsub, const double* Fp0, StateRef state0,
+                                         double dt, double* state, double* Lp, double* S, double* P, double* Fp,
+                                         double* Fe, const Hist<typename std::conditional<MX, float, double>::type>& hist,
+                                         LpPredictor* pred, unsigned* c, const WarmPrev* wp) {
+  double invFp0[9], A[9];
+  if (!sub_step_maps(Fsub, Fp0, invFp0, A)) { c[1]++; return false; }   // counted as an attempted integration
+  if (integrate_state<MX>(mp, Fsub, A, invFp0, state0, dt, state, Lp, S, hist, pred, &c[0], &c[2], &c[1], &c[3], wp))
+    return false;
+  return !stress_outputs(Fsub, invFp0, dt, Lp, S, P, Fp, Fe);
+}
+
+// The reference's sub-step cut-back driver (phase_mechanical_constitutive,
+// phase_mechanical.f90:1013-1100) after a failed full step: halve the step, restore
+// the last converged sub-step, grow the step by r_increase after each success, give
+// up below r_cutback_min.  Everything is reloaded from the committed planes, so the
+// common case (the full step converges) keeps none of it live.  Out of line: it runs
+// for few cells.  Returns true if the cell converged; outputs as the full step's.
+template <bool MX>
+__device__ __noinline__ bool cutback_driver(const MatParams& mp, const PointState& ps, const double* __restrict__ Fin,
+                                            int64_t ldF, int64_t e, double dt, double* state, double* Lp, double* S,
+                                            double* P, double* Fp, double* Fe,
+                                            const Hist<typename std::conditional<MX, float, double>::type>& hist,
+                                            LpPredictor* pred, unsigned* c) {
+  double F[9], F0c[9], Fphase0[9], Fp0[9], Lp0[9], S0[9], state0[2 * NSLIP], Fsub[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    F[k] = Fin[k * ldF + e];
+    Fphase0[k] = ldp(ps.F0, ps.ld, k, e);
+    F0c[k] = Fphase0[k];
+    Fp0[k] = ldp(ps.Fp0, ps.ld, k, e);
+    Lp0[k] = ldp(ps.Lp0, ps.ld, k, e);
+    S0[k] = ldp(ps.S0, ps.ld, k, e);
+  }
+#pragma unroll
+  for (int i = 0; i < 2 * NSLIP; ++i) state0[i] = ldp(ps.st0, ps.ld, i, e);
+  // state after the failed full step
+  double stepFrac = 0.0, step = mp.r_cutback * (1.0 / mp.r_cutback);
+  bool converged = false, todo = true;
+  int passes = 1;
+  while (todo) {
+    if (++passes > 4096) { converged = false; break; }   // hard cap: a point never loops unbounded
+    if (converged) {
+      stepFrac += step;
+      step = fmin(1.0 - stepFrac, mp.r_increase * step);
+      todo = step > 0.0;
+      if (todo) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) { F0c[k] = Fsub[k]; Lp0[k] = Lp[k]; Fp0[k] = Fp[k]; }
+#pragma unroll
+        for (int i = 0; i < 2 * NSLIP; ++i) state0[i] = state[i];
+      }
+    } else {
+      step = mp.r_cutback * step;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) { Fp[k] = Fp0[k]; S[k] = S0[k]; if (step < 1.0) Lp[k] = Lp0[k]; }
+#pragma unroll
+      for (int i = 0; i < 2 * NSLIP; ++i) state[i] = state0[i];
+      todo = step > mp.r_cutback_min;
+    }
+    if (todo) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
+      converged = sub_step<MX>(mp, Fsub, Fp0, StateRef{state0, 1}, step * dt, state, Lp, S, P, Fp, Fe, hist, pred, c,
+                               nullptr);
+    }
+  }
+  return converged;
+}
+
 // Per-point constitutive response (restore, cut-back driver, FPI, P) of one tile of
 // BS points plus the partial sums of P (per 32 points, one warp) for P_av.  One thread
-// per point.
+// per point.  The reference's driver starts with a pretended failed step of
+// 1 / r_cutback, i.e. with the full step (step 1) from the committed state; that
+// attempt runs here straight from the committed planes, and only a cell whose full
+// step fails enters the out-of-line cut-back driver.
 // Mixed form with warm set: the state planes hold the converged state of the previous
 // evaluation in the same step, which seeds the state iteration of the full step.
+// smem: this block's Hist records (and the mixed form's LpPredictor records).
 template <int BS, bool MX>
 __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState& ps, const double* __restrict__ Fin,
                                           int64_t ldF, double dt, double* __restrict__ Ppart, int* __restrict__ ill,
-                                          ConsCounters* cnt, int64_t tile, int warm = 0) {
+                                          ConsCounters* cnt, int64_t tile, unsigned char* smem, int warm = 0) {
+  using DT = typename std::conditional<MX, float, double>::type;
   const int64_t e = tile * BS + threadIdx.x;
+  const Hist<DT> hist{reinterpret_cast<DT*>(smem) + threadIdx.x, BS};
+  // mixed form only (the plain form's blocks have no predictor records)
+  LpPredictor* pred = MX ? reinterpret_cast<LpPredictor*>(smem + 4 * NSLIP * BS * sizeof(DT)) + threadIdx.x : nullptr;
   double P[9];
-  unsigned lp_iters = 0, st_iters = 0, jac_iters = 0, fpi_iters = 0;
+  unsigned c[4] = {0, 0, 0, 0};             // Lp iterations, state integrations, Jacobians, fixed-point passes
   bool ok = true;
   if (e < ps.n) {
-    double F[9], F0c[9], Fphase0[9], Fp0[9], Lp[9], Lp0[9], S[9], S0[9], state0[2 * NSLIP], state[2 * NSLIP];
-    double Fp[9], Fe[9];
+    double state[2 * NSLIP], Lp[9], S[9], Fp[9], Fe[9];
+    // the full step (the driver's first step, r_cutback / r_cutback = 1 for the usual
+    // values): Fsub = F0 + step (F - F0) from the committed state, S0, Fp0 and the warm
+    // Lp (the committed Lp0 if the step comes out below 1) from the planes
+    const double step1 = mp.r_cutback * (1.0 / mp.r_cutback);
+    double Fsub[9], Fp0[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      F[k] = Fin[k * ldF + e];
-      Fphase0[k] = ldp(ps.F0, ps.ld, k, e);
+      const double f0 = ldp(ps.F0, ps.ld, k, e);
+      Fsub[k] = f0 + step1 * (Fin[k * ldF + e] - f0);
       Fp0[k] = ldp(ps.Fp0, ps.ld, k, e);
-      Lp[k] = ldp(ps.Lp, ps.ld, k, e);
-      S0[k] = ldp(ps.S0, ps.ld, k, e);
-      F0c[k] = Fphase0[k];
-      Lp0[k] = ldp(ps.Lp0, ps.ld, k, e);
-      Fp[k] = Fp0[k];
-      Fe[k] = 0.0;
+      Lp[k] = step1 < 1.0 ? ldp(ps.Lp0, ps.ld, k, e) : ldp(ps.Lp, ps.ld, k, e);
+      S[k] = ldp(ps.S0, ps.ld, k, e);
       P[k] = 0.0;
+      Fe[k] = 0.0;
+      Fp[k] = Fp0[k];
     }
+    const StateRef st0{ps.st0 + e, ps.ld};
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) { state0[i] = ldp(ps.st0, ps.ld, i, e); state[i] = state0[i]; }
-    // phase_mechanical_constitutive: pretend a failed step of 1/r_cutback
-    double stepFrac = 0.0, step = 1.0 / mp.r_cutback, Fsub[9];
-    bool converged = false, todo = true;
-    int passes = 0;
-    while (todo) {
-      if (++passes > 4096) { converged = false; break; }   // hard cap: a point never loops unbounded
-      if (converged) {
-        stepFrac += step;
-        step = fmin(1.0 - stepFrac, mp.r_increase * step);
-        todo = step > 0.0;
-        if (todo) {
-#pragma unroll
-          for (int k = 0; k < 9; ++k) { F0c[k] = Fsub[k]; Lp0[k] = Lp[k]; Fp0[k] = Fp[k]; }
-#pragma unroll
-          for (int i = 0; i < 2 * NSLIP; ++i) state0[i] = state[i];
-        }
-      } else {
-        step = mp.r_cutback * step;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) { Fp[k] = Fp0[k]; S[k] = S0[k]; if (step < 1.0) Lp[k] = Lp0[k]; }
-#pragma unroll
-        for (int i = 0; i < 2 * NSLIP; ++i) state[i] = state0[i];
-        todo = step > mp.r_cutback_min;
-      }
-      if (todo) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
-        const WarmPrev wp{ps.F + e, ps.Fe + e, ps.S + e, ps.st + e, ps.ld};
-        converged = !integrate_state<MX>(mp, Fsub, Fp0, state0, step * dt, state, Lp, S, P, Fp, Fe, &lp_iters, &jac_iters,
-                                     &st_iters, &fpi_iters, (MX && warm && passes == 1) ? &wp : nullptr);
-      }
+    for (int i = 0; i < 2 * NSLIP; ++i) state[i] = st0[i];
+    const WarmPrev wp{ps.F + e, ps.Fe + e, ps.S + e, ps.st + e, ps.ld};
+    if (step1 > mp.r_cutback_min) {
+      ok = sub_step<MX>(mp, Fsub, Fp0, st0, step1 * dt, state, Lp, S, P, Fp, Fe, hist, pred, c,
+                        (MX && warm) ? &wp : nullptr);
+      if (!ok) ok = cutback_driver<MX>(mp, ps, Fin, ldF, e, dt, state, Lp, S, P, Fp, Fe, hist, pred, c);
+    } else {
+      ok = false;
     }
-    ok = converged;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      ps.F[k * ps.ld + e] = F[k];
+      ps.F[k * ps.ld + e] = Fin[k * ldF + e];
       ps.Fp[k * ps.ld + e] = Fp[k];
       ps.Lp[k * ps.ld + e] = Lp[k];
       ps.S[k * ps.ld + e] = S[k];
@@ -1131,7 +1215,7 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
   }
   if (cnt) {
     // per-warp aggregation of the work counters
-    unsigned lp = lp_iters, st = st_iters, jc = jac_iters, fp = fpi_iters;
+    unsigned lp = c[0], st = c[1], jc = c[2], fp = c[3];
     for (int o = 16; o > 0; o >>= 1) {
       lp += __shfl_down_sync(0xffffffffu, lp, o);
       st += __shfl_down_sync(0xffffffffu, st, o);
@@ -1147,11 +1231,18 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
   }
 }
 
+// dynamic shared memory of a constitutive block: the Hist records of BS threads
+// (4 x 12 rates wide: two history rates of 24 entries), and the LpPredictor records
+__host__ __device__ constexpr size_t cons_smem_bytes(int bs, bool mx) {
+  return (size_t)4 * NSLIP * bs * (mx ? sizeof(float) : sizeof(double)) + (mx ? (size_t)bs * sizeof(LpPredictor) : 0);
+}
+
 template <int BS, bool MX>
 __global__ void __launch_bounds__(BS)
 k_constitutive(MatParams mp, PointState ps, const double* __restrict__ Fin, int64_t ldF, double dt,
                double* __restrict__ Ppart, int* __restrict__ ill, ConsCounters* cnt) {
-  cons_tile<BS, MX>(mp, ps, Fin, ldF, dt, Ppart, ill, cnt, blockIdx.x);
+  extern __shared__ __align__(16) unsigned char cons_smem[];
+  cons_tile<BS, MX>(mp, ps, Fin, ldF, dt, Ppart, ill, cnt, blockIdx.x, cons_smem);
 }
 
 // Batched form: the points of many RVEs (uneven sizes) in one persistent launch.
@@ -1163,6 +1254,7 @@ template <int BS, int MINB, bool MX>
 __global__ void __launch_bounds__(BS, MINB)
 k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitems, long long ntiles,
                      unsigned long long* __restrict__ queue, ConsCounters* cnt) {
+  extern __shared__ __align__(16) unsigned char cons_smem[];
   __shared__ ConsItem s_it;
   __shared__ long long s_tile;
   for (;;) {
@@ -1180,7 +1272,8 @@ k_constitutive_batch(MatParams mp, const ConsItem* __restrict__ items, int nitem
     __syncthreads();
     const long long t = s_tile;
     if (t >= ntiles) break;
-    cons_tile<BS, MX>(mp, s_it.ps, s_it.F, s_it.ldF, s_it.dt, s_it.Ppart, s_it.ill, cnt, t - s_it.tile0, s_it.warm);
+    cons_tile<BS, MX>(mp, s_it.ps, s_it.F, s_it.ldF, s_it.dt, s_it.Ppart, s_it.ill, cnt, t - s_it.tile0, cons_smem,
+                      s_it.warm);
   }
 }
 
@@ -1508,18 +1601,58 @@ __global__ void __launch_bounds__(256) k_pav_finish(const double* __restrict__ p
 namespace dgx {
 // block size of the constitutive launch (32, 64, 128 or 256 threads); P_av partials are
 // per 32 cells whatever the block size: ceil(n / 32) x 9 doubles
+// The constitutive kernels take cons_smem_bytes of dynamic shared memory; the limit
+// above 48 KB is raised once per device for every instantiation (before any capture:
+// the first launch or residency query on a device does it).
+template <typename K>
+static bool cons_smem_attr(K* k, int bs, bool mx) {
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cons_smem_bytes(bs, mx)) == cudaSuccess;
+}
+static bool prepare_cons_kernels() {
+  static std::mutex mu;
+  static std::set<int> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count(dev)) return true;
+  bool ok = true;
+  ok &= cons_smem_attr(k_constitutive<32, false>, 32, false);
+  ok &= cons_smem_attr(k_constitutive<64, false>, 64, false);
+  ok &= cons_smem_attr(k_constitutive<128, false>, 128, false);
+  ok &= cons_smem_attr(k_constitutive<256, false>, 256, false);
+  ok &= cons_smem_attr(k_constitutive<128, true>, 128, true);
+  ok &= cons_smem_attr(k_constitutive_batch<64, 1, false>, 64, false);
+  ok &= cons_smem_attr(k_constitutive_batch<128, 1, false>, 128, false);
+  ok &= cons_smem_attr(k_constitutive_batch<256, 1, false>, 256, false);
+  ok &= cons_smem_attr(k_constitutive_batch<128, 3, false>, 128, false);
+  ok &= cons_smem_attr(k_constitutive_batch<32, 1, false>, 32, false);
+  ok &= cons_smem_attr(k_constitutive_batch<64, 1, true>, 64, true);
+  ok &= cons_smem_attr(k_constitutive_batch<128, 1, true>, 128, true);
+  ok &= cons_smem_attr(k_constitutive_batch<256, 1, true>, 256, true);
+  ok &= cons_smem_attr(k_constitutive_batch<128, 3, true>, 128, true);
+  ok &= cons_smem_attr(k_constitutive_batch<32, 1, true>, 32, true);
+  if (ok) done.insert(dev);
+  return ok;
+}
+
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
                          double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block) {
+  prepare_cons_kernels();
   if (mp.mixed) {                                  // mixed form: one launch shape
-    k_constitutive<128, true><<<(int)((ps.n + 127) / 128), 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<128, true><<<(int)((ps.n + 127) / 128), 128, cons_smem_bytes(128, true), st>>>(mp, ps, F, ldF, dt,
+                                                                                                  Ppart, ill, cnt);
   } else if (block == 32) {
-    k_constitutive<32, false><<<(int)((ps.n + 31) / 32), 32, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<32, false><<<(int)((ps.n + 31) / 32), 32, cons_smem_bytes(32, false), st>>>(mp, ps, F, ldF, dt, Ppart,
+                                                                                               ill, cnt);
   } else if (block == 64) {
-    k_constitutive<64, false><<<(int)((ps.n + 63) / 64), 64, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<64, false><<<(int)((ps.n + 63) / 64), 64, cons_smem_bytes(64, false), st>>>(mp, ps, F, ldF, dt, Ppart,
+                                                                                               ill, cnt);
   } else if (block == 256) {
-    k_constitutive<256, false><<<(int)((ps.n + 255) / 256), 256, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<256, false><<<(int)((ps.n + 255) / 256), 256, cons_smem_bytes(256, false), st>>>(mp, ps, F, ldF, dt,
+                                                                                                    Ppart, ill, cnt);
   } else {
-    k_constitutive<128, false><<<(int)((ps.n + 127) / 128), 128, 0, st>>>(mp, ps, F, ldF, dt, Ppart, ill, cnt);
+    k_constitutive<128, false><<<(int)((ps.n + 127) / 128), 128, cons_smem_bytes(128, false), st>>>(mp, ps, F, ldF, dt,
+                                                                                                    Ppart, ill, cnt);
   }
 }
 // the batched kernel of a launch variant and form
@@ -1536,19 +1669,21 @@ static void* cons_batch_fn(int variant) {
 // persistent batched launch: grid = min(tiles, resident blocks); queue must be zero
 void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
                                unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int variant, int grid) {
+  prepare_cons_kernels();
   const int bs = cons_variant_bs(variant);
   MatParams m = mp;
   const ConsItem* it = items;
   void* args[] = {&m, &it, &nitems, &ntiles, &queue, &cnt};
   cudaLaunchKernel(mp.mixed ? cons_batch_fn<true>(variant) : cons_batch_fn<false>(variant), dim3(grid), dim3(bs), args,
-                   0, st);
+                   cons_smem_bytes(bs, mp.mixed != 0), st);
 }
 int constitutive_batch_resident(int variant, bool mixed) {
+  prepare_cons_kernels();
   int nb = 0, dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mixed ? cons_batch_fn<true>(variant) : cons_batch_fn<false>(variant),
-                                                cons_variant_bs(variant), 0);
+                                                cons_variant_bs(variant), cons_smem_bytes(cons_variant_bs(variant), mixed));
   return std::max(1, nb) * std::max(1, sms);
 }
 void launch_pav_finish_batch(const ConsItem* items, int nitems, double* Pav, cudaStream_t st) {

@@ -967,15 +967,25 @@ void gamma_table(const SpecGeom& g, bool fp32, const GammaArgs& ga, void* gtab, 
 }
 
 void fw_axis(int axis, const int cells[3], std::vector<double>& v) {
-  // D = e^(i theta) - 1, E = e^(i theta) + 1, theta = 2 pi k / n (k in FFT order), as
-  // the reference's forward/backward difference (spectral.cpp:115-124)
+  // D = e^(i theta) - 1, E = e^(i theta) + 1, theta = 2 pi k / n (k in FFT order), the
+  // factors of the reference's forward/backward difference (spectral.cpp:115-124);
+  // cos / sin exact at quarter turns, where D or E vanishes (and xi with it)
   const double TAU = 6.283185307179586476925286766559;
   const int n = cells[axis];
   const int len = axis == 0 ? n / 2 + 1 : n;
   v.assign(4 * (size_t)len, 0.0);
   for (int i = 0; i < len; ++i) {
     const int k = axis == 0 ? i : (i > n / 2 ? i - n : i);
-    const double c = std::cos(TAU * k / n), s = std::sin(TAU * k / n);
+    double c, s;
+    if ((4L * k) % n == 0) {
+      long quarter = ((4L * k) / n) % 4;
+      if (quarter < 0) quarter += 4;
+      const double cc[4] = {1.0, 0.0, -1.0, 0.0}, ss[4] = {0.0, 1.0, 0.0, -1.0};
+      c = cc[quarter]; s = ss[quarter];
+    } else {
+      c = std::cos(TAU * k / n);
+      s = std::sin(TAU * k / n);
+    }
     v[4 * i] = c - 1.0; v[4 * i + 1] = s; v[4 * i + 2] = c + 1.0; v[4 * i + 3] = s;
   }
 }
