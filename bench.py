@@ -356,7 +356,7 @@ def mixed_large_leg(g, torch, cells=128, grains=1000, inc_each=30):
     out = {"workload": f"{cells}^3 cells, {grains} grains (seed {SEED + 1}), tension x then shear xy, "
                        f"{inc_each} + {inc_each} increments"}
     recs = {}
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed", "fp64"):       # FP64 last: its converged field gives the divergence noise floor
         rve = g.RVE(c3, (1.0, 1.0, 1.0), mat_at, q, num=g.numerics(precision=prec))
         st = torch.cuda.ExternalStream(rve.stream)
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
@@ -370,7 +370,23 @@ def mixed_large_leg(g, torch, cells=128, grains=1000, inc_each=30):
         lat = [x["seconds"] for x in recs[prec]]
         out[prec] = {"value": rve.N * ev / (ms * 1e-3), "unit": UNIT, "seconds": ms * 1e-3, "evaluations": ev,
                      "p50_increment_ms": 1e3 * _pct(lat, 50), "p99_increment_ms": 1e3 * _pct(lat, 99)}
-        rve.close()
+        if prec == "fp64":
+            # FP32-spectrum noise floor of the divergence test: the divergence RMS of the
+            # converged FP64 stress field with FP64 and with FP32 spectra, against divTol
+            P = rve.get("P")
+            rms64 = rve.calculate_divergence_rms(P)
+            rve.close()
+            r32 = g.RVE(c3, (1.0, 1.0, 1.0), mat_at, q, num=g.numerics(precision="mixed"))
+            rms32 = r32.calculate_divergence_rms(P)
+            r32.close()
+            num = g.numerics()
+            div_tol = max(float(abs(recs[prec][-1]["P_av"]).max()) * num.eps_rel_div, num.eps_abs_div)
+            out["divergence_fp32_noise_over_divTol"] = abs(rms32 - rms64) / div_tol
+            out["err_div_over_divTol_at_convergence"] = {
+                p_: max(float(r["err_div"]) / max(float(abs(r["P_av"]).max()) * num.eps_rel_div, num.eps_abs_div)
+                        for r in recs[p_]) for p_ in recs}
+        else:
+            rve.close()
     errs = [float(abs(a["P_av"] - b["P_av"]).max() / abs(b["P_av"]).max()) for a, b in zip(recs["mixed"], recs["fp64"])]
     out["max_rel_P_av_error_vs_fp64"] = max(errs)
     out["per_increment_error"] = errs

@@ -49,7 +49,7 @@ typedef struct dgx_numerics {
   int32_t itmin, itmax, update_gamma;
   double eps_abs_div, eps_rel_div, eps_abs_P, eps_rel_P;
   int32_t divergence_correction;  /* 0 none, 1 size, 2 size+grid */
-  int32_t derivative;             /* 0 continuous, 1 central_difference (2 FWBW: unsupported) */
+  int32_t derivative;             /* 0 continuous, 1 central_difference, 2 FWBW_difference */
   int32_t stag_iter_max, max_cut_back;
   int32_t solver;                 /* 0 NGMRES (PETSc SNESNGMRES defaults), 1 fixed point */
   int32_t ngmres_m, snes_max_it;
