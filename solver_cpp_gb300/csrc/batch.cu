@@ -173,6 +173,13 @@ struct GraphEntry {
 constexpr size_t GRAPH_CACHE = 16;
 
 constexpr int TUNE_TRIALS = 5;               // interleaved timed rounds per constitutive launch variant
+// Rounds of at least this many points (two full waves of 128-point tiles at 4 blocks per
+// SM) take the launch variant measured best for large work (mixed form: 128 points at 4
+// blocks per SM, 1.54 ms per 64^3 launch against 1.65 at 3 and 1.81 at 2; FP64 form: 128
+// points at 2 blocks per SM, 3.82 ms against 3.86 and 3.90); the online tuner decides
+// for smaller rounds, where the block size and the wave count matter.
+constexpr long long LARGE_ROUND_POINTS = 152LL * 128 * 4 * 2;
+constexpr int LARGE_VARIANT_MIXED = 5, LARGE_VARIANT_FP64 = 1;
 
 struct Executor {
   cudaStream_t st = nullptr;
@@ -194,6 +201,7 @@ struct Executor {
   // rounds per variant, and per grid the FFT tile shape, timed on the first round's data
   // (results do not depend on either)
   bool tune_cons = true, tune_spec = true;
+  bool variant_pinned = false;                 // DGX_CONS_VARIANT or an explicit block size
   int res_by_variant[2][CONS_VARIANTS] = {};   // [mixed form][variant]: resident blocks
   double cons_cost[CONS_VARIANTS][5] = {};     // TUNE_TRIALS per variant
   int cons_trials[CONS_VARIANTS] = {}, cons_round = 0, tune_skipped = 0;
@@ -267,11 +275,13 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   const char* at = std::getenv("DGX_AUTOTUNE");
   const bool tune = !(at && at[0] == '0');
   e->tune_cons = tune && cons_block <= 0;       // an explicit block size is kept
+  e->variant_pinned = cons_block > 0;
   const char* cv = std::getenv("DGX_CONS_VARIANT");   // pin a launch variant (0..4) for measurements
   if (cv && cv[0] >= '0' && cv[0] < '0' + CONS_VARIANTS && cv[1] == 0) {
     e->cons_variant = cv[0] - '0';
     e->resident = e->res_by_variant[0][e->cons_variant];
     e->tune_cons = false;
+    e->variant_pinned = true;
   }
   e->tune_spec = tune;
   const char* gr = std::getenv("DGX_GRAPHS");          // 0: launch every round directly
@@ -560,6 +570,7 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
   const int n = (int)q.size();
   if (n > e->cap) { set_err("executor: %d residual requests exceed capacity %d", n, e->cap); return DGX_ERR_STATE; }
   int cand = -1;
+  bool large_round = false;
   std::vector<int> slot_of(n);
   RoundPlan p;
   p.n = n;
@@ -572,11 +583,16 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
       if (c != 0) return c < 0;
       return q[a].r->N > q[b].r->N;
     });
-    if (e->tune_cons) {
+    long long round_points = 0;
+    bool round_mixed = true;
+    for (int i = 0; i < n; ++i) { round_points += q[i].r->N; round_mixed &= q[i].r->mp.mixed != 0; }
+    large_round = !e->variant_pinned && round_points >= LARGE_ROUND_POINTS;
+    if (e->tune_cons && !large_round) {
       cand = e->cons_round % CONS_VARIANTS;
       if (e->cons_trials[cand] >= TUNE_TRIALS) cand = -1;
     }
-    p.variant = cand >= 0 ? cand : e->cons_variant;
+    p.variant = large_round ? (round_mixed ? LARGE_VARIANT_MIXED : LARGE_VARIANT_FP64)
+                            : (cand >= 0 ? cand : e->cons_variant);
     const int BS = cons_variant_bs(p.variant);
     for (int j = 0; j < n; ++j) slot_of[order[j]] = j;
     {
@@ -623,7 +639,7 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
         it.div_part = r->d_divpart; it.rms = e->d_rms + i;
       }
     }
-    p.cnt_d2h = e->tune_cons;
+    p.cnt_d2h = e->tune_cons && !large_round;
   }
   TRY(ex_multi_stage(e, mq, p));
   TRY(ex_issue_round(e, p));
@@ -639,7 +655,7 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
     cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[0] += ms; e->t_n[0]++;
     const float cons_ms = ms;
     cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[1] += ms; e->t_n[1]++;
-    if (e->tune_cons) {
+    if (e->tune_cons && !large_round) {
       // cost per counted FP64 flop (the constitutive roofline's own flop model; the
       // mixed form's FP64 model when every member of the round is mixed)
       const ConsCounters& c1 = *e->h_cnt;

@@ -1067,8 +1067,10 @@ __device__ __forceinline__ bool sub_step_maps(const double* Fsub, const double* 
 // One sub-step of the cut-back driver: state integration, then P, Fp, Fe of its
 // converged stress integration (as the reference leaves them).  Returns true if the
 // sub-step converged.
+// Out of line: the full step and the cut-back driver share one copy of the state
+// integration (the kernel is large enough that instruction fetch shows in its stalls).
 template <bool MX>
-__device__ __forceinline__ bool sub_step(const MatParams& mp, const double* Fsub, const double* Fp0, StateRef state0,
+__device__ __noinline__ bool sub_step(const MatParams& mp, const double* Fsub, const double* Fp0, StateRef state0,
                                          double dt, double* state, double* Lp, double* S, double* P, double* Fp,
                                          double* Fe, const Hist<typename std::conditional<MX, float, double>::type>& hist,
                                          LpPredictor* pred, unsigned* c, const WarmPrev* wp) {
@@ -1631,6 +1633,8 @@ static bool prepare_cons_kernels() {
   ok &= cons_smem_attr(k_constitutive_batch<256, 1, true>, 256, true);
   ok &= cons_smem_attr(k_constitutive_batch<128, 3, true>, 128, true);
   ok &= cons_smem_attr(k_constitutive_batch<32, 1, true>, 32, true);
+  ok &= cons_smem_attr(k_constitutive_batch<128, 4, false>, 128, false);
+  ok &= cons_smem_attr(k_constitutive_batch<128, 4, true>, 128, true);
   if (ok) done.insert(dev);
   return ok;
 }
@@ -1663,6 +1667,7 @@ static void* cons_batch_fn(int variant) {
     case 2: return (void*)k_constitutive_batch<256, 1, MX>;
     case 3: return (void*)k_constitutive_batch<128, 3, MX>;
     case 4: return (void*)k_constitutive_batch<32, 1, MX>;
+    case 5: return (void*)k_constitutive_batch<128, 4, MX>;
     default: return (void*)k_constitutive_batch<128, 1, MX>;
   }
 }
