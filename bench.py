@@ -40,9 +40,9 @@ UNIT = "point-updates/s"
 SEED = 42
 
 # DRAM traffic of one constitutive launch per cell, from an ncu capture of this
-# workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch / 262,144 cells:
-# 0.372 GB read + 0.980 GB written; mostly register-spill write-back)
-TRAFFIC_BYTES_PER_CELL = 5157.0
+# workload (dram__bytes.sum.per_second x gpu__time_duration.sum of one launch / 262,144
+# cells: 170.4 GB/s x 2.985 ms = 0.509 GB; profiles/constitutive_64cube.md)
+TRAFFIC_BYTES_PER_CELL = 1940.0
 
 
 def args_():
