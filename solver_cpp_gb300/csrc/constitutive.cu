@@ -1635,10 +1635,6 @@ static bool prepare_cons_kernels() {
   ok &= cons_smem_attr(k_constitutive_batch<32, 1, true>, 32, true);
   ok &= cons_smem_attr(k_constitutive_batch<128, 4, false>, 128, false);
   ok &= cons_smem_attr(k_constitutive_batch<128, 4, true>, 128, true);
-  ok &= cons_smem_attr(k_constitutive_batch<96, 5, false>, 96, false);
-  ok &= cons_smem_attr(k_constitutive_batch<96, 5, true>, 96, true);
-  ok &= cons_smem_attr(k_constitutive_batch<64, 7, false>, 64, false);
-  ok &= cons_smem_attr(k_constitutive_batch<64, 7, true>, 64, true);
   if (ok) done.insert(dev);
   return ok;
 }
@@ -1672,8 +1668,6 @@ static void* cons_batch_fn(int variant) {
     case 3: return (void*)k_constitutive_batch<128, 3, MX>;
     case 4: return (void*)k_constitutive_batch<32, 1, MX>;
     case 5: return (void*)k_constitutive_batch<128, 4, MX>;
-    case 6: return (void*)k_constitutive_batch<96, 5, MX>;
-    case 7: return (void*)k_constitutive_batch<64, 7, MX>;
     default: return (void*)k_constitutive_batch<128, 1, MX>;
   }
 }

@@ -142,15 +142,14 @@ struct ConsItem {
 void launch_constitutive(const MatParams& mp, const PointState& ps, const double* F, int64_t ldF, double dt,
                          double* Ppart, int* ill, ConsCounters* cnt, cudaStream_t st, int block);
 // launch variants of the batched constitutive kernel: points per block (64, 128, 256,
-// 128, 32, 128, 96, 64), and the blocks per SM its register allocation targets (1, 1,
-// 1, 3, 1, 4, 5, 7: more blocks, fewer registers and more spills).  32 points per block
-// spreads a small RVE over the most SMs (one warp each), which matters because one SM's
-// FP64 unit is the scarce resource.
-constexpr int CONS_VARIANTS = 8;
-__host__ __device__ constexpr int cons_variant_bs(int v) {
-  return v == 0 || v == 7 ? 64 : v == 2 ? 256 : v == 4 ? 32 : v == 6 ? 96 : 128;
-}
-__host__ __device__ constexpr int cons_variant_minb(int v) { return v == 3 ? 3 : v == 5 ? 4 : v == 6 ? 5 : v == 7 ? 7 : 1; }
+// 128, 32, 128), and the blocks per SM its register allocation targets (1, 1, 1, 3, 1,
+// 4: more blocks, fewer registers and more spills).  32 points per block spreads a small
+// RVE over the most SMs (one warp each), which matters because one SM's FP64 unit is the
+// scarce resource.  (Measured and dropped: 96 points at 5 blocks and 64 at 7, 136 and
+// 144 registers: no faster than 128 at 4 in the mixed form, slower in FP64.)
+constexpr int CONS_VARIANTS = 6;
+__host__ __device__ constexpr int cons_variant_bs(int v) { return v == 0 ? 64 : v == 2 ? 256 : v == 4 ? 32 : 128; }
+__host__ __device__ constexpr int cons_variant_minb(int v) { return v == 3 ? 3 : v == 5 ? 4 : 1; }
 void launch_constitutive_batch(const MatParams& mp, const ConsItem* items, int nitems, long long ntiles,
                                unsigned long long* queue, ConsCounters* cnt, cudaStream_t st, int variant, int grid);
 int constitutive_batch_resident(int variant, bool mixed);
