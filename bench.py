@@ -261,8 +261,11 @@ def _run_batch(g, torch, pop, precision, increments, seconds):
     pending = {slot for _, slot in rves}
     done_at = {}
     active = 1
+    t_in_step = 0.0
     while active and time.perf_counter() - t_start < seconds:
+        ts = time.perf_counter()
         active = batch.step()
+        t_in_step += time.perf_counter() - ts
         now = time.perf_counter() - t_start
         for slot in list(pending):
             if batch.member(slot)["done"]:
@@ -288,6 +291,7 @@ def _run_batch(g, torch, pop, precision, increments, seconds):
            "spectral_share": (s1["spectral_ms"] - s0["spectral_ms"]) / ms,
            "round_device_share": (s1["round_device_ms"] - s0["round_device_ms"]) / ms,
            "graph_rounds": s1["graph_rounds"] - s0["graph_rounds"],
+           "host_ms": batch.host_times(), "wall_in_step_s": t_in_step,
            "launches": s1["launches"] - s0["launches"], "autotuned": batch.tuning()}
     batch.close()
     for r, _ in rves:

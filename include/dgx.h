@@ -292,6 +292,10 @@ dgx_status dgx_batch_remove(dgx_batch* batch, int32_t slot);
  * repeat; DGX_GRAPHS=0 in the environment at creation launches every round directly). */
 dgx_status dgx_batch_stats(const dgx_batch* batch, double ms[3], int64_t out[10]);
 void* dgx_batch_stream(const dgx_batch* batch);
+/* Host wall time of the batch's rounds (ms, accumulated): [0] planning and issuing,
+ * [1] waiting for the device, [2] reading results after the wait, [3] advancing the
+ * members' solver logic on the host.  No reference counterpart. */
+dgx_status dgx_batch_host_times(const dgx_batch* batch, double ms[4]);
 /* Cap the residual evaluations served per round at `points` cells (0: no cap).  Above
  * the cap, members with the least remaining work (cells x increments left) go first;
  * a member passed over gains priority every round it waits.  Lowers the latency of

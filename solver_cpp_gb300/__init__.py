@@ -329,6 +329,12 @@ class Batch:
                     state_iterations=a[1], lp_iterations=a[2], rounds=a[3], launches=a[4], jacobians=a[5],
                     h2d_bytes=a[6], d2h_bytes=a[7], fpi_iterations=a[8], graph_rounds=a[9])
 
+    def host_times(self):
+        """Host wall time of the rounds (dgx_batch_host_times): plan / wait / results / advance, ms."""
+        ms = (C.c_double * 4)()
+        _d.check(_d.lib().dgx_batch_host_times(self.h, ms), "dgx_batch_host_times")
+        return dict(plan_issue=ms[0], wait=ms[1], results=ms[2], advance=ms[3])
+
     def set_round_points(self, points):
         """Cap the residual evaluations per round (cells); 0 serves every request."""
         _d.check(_d.lib().dgx_batch_set_round_points(self.h, int(points)), "dgx_batch_set_round_points")

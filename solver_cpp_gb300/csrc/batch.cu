@@ -211,6 +211,9 @@ struct Executor {
   std::map<std::tuple<int, int, int, double, double, double, int, int, int>, SpecLaunch> spec_tuned;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // [4], [5]: a round's first and last copy
   double t_ms[3] = {0, 0, 0};
+  // host wall time of the rounds (ms): [0] planning and issue, [1] waiting for the
+  // device, [2] after the wait (results, tuner), [3] advancing the tasks' host logic
+  double host_ms[4] = {0, 0, 0, 0};
   int64_t t_n[3] = {0, 0, 0};
   int64_t launches = 0, bytes_h2d = 0, bytes_d2h = 0, point_evals = 0, rounds = 0;
   // CUDA graphs of rounds (see ex_issue_round)
@@ -566,7 +569,12 @@ static dgx_status ex_issue_round(Executor* e, RoundPlan& p) {
 // evaluations R = Gamma * P(X) of every request (form_residual: constitutive pass,
 // P_av, stress BC step, spectral pass, divergence RMS), then the fused reductions
 // (which may read the residuals of this round).
+static double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<MultiReq>& mq) {
+  auto h0 = std::chrono::steady_clock::now();
   const int n = (int)q.size();
   if (n > e->cap) { set_err("executor: %d residual requests exceed capacity %d", n, e->cap); return DGX_ERR_STATE; }
   int cand = -1;
@@ -643,8 +651,16 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
   }
   TRY(ex_multi_stage(e, mq, p));
   TRY(ex_issue_round(e, p));
+  e->host_ms[0] += ms_since(h0);
+  h0 = std::chrono::steady_clock::now();
   CK(cudaStreamSynchronize(e->st));
   CK(cudaGetLastError());
+  e->host_ms[1] += ms_since(h0);
+  h0 = std::chrono::steady_clock::now();
+  struct AddOnExit {
+    Executor* e; std::chrono::steady_clock::time_point t0;
+    ~AddOnExit() { e->host_ms[2] += ms_since(t0); }
+  } add_on_exit{e, h0};
   e->rounds++;
   if (n > 0 || p.nm > 0) {
     float ms = 0.f;
@@ -1056,11 +1072,13 @@ static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks, int64_t po
       }
     }
   }
+  const auto h0 = std::chrono::steady_clock::now();
   for (Task* t : served) {
     t->want = 0; t->nmq = 0;
     dgx_status s = advance(*t);
     if (s != DGX_OK) { t->err = s; t->pc = T_DONE; }
   }
+  e->host_ms[3] += ms_since(h0);
   return DGX_OK;
 }
 
@@ -1176,6 +1194,12 @@ extern "C" dgx_status dgx_batch_run(dgx_batch* b) {
   if (!b) return DGX_ERR_ARG;
   int32_t n = 1;
   while (n > 0) TRY(dgx_batch_step(b, &n));
+  return DGX_OK;
+}
+
+extern "C" dgx_status dgx_batch_host_times(const dgx_batch* b, double ms[4]) {
+  if (!b || !ms) return DGX_ERR_ARG;
+  for (int k = 0; k < 4; ++k) ms[k] = b->ex->host_ms[k];
   return DGX_OK;
 }
 

@@ -78,7 +78,7 @@ SYMBOLS = ["dgx_material_default", "dgx_numerics_default", "dgx_rve_create", "dg
            "dgx_result_close", "dgx_restart_write", "dgx_restart_read", "dgx_run_loadcase_output", "dgx_batch_tuning", "dgx_flop_model", "dgx_flop_model_mixed",
            "dgx_batch_set_round_points",
            "dgx_server_set_round_points", "dgx_device_math", "dgx_fields", "dgx_constitutive_response_fields",
-           "dgx_vti_read_cells_size_origin", "dgx_vti_read_dataset_int"]
+           "dgx_vti_read_cells_size_origin", "dgx_vti_read_dataset_int", "dgx_batch_host_times"]
 
 
 class FieldPtrs(C.Structure):
@@ -168,6 +168,7 @@ def lib():
     L.dgx_server_stats.argtypes = [vp, C.POINTER(ServerInfo)]
     L.dgx_divergence_rms_static.argtypes = [ip, dp, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
     L.dgx_fields.argtypes = [vp, C.c_int32, C.POINTER(FieldPtrs)]
+    L.dgx_batch_host_times.argtypes = [vp, dp]
     L.dgx_constitutive_response_fields.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, C.c_int32]
     L.dgx_vti_read_cells_size_origin.argtypes = [C.c_char_p, C.c_int64, ip, dp, dp]
     L.dgx_vti_read_dataset_int.argtypes = [C.c_char_p, C.c_int64, C.c_char_p, C.c_int32, ip, i64p]
