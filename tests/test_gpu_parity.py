@@ -52,12 +52,14 @@ def test_constitutive_sequence_vs_oracle(gpu):
             assert rel(rve.get(name), dgo.from_fortran9(ops.field(name))) < TOL, name
         assert rel(rve.get("xi"), ops.field("xi", 12)) < TOL
         d_or = ops.field("dPdF", 81).reshape(n, 3, 3, 3, 3, order="C").transpose(0, 4, 3, 2, 1)
-        assert rel(dPdF, d_or) < 1e-7
+        e_d = rel(dPdF, d_or)
+        print(f"dPdF vs oracle: {e_d:.2e}")
+        assert e_d < TOL
         Pav, Cv, Cm = rve.averages()
         P_av, Cv_o, Cm_o = dgo.averages(ops.field("P"), ops.field("dPdF", 81))
         assert rel(Pav, dgo.from_fortran9(P_av)) < TOL
-        assert rel(Cv.ravel(order="F"), Cv_o) < 1e-7
-        assert rel(Cm.ravel(order="F"), Cm_o) < 1e-7
+        assert rel(Cv.ravel(order="F"), Cv_o) < TOL
+        assert rel(Cm.ravel(order="F"), Cm_o) < TOL
         rve.commit()
         ops.commit()
 
