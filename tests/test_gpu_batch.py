@@ -162,3 +162,34 @@ def test_single_rve_uses_graphs(gpu):
     rve, steps = _make(gpu, CASES[0], N=3)
     rve.loop_over_loadcase(steps)
     assert rve.counters()["graph_rounds"] > 0
+
+
+def test_batch_of_derivatives_and_prime_grids_equals_solo(gpu):
+    """Members with the forward/backward-difference and central-difference derivatives
+    and grid lengths with prime factors above 16 (two FWBW members of one grid share a
+    size group: the complex-xi z pass, each member's own Gamma table), next to a
+    continuous-derivative member: each bitwise equal to its solo run."""
+    cases = [((17, 6, 5), 5, 21, "tensionX", "fp64", "FWBW_difference"),
+             ((17, 6, 5), 4, 22, "shearXY", "fp64", "FWBW_difference"),
+             ((12, 10, 9), 6, 23, "tensionY", "fp64", "central_difference"),
+             ((19, 4, 6), 3, 24, "tensionZ", "mixed", "continuous"),
+             ((8, 8, 8), 5, 25, "tensionX", "mixed", "FWBW_difference")]
+
+    def make(c):
+        cells, ng, seed, kind, prec, deriv = c
+        mat, q = synthetic.microstructure(cells, ng, seed)
+        size = tuple(n / max(cells) for n in cells)
+        rve = gpu.RVE(cells, size, mat, q, num=gpu.numerics(precision=prec, derivative=deriv))
+        return rve, [gpu.load_step(kind, t=3.0, N=3)]
+
+    solo = [r.loop_over_loadcase(s) for r, s in (make(c) for c in cases)]
+    batch = gpu.Batch(len(cases))
+    members = [make(c) for c in cases]
+    slots = [batch.add(r, s) for r, s in members]
+    batch.run()
+    ht = batch.host_times()
+    assert min(ht.values()) >= 0.0 and ht["wait"] > 0.0 and ht["advance"] > 0.0
+    for slot, srecs in zip(slots, solo):
+        m = batch.member(slot)
+        assert m["done"] and m["status"] == 0
+        _same(batch.records(slot), srecs)
