@@ -67,5 +67,6 @@ def test_static_divergence_rms_rejects_bad_arguments():
     # divergence correction outside none / size / size+grid
     assert _static_rms(lib, (4, 4, 4), (1.0, 1.0, 1.0), 3, 0, P.data_ptr(), out.data_ptr(), 0) == -1
     assert _static_rms(lib, (4, 4, 4), (1.0, 1.0, 1.0), -1, 0, P.data_ptr(), out.data_ptr(), 0) == -1
-    # unknown derivative
+    # unknown derivative; the forward/backward difference is not offered here
     assert _static_rms(lib, (4, 4, 4), (1.0, 1.0, 1.0), 2, 7, P.data_ptr(), out.data_ptr(), 0) == -1
+    assert _static_rms(lib, (4, 4, 4), (1.0, 1.0, 1.0), 2, 2, P.data_ptr(), out.data_ptr(), 0) == -4
