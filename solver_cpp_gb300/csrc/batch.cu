@@ -181,6 +181,47 @@ constexpr int TUNE_TRIALS = 5;               // interleaved timed rounds per con
 constexpr long long LARGE_ROUND_POINTS = 152LL * 128 * 4 * 2;
 constexpr int LARGE_VARIANT_MIXED = 5, LARGE_VARIANT_FP64 = 1;
 
+// ------------------------------------------------------------------ members' vector ops
+// The NGMRES vector operations a member's host logic decides between two rounds
+// (x^M = x - F, the combination x^A = c0 x^M + sum beta_i x_i, the history copies) are
+// recorded and run at the start of the next round as one launch per position in the
+// members' sequences, instead of one API call each.  The arithmetic per element is that
+// of k_axpy / k_combine (solver.cu), so results are bitwise the same.
+constexpr int PREOP_MAX_L = 30;       // NGMRES window (ngmres_m <= 30)
+constexpr int PREOP_LEVELS = 4;       // ops a member records between two rounds (at most 3)
+struct PreOp {
+  int kind;                           // 0 copy z = x, 1 axpy z = x + a y, 2 combine z = a x + sum_i beta_i v_i
+  int l;
+  int64_t n;
+  double* z;
+  const double* x;
+  const double* y;
+  double a;
+  double beta[PREOP_MAX_L];
+  const double* v[PREOP_MAX_L];
+};
+
+__global__ void __launch_bounds__(256) k_preops(const PreOp* __restrict__ ops) {
+  const PreOp& op = ops[blockIdx.y];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  if (op.kind == 0) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < op.n; t += stride) op.z[t] = op.x[t];
+  } else if (op.kind == 1) {
+    const double a = op.a;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < op.n; t += stride) op.z[t] = op.x[t] + a * op.y[t];
+  } else {
+    __shared__ double sb[32];
+    if (threadIdx.x < 32) sb[threadIdx.x] = threadIdx.x < op.l ? op.beta[threadIdx.x] : 0.0;
+    __syncthreads();
+    const double c0 = op.a;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < op.n; t += stride) {
+      double v = op.x[t] * c0;
+      for (int i = 0; i < op.l; ++i) v += sb[i] * op.v[i][t];
+      op.z[t] = v;
+    }
+  }
+}
+
 struct Executor {
   cudaStream_t st = nullptr;
   int cap = 0;                               // residual items per round; 2 cap reductions
@@ -192,6 +233,7 @@ struct Executor {
   int* h_ill = nullptr; double* h_Pav = nullptr; double* h_rms = nullptr;
   double* h_mout = nullptr;
   BcItem* d_bcitem = nullptr; BcItem* h_bcitem = nullptr;
+  PreOp* d_preop = nullptr; PreOp* h_preop = nullptr;   // the members' recorded vector ops, by level
   double* d_bcout = nullptr; double* h_bcout = nullptr;
   ConsCounters* cnt = nullptr;
   bool own_cnt = false;
@@ -257,6 +299,7 @@ dgx_status executor_create(int cap, cudaStream_t st, ConsCounters* cnt, int cons
   EA(&e->d_cons, &e->h_cons, cap);
   EA(&e->d_spec, &e->h_spec, cap);
   EA(&e->d_multi, &e->h_multi, 2 * cap);
+  EA(&e->d_preop, &e->h_preop, (size_t)PREOP_LEVELS * cap);
   EA(&e->d_ill, &e->h_ill, cap);
   EA(&e->d_Pav, &e->h_Pav, 9 * cap);
   EA(&e->d_aim, (double**)nullptr, 9 * cap);
@@ -386,6 +429,7 @@ struct SpecGroup {
 };
 struct RoundPlan {
   int n = 0, nm = 0, maxnb = 1, variant = 1;
+  int npre[PREOP_LEVELS] = {0, 0, 0, 0}, prenb[PREOP_LEVELS] = {0, 0, 0, 0};   // ops and blocks per level
   bool cnt_d2h = false;
   std::vector<ConsGroup> cons;
   std::vector<SpecGroup> spec;
@@ -402,6 +446,7 @@ constexpr size_t MATPARAMS_BYTES = offsetof(MatParams, a_quarters) + sizeof(int)
 static std::string plan_signature(const RoundPlan& p) {
   Sig s;
   s.put(p.n); s.put(p.nm); s.put(p.maxnb); s.put(p.variant); s.put(p.cnt_d2h);
+  for (int k = 0; k < PREOP_LEVELS; ++k) { s.put(p.npre[k]); s.put(p.prenb[k]); }
   for (const ConsGroup& c : p.cons) { s.put(c.j0); s.put(c.cnt); s.put(c.grid); s.put(c.tiles); s.raw(c.mp, MATPARAMS_BYTES); }
   for (const SpecGroup& g : p.spec) {
     const SpecLaunch& L = *g.L;
@@ -454,6 +499,20 @@ static dgx_status ex_issue(Executor* e, RoundPlan& p, bool capture, IssueCount& 
   auto d2h = [&](void* h, const void* d, size_t b) { c.d2h += (int64_t)b; return cudaMemcpyAsync(h, d, b, cudaMemcpyDeviceToHost, st); };
   const int n = p.n;
   CK(rec(4));
+  {
+    int tot = 0;
+    for (int k = 0; k < PREOP_LEVELS; ++k) tot += p.npre[k];
+    if (tot > 0) {
+      CK(h2d(e->d_preop, e->h_preop, sizeof(PreOp) * tot));
+      int off = 0;
+      for (int k = 0; k < PREOP_LEVELS; ++k) {
+        if (p.npre[k] == 0) continue;
+        k_preops<<<dim3(p.prenb[k], p.npre[k]), 256, 0, st>>>(e->d_preop + off);
+        c.launches++;
+        off += p.npre[k];
+      }
+    }
+  }
   if (n > 0) {
     CK(cudaMemsetAsync(e->d_ill, 0, sizeof(int) * n, st));
     CK(cudaMemsetAsync(e->d_queue, 0, sizeof(unsigned long long) * e->qcap, st));
@@ -573,7 +632,10 @@ static double ms_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<MultiReq>& mq) {
+// npre / maxn: the members' recorded vector ops staged in h_preop by level (counts and
+// the longest vector of each level)
+static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<MultiReq>& mq,
+                           const int npre[PREOP_LEVELS], const int64_t maxn[PREOP_LEVELS]) {
   auto h0 = std::chrono::steady_clock::now();
   const int n = (int)q.size();
   if (n > e->cap) { set_err("executor: %d residual requests exceed capacity %d", n, e->cap); return DGX_ERR_STATE; }
@@ -582,6 +644,10 @@ static dgx_status ex_round(Executor* e, std::vector<ResReq>& q, std::vector<Mult
   std::vector<int> slot_of(n);
   RoundPlan p;
   p.n = n;
+  for (int k = 0; k < PREOP_LEVELS; ++k) {
+    p.npre[k] = npre[k];
+    p.prenb[k] = npre[k] ? (int)std::min<int64_t>(1216, (maxn[k] + 255) / 256) : 0;
+  }
   if (n > 0) {
     // constitutive pass: items grouped by material, largest RVEs first in the tile queue
     std::vector<int> order(n);
@@ -766,6 +832,7 @@ struct Task {
   double *X = nullptr, *F = nullptr;
   double fnorm = 0.0, fminnorm = 0.0, fMnorm = 0.0;
   std::vector<double> qm, beta, xi, tmp, tmpA;
+  std::vector<PreOp> ops;             // vector ops recorded since the last round, in order
   bool done() const { return pc == T_DONE; }
   const dgx_loadstep* cur_step() const { return mode == 2 ? &steps[l] : steps; }
 };
@@ -779,16 +846,62 @@ static void req_multi(Task& t, int mode, const double* a, const double* b, const
   t.nmq++;
   t.want |= 2;
 }
-static dgx_status d2d9(dgx_rve* r, double* dst, const double* src) {
-  CK(cudaMemcpyAsync(dst, src, sizeof(double) * 9 * r->N, cudaMemcpyDeviceToDevice, r->st));
+// Issue a member's recorded vector ops directly, in order (before work of its own on the
+// stream that reads or writes the same vectors, and when more ops are recorded than a
+// round takes).
+static dgx_status flush_ops(Task& t) {
+  dgx_rve* r = t.r;
+  for (const PreOp& op : t.ops) {
+    if (op.kind == 0) {
+      CK(cudaMemcpyAsync(op.z, op.x, sizeof(double) * op.n, cudaMemcpyDeviceToDevice, r->st));
+    } else if (op.kind == 1) {
+      launch_axpy(op.z, op.x, op.a, op.y, op.n, r->st);
+      r->n_launch++;
+    } else {
+      VecList xl{};
+      for (int i = 0; i < op.l; ++i) xl.v[i] = op.v[i];
+      CK(h2d(r, r->d_beta, op.beta, sizeof(double) * op.l));
+      launch_combine(op.z, op.x, xl, op.l, op.a, r->d_beta, op.n, r->nb_red, r->st);
+      r->n_launch++;
+    }
+    // the combination's coefficients are read from host memory by the copy above
+    // (pageable: staged before the call returns), so the record may go
+    CK(cudaGetLastError());
+  }
+  t.ops.clear();
   return DGX_OK;
+}
+static dgx_status record_op(Task& t, const PreOp& op) {
+  if ((int)t.ops.size() >= PREOP_LEVELS) TRY(flush_ops(t));
+  t.ops.push_back(op);
+  return DGX_OK;
+}
+static dgx_status op_copy(Task& t, double* dst, const double* src) {
+  PreOp op{};
+  op.kind = 0; op.n = 9 * t.r->N; op.z = dst; op.x = src;
+  return record_op(t, op);
+}
+static dgx_status op_axpy(Task& t, double* z, const double* x, double a, const double* y) {
+  PreOp op{};
+  op.kind = 1; op.n = 9 * t.r->N; op.z = z; op.x = x; op.y = y; op.a = a;
+  return record_op(t, op);
+}
+static dgx_status op_combine(Task& t, double* z, const double* x, double c0, const double* beta, int l) {
+  if (l > PREOP_MAX_L) { set_err("NGMRES window above %d", PREOP_MAX_L); return DGX_ERR_ARG; }
+  PreOp op{};
+  op.kind = 2; op.n = 9 * t.r->N; op.z = z; op.x = x; op.a = c0; op.l = l;
+  for (int i = 0; i < l; ++i) { op.beta[i] = beta[i]; op.v[i] = t.r->Xdot[i]; }
+  return record_op(t, op);
 }
 
 // run the task's host logic until it parks a device request or finishes
 static dgx_status advance(Task& t) {
   dgx_rve* r = t.r;
-  const int64_t n9 = 9 * r->N;
   for (;;) {
+    // states that issue work of their own on the stream run after the recorded ops
+    if (!t.ops.empty() && (t.pc == T_LC_BEGIN || t.pc == T_SUB_CHECK || t.pc == T_SOLVE_BEGIN ||
+                           t.pc == T_SOLVE_END || t.pc == T_INC_END || t.pc == T_DONE))
+      TRY(flush_ops(t));
     switch (t.pc) {
       case T_LC_BEGIN:
         t.l = 0; t.inc = 0; t.nrec = 0; t.total = 0;
@@ -843,7 +956,7 @@ static dgx_status advance(Task& t) {
         if (r->num.solver == 1) { t.pc = T_FP_ITER; break; }
         const int m = r->num.ngmres_m;
         t.qm.assign((size_t)m * m, 0.0); t.beta.assign(m, 0.0); t.xi.assign(m, 0.0);
-        TRY(d2d9(r, r->Fdot[0], t.F)); TRY(d2d9(r, r->Xdot[0], t.X));
+        TRY(op_copy(t, r->Fdot[0], t.F)); TRY(op_copy(t, r->Xdot[0], t.X));
         t.k_restart = 1; t.lh = 1; t.ivec = 0; t.restart_count = 0;
         t.pc = T_N_ITER;
         break;
@@ -851,8 +964,7 @@ static dgx_status advance(Task& t) {
       // ---- fixed point: X <- X - F
       case T_FP_ITER:
         if (t.k > r->num.snes_max_it) { t.reason = -1; t.pc = T_SOLVE_END; break; }
-        launch_axpy(t.X, t.X, -1.0, t.F, n9, r->st);
-        r->n_launch++;
+        TRY(op_axpy(t, t.X, t.X, -1.0, t.F));
         r->total_iter = t.k;
         req_residual(t, t.X, t.F);
         req_multi(t, 0, t.F, nullptr, {t.F}, 0, t.tmp.data());
@@ -870,8 +982,7 @@ static dgx_status advance(Task& t) {
       // ---- NGMRES iteration k
       case T_N_ITER:
         if (t.k > r->num.snes_max_it) { t.reason = 0; t.pc = T_SOLVE_END; break; }
-        launch_axpy(r->XM, t.X, -1.0, t.F, n9, r->st);       // x^M = x - F(x) (basic line search)
-        r->n_launch++;
+        TRY(op_axpy(t, r->XM, t.X, -1.0, t.F));             // x^M = x - F(x) (basic line search)
         r->total_iter = t.k;
         req_residual(t, r->XM, r->FM);
         {
@@ -900,11 +1011,7 @@ static dgx_status advance(Task& t) {
           if (!std::isfinite(t.beta[i])) { set_err("NGMRES: non-finite coefficient"); return DGX_ERR_STATE; }
         double alph = 0.0;
         for (int i = 0; i < l; ++i) alph += t.beta[i];
-        VecList xl{};
-        for (int i = 0; i < l; ++i) xl.v[i] = r->Xdot[i];
-        CK(h2d(r, r->d_beta, t.beta.data(), sizeof(double) * l));
-        launch_combine(r->XA, r->XM, xl, l, 1.0 - alph, r->d_beta, n9, r->nb_red, r->st);
-        r->n_launch++;
+        TRY(op_combine(t, r->XA, r->XM, 1.0 - alph, t.beta.data(), l));
         if (t.fminnorm > t.fMnorm) t.fminnorm = t.fMnorm;
         req_residual(t, r->XA, r->FA);
         // |FA|^2 ; |XA - XM|^2, |XA - Xdot_i|^2 after the residual
@@ -934,12 +1041,12 @@ static dgx_status advance(Task& t) {
           t.restart_count = 0; t.k_restart = 1; t.lh = 1; t.ivec = 0;
           const double* srcF = selectA ? r->FM : t.F;    // the x^M pair, wherever it now lives
           const double* srcX = selectA ? r->XM : t.X;
-          TRY(d2d9(r, r->Fdot[0], srcF)); TRY(d2d9(r, r->Xdot[0], srcX));
+          TRY(op_copy(t, r->Fdot[0], srcF)); TRY(op_copy(t, r->Xdot[0], srcX));
         } else {
           if (t.lh < m) t.lh++;
           t.k_restart++;
           if (t.fminnorm > t.fnorm) t.fminnorm = t.fnorm;
-          TRY(d2d9(r, r->Fdot[t.ivec], t.F)); TRY(d2d9(r, r->Xdot[t.ivec], t.X));
+          TRY(op_copy(t, r->Fdot[t.ivec], t.F)); TRY(op_copy(t, r->Xdot[t.ivec], t.X));
         }
         t.reason = converged(r);
         if (t.reason) { t.pc = T_SOLVE_END; break; }
@@ -1057,7 +1164,23 @@ static dgx_status serve_round(Executor* e, std::vector<Task*>& tasks, int64_t po
   for (Task* t : res_tasks) { rq.push_back({t->r, t->rin, t->rout}); t->skips = 0; served.push_back(t); }
   std::vector<MultiReq> mq;
   for (Task* t : served) for (int i = 0; i < t->nmq; ++i) mq.push_back(t->mq[i]);
-  TRY(ex_round(e, rq, mq));
+  // the served members' recorded vector ops, staged level by level (op k of every member
+  // in one launch at the start of the round)
+  int npre[PREOP_LEVELS] = {0, 0, 0, 0};
+  int64_t maxn[PREOP_LEVELS] = {0, 0, 0, 0};
+  {
+    int off = 0;
+    for (int k = 0; k < PREOP_LEVELS; ++k)
+      for (Task* t : served)
+        if ((int)t->ops.size() > k) {
+          if (off >= PREOP_LEVELS * e->cap) { set_err("executor: vector ops exceed capacity"); return DGX_ERR_STATE; }
+          e->h_preop[off++] = t->ops[k];
+          npre[k]++;
+          maxn[k] = std::max(maxn[k], t->ops[k].n);
+        }
+    for (Task* t : served) t->ops.clear();
+  }
+  TRY(ex_round(e, rq, mq, npre, maxn));
   if (!tan_tasks.empty()) {
     CK(cudaStreamSynchronize(e->st));
     for (size_t i = 0; i < tan_tasks.size(); ++i) {
