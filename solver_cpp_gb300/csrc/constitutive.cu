@@ -603,10 +603,11 @@ __device__ __forceinline__ bool jacobian_step(const MatParams& mp, const R* A, c
   return true;
 }
 
-// The mixed form's FP32 Newton direction as one out-of-line function shared by its two
-// call sites (the Newton step and the first-order start): one copy of the code keeps
-// the kernel's instruction footprint down.
-__device__ __noinline__ bool jacobian_step_f32(const MatParams& mp, const float* A, const float* Fe_, double dt,
+// The mixed form's FP32 Newton direction, at its two call sites (the Newton step and the
+// first-order start).  Inlined: as an out-of-line function (one copy of its code) each
+// call saved and restored the caller's live registers through local memory, 2 % slower
+// per launch at 64^3.
+__device__ __forceinline__ bool jacobian_step_f32(const MatParams& mp, const float* A, const float* Fe_, double dt,
                                                const float* dg, const double* res, double* dLp) {
   return jacobian_step<float, double>(mp, A, Fe_, dt, dg, res, dLp);
 }
@@ -639,20 +640,30 @@ __device__ __forceinline__ void plane_butterfly(const T* g, T* L) {
 }
 
 // Mixed form: what a first-order start of the next Lp Newton needs from the converged
-// one of the previous fixed-point pass (FP32): Fe, r = |tau| prxi, prxi and the slip
-// rates g there, and the state change of the xi half that followed (xi - xi').
-// mode 2 (first pass of a warm evaluation): g holds the precomputed u_a of the change
-// of Lp(S) and dxi is unused.
+// one of the previous fixed-point pass (FP32): Fe and r = |tau| prxi there, and in g
+// the slip rates g_a of that solution; the state update that follows multiplies them
+// by n (xi - xi') (mode 1).  mode 2 (first pass of a warm evaluation): g holds the
+// precomputed u_a of the change of Lp(S).  35 words per thread (odd: no shared-memory
+// bank conflicts between the threads' records).
 struct LpPredictor {
-  bool valid;
-  int mode;                          // 1: change of the slip resistances, 2: u given
-  float Fe[9], r[NSLIP], prxi[NSLIP], g[NSLIP], dxi[NSLIP];
+  int valid, mode;                   // mode 1: g = n g_a (xi_a - xi'_a), 2: g = u_a
+  float Fe[9], r[NSLIP], g[NSLIP];
 };
 
 // The previous evaluation of the same step (planes of stride ld at one cell): its
 // deformation gradient, elastic deformation gradient, stress and converged state.
 struct WarmPrev {
   const double *F, *Fe, *S, *st;
+  int64_t ld;
+};
+
+// Mixed form: where the Lp Newton keeps its line-search data (the last accepted
+// iterate and the last direction), read back only when a step is rejected: two sets
+// of 9 planes of stride ld at one cell (the cell's P and Fp output planes, which the
+// constitutive kernel writes only once the cell is done), so that they occupy no
+// registers through the iteration.
+struct LsBuf {
+  double *old, *dir;
   int64_t ld;
 };
 
@@ -663,12 +674,14 @@ struct WarmPrev {
 // (pr->valid) gives the Newton a first-order start, Lp + J^-1 dLp_c with dLp_c the
 // change of Lp(S) from the new slip resistances, dg_a / dprxi_a = n g_a / prxi_a, and J
 // the FP32 Jacobian at the previous solution; on convergence the solution's data are
-// stored for the next pass.  The iteration from that start is the same FP64 Newton.
+// stored for the next pass.  The iteration from that start is the same FP64 Newton;
+// its line-search data (last accepted iterate, last direction) live in the planes of
+// ls (not null in the mixed form).
 template <bool MX>
 __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt, const double* prxi, double* Lp,
                                  double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters,
-                                 LpPredictor* pr = nullptr) {
-  double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
+                                 LpPredictor* pr = nullptr, const LsBuf* ls = nullptr) {
+  double Lpg[9], Lpg_old[MX ? 1 : 9], dLp[9], B[9], Fe_[9];
   float Af[MX ? 9 : 1], prxi_f[MX ? NSLIP : 1];
   if constexpr (MX) {
 #pragma unroll
@@ -680,13 +693,15 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
   for (int k = 0; k < 9; ++k) Lpg[k] = Lp[k];
   if constexpr (MX) {
     if (pr && pr->valid) {
-      // u_a = n g_a rho_a, rho_a = prxi'_a / prxi_a - 1 = (xi_a - xi'_a) / xi'_a
+      // u_a = n g_a rho_a, rho_a = prxi'_a / prxi_a - 1 = (xi_a - xi'_a) / xi'_a; the
+      // derivative at the previous solution prxi r^(n-1) takes the new prxi' (the two
+      // differ by rho, which only scales the start's correction)
       float u[NSLIP], dg0[NSLIP], dLc[9];
       double delta_[9], delta[9];
 #pragma unroll
       for (int a = 0; a < NSLIP; ++a) {
-        u[a] = pr->mode == 2 ? pr->g[a] : mp.n_f * pr->g[a] * (pr->dxi[a] * (prxi_f[a] * mp.rpval_f));
-        dg0[a] = pr->prxi[a] * pow_nm1_f(pr->r[a], mp);
+        u[a] = pr->mode == 2 ? pr->g[a] : pr->g[a] * (prxi_f[a] * mp.rpval_f);
+        dg0[a] = prxi_f[a] * pow_nm1_f(pr->r[a], mp);
       }
       plane_butterfly(u, dLc);
 #pragma unroll
@@ -704,8 +719,10 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       pr->valid = false;
     }
   }
+  if constexpr (!MX) {
 #pragma unroll
-  for (int k = 0; k < 9; ++k) { Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
+    for (int k = 0; k < 9; ++k) { Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
+  }
   long long res_old_n = 0;
   double step = 1.0;
   int jaco = 0;
@@ -716,6 +733,11 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     for (int k = 0; k < 9; ++k) B[k] = ((k % 4) == 0 ? 1.0 : 0.0) - dt * Lpg[k];
     mm(A, B, Fe_);
     hooke_S(mp, Fe_, S);
+    float Fef[MX ? 9 : 1];                     // mixed form: Fe for the FP32 Jacobian and the predictor
+    if constexpr (MX) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Fef[k] = to_f32(Fe_[k]);
+    }
     // slip rates (units of gdot0) and what the Jacobian needs of them: plain form
     // r^(n-1) (dg = prxi r^(n-1) is formed with the Jacobian), mixed form r in FP32
     using KT = typename std::conditional<MX, float, double>::type;
@@ -792,10 +814,10 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       if constexpr (MX) {
         if (pr) {
 #pragma unroll
-          for (int k = 0; k < 9; ++k) pr->Fe[k] = to_f32(Fe_[k]);
+          for (int k = 0; k < 9; ++k) pr->Fe[k] = Fef[k];
 #pragma unroll
           for (int a = 0; a < NSLIP; ++a) {
-            pr->r[a] = kaux[a]; pr->prxi[a] = prxi_f[a]; pr->g[a] = to_f32(gdot[a]);
+            pr->r[a] = kaux[a]; pr->g[a] = to_f32(gdot[a]);
           }
           pr->valid = true;
           pr->mode = 1;
@@ -805,13 +827,23 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     }
     if (it == 1 || nr2b < res_old_n) {
       res_old_n = nr2b;
+      if constexpr (MX) {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
+        for (int k = 0; k < 9; ++k) ls->old[k * ls->ld] = Lpg[k];
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
+      }
       step = 1.0;
     } else {
       step *= mp.r_linesearch_Lp;
+      if constexpr (MX) {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg_old[k]);
+        for (int k = 0; k < 9; ++k) Lpg[k] = fma(ls->dir[k * ls->ld], step, ls->old[k * ls->ld]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg_old[k]);
+      }
       continue;
     }
     if (jaco % mp.f_update_jacobi_Lp == 0) {
@@ -825,14 +857,18 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
         else dg[a] = prxi[a] * kaux[a];
       }
       if constexpr (MX) {
-        float Fef[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Fef[k] = to_f32(Fe_[k]);
         ok = jacobian_step_f32(mp, Af, Fef, dt, dg, res, dLp);
       } else {
         ok = jacobian_step<double, double>(mp, A, Fe_, dt, dg, res, dLp);
       }
       if (!ok) return true;
+      if constexpr (MX) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) ls->dir[k * ls->ld] = dLp[k];
+      }
+    } else if constexpr (MX) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dLp[k] = ls->dir[k * ls->ld];
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg[k]);
@@ -857,6 +893,28 @@ __device__ bool stress_outputs(const double* F, const double* invFp0, double dt,
              - Fp_new[3] * (Fp_new[1] * Fp_new[8] - Fp_new[7] * Fp_new[2])
              + Fp_new[6] * (Fp_new[1] * Fp_new[5] - Fp_new[4] * Fp_new[2]);
   // Fp / det(Fp)^(1/3); a non-positive determinant gives NaN as the power would
+  const double rs = dFp > 0.0 ? rcbrt(dFp) : __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) { Fp[k] = Fp_new[k] * rs; Fe[k] = t1[k]; }
+  return false;
+}
+
+// Mixed form of stress_outputs with Fe = A (I - dt Lp), A = F Fp0^-1 (the Newton's own
+// elastic deformation gradient), so that F need not be kept through the iteration.
+__device__ bool stress_outputs_mx(const double* A, const double* invFp0, double dt, const double* Lp, const double* S,
+                                  double* P, double* Fp, double* Fe) {
+  double B[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) B[k] = ((k % 4) == 0 ? 1.0 : 0.0) - dt * Lp[k];
+  double invFp_new[9], Fp_new[9], t1[9], t2[9], det;
+  mm(invFp0, B, invFp_new);
+  if (!inv33(invFp_new, Fp_new, &det)) return true;
+  mm(A, B, t1);
+  mmt(S, invFp_new, t2);
+  mm(t1, t2, P);
+  double dFp = Fp_new[0] * (Fp_new[4] * Fp_new[8] - Fp_new[7] * Fp_new[5])
+             - Fp_new[3] * (Fp_new[1] * Fp_new[8] - Fp_new[7] * Fp_new[2])
+             + Fp_new[6] * (Fp_new[1] * Fp_new[5] - Fp_new[4] * Fp_new[2]);
   const double rs = dFp > 0.0 ? rcbrt(dFp) : __longlong_as_double(0x7ff8000000000000LL);
 #pragma unroll
   for (int k = 0; k < 9; ++k) { Fp[k] = Fp_new[k] * rs; Fe[k] = t1[k]; }
@@ -899,29 +957,76 @@ __device__ __forceinline__ R damper(const R* o0, const Hist<DT>& h) {
 __device__ __forceinline__ bool bad_rate(double x) { return nan_bits(x); }
 __device__ __forceinline__ bool bad_rate(float x) { return absbits(x) >= 0x7f800000; }
 
-// integrateStateFPI; returns true if broken.  S on entry: stress used for the
-// first dot state (restored committed stress); state in/out; on success Lp, S and
-// the state are the converged ones and the caller forms P, Fp, Fe (stress_outputs).
+// integrateStateFPI (plain FP64 form); returns true if broken.  S on entry: stress used
+// for the first dot state (restored committed stress); state in/out; on success Lp, S
+// and the state are the converged ones and the caller forms P, Fp, Fe (stress_outputs).
 // A = F Fp0^-1 is fixed for the whole iteration.
-// guess (mixed form, may be null): a state (planes of stride gld) that replaces the
-// explicit predictor state0 + dot(S) dt as the iteration's start, with the rate it
-// implies, (guess - state0) / dt, as the first rate of the damper's history.  The
-// fixed point and its FP64 test are unchanged.
-template <bool MX>
-__device__ bool integrate_state(const MatParams& mp, const double* F, const double* A, const double* invFp0,
-                                StateRef state0, double dt, double* state, double* Lp, double* S,
-                                const Hist<typename std::conditional<MX, float, double>::type>& hist,
-                                LpPredictor* pred_s, unsigned* lp_iters, unsigned* jac_iters, unsigned* st_iters,
-                                unsigned* fpi_iters, const WarmPrev* wp = nullptr) {
-  // rates: FP64 in the plain form, FP32 in the mixed form
-  using DT = typename std::conditional<MX, float, double>::type;
-  DT dot[2 * NSLIP];
+__device__ bool integrate_state(const MatParams& mp, const double* A, StateRef state0, double dt, double* state,
+                                double* Lp, double* S, const Hist<double>& hist, unsigned* lp_iters,
+                                unsigned* jac_iters, unsigned* st_iters, unsigned* fpi_iters) {
+  double dot[2 * NSLIP];
   double prxi[NSLIP], gdot[NSLIP];
-  // pred_s (mixed form only): start of the next pass's Lp Newton
-  if constexpr (MX) pred_s->valid = false;
+  (*st_iters)++;
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
+  dot_state(mp, S, state, prxi, dot);
+  bool nan = false;
+#pragma unroll
+  for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
+  if (nan) return true;
+#pragma unroll
+  for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(dot[i], dt, state0[i]);
+  for (int it = 1; it <= mp.N_iter_state_max; ++it) {
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) { hist.l2(i) = it > 1 ? hist.l1(i) : 0.0; hist.l1(i) = dot[i]; }
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
+    (*fpi_iters)++;
+    if (integrate_stress<false>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters)) return true;
+    dot_state(mp, S, state, prxi, dot, gdot);
+    nan = false;
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
+    if (nan) return true;
+    const double z = damper(dot, hist);
+    bool conv = true;
+#pragma unroll
+    for (int i = 0; i < 2 * NSLIP; ++i) {
+      const double d = dot[i] * z + hist.l1(i) * (1.0 - z);
+      double r = state[i] - state0[i] - d * dt;
+      state[i] = state[i] - r;
+      // |r| <= max(atol, eps |state|), compared exactly as integers (r and state are
+      // not NaN here: a NaN dot state ended the iteration above)
+      const long long atol = absbits(i < NSLIP ? mp.atol_xi : mp.atol_gamma);
+      conv &= absbits(r) <= max(atol, absbits(mp.eps_rel_state * state[i]));
+      dot[i] = d;
+    }
+    if (conv) return false;
+  }
+  return true;
+}
+
+// Mixed form of integrateStateFPI.  The iterate is not held between the state
+// updates: with the current FP32 rate D (the damper's newest history entry, in shared
+// memory) it is x = state0 + D dt, formed in FP64 where it is needed (the slip
+// resistances of a pass, the update and its test), so the Lp Newton between two
+// updates keeps none of the 24 state values in registers.  The iteration is the FP64
+// form's: the damped rate d, x_new = state0 + d dt, the residual r = x - x_new and the
+// test |r| <= max(atol, eps |x_new|) in FP64.  A guess (warm start) enters as its rate
+// (guess - state0) / dt in FP32, i.e. as state0 + D dt (within FP32 rounding of the
+// increment, far below the tolerances).  On entry state holds state0 (the callers
+// restore it); on success it receives the converged state.  Returns true if broken.
+__device__ bool integrate_state_mx(const MatParams& mp, const double* F, const double* A, const double* invFp0,
+                                   StateRef state0, double dt, double* state, double* Lp, double* S,
+                                   const Hist<float>& hist, LpPredictor* pred_s, unsigned* lp_iters,
+                                   unsigned* jac_iters, unsigned* st_iters, unsigned* fpi_iters,
+                                   const WarmPrev* wp, const LsBuf* ls) {
+  float dot[2 * NSLIP];
+  double gdot[NSLIP];
+  pred_s->valid = false;
   (*st_iters)++;
   bool seeded = false;
-  if (MX && wp && dt > 0.0) {
+  if (wp && dt > 0.0) {
     // the guess seeds the iteration only if its slip resistances are positive and its
     // implied rates finite; otherwise the explicit predictor below is used
     const float rdt = to_f32(rcp(dt));
@@ -929,126 +1034,111 @@ __device__ bool integrate_state(const MatParams& mp, const double* F, const doub
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) {
       const double g = wp->st[i * wp->ld];
-      dot[i] = (DT)to_f32(g - state0[i]) * (DT)rdt;
+      dot[i] = to_f32(g - state0[i]) * rdt;
       ok &= !bad_rate(dot[i]) && (i >= NSLIP || g > 0.0);
     }
-    if (ok) {
-#pragma unroll
-      for (int i = 0; i < 2 * NSLIP; ++i) state[i] = wp->st[i * wp->ld];
-      seeded = true;
-    }
+    seeded = ok;
   }
-  if constexpr (MX) {
-    if (seeded) {
-      // first-order start of the first pass: the previous evaluation converged at Lp for
-      // F_prev and the same slip resistances, so R(Lp; F) ~ -dLp_c with dLp_c the change
-      // of Lp(S) from dF = F - F_prev: dFe = dF Fp0^-1 (I - dt Lp), 2 dE = Fe^T dFe +
-      // dFe^T Fe, dS = C : dE, dt_a = d_a . (dS n_a), u_a = n prxi r^(n-1) dt_a (FP32)
-      float M[9], dF[9], dFe[9], Fep[9], Sp[9], B[9];
+  if (seeded) {
+    // first-order start of the first pass (as in integrate_state): R(Lp; F) ~ -dLp_c,
+    // dLp_c the change of Lp(S) from dF = F - F_prev at the guess's slip resistances
+    float M[9], dF[9], dFe[9], Fep[9], Sp[9], B[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        dF[k] = to_f32(F[k] - wp->F[k * wp->ld]);
-        Fep[k] = to_f32(wp->Fe[k * wp->ld]);
-        Sp[k] = to_f32(wp->S[k * wp->ld]);
-        B[k] = ((k % 4) == 0 ? 1.0f : 0.0f) - to_f32(dt) * to_f32(Lp[k]);
-        M[k] = to_f32(invFp0[k]);
-      }
-      float IB[9];
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) IB[i + 3 * j] = M[i] * B[3 * j] + M[i + 3] * B[1 + 3 * j] + M[i + 6] * B[2 + 3 * j];
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) dFe[i + 3 * j] = dF[i] * IB[3 * j] + dF[i + 3] * IB[1 + 3 * j] + dF[i + 6] * IB[2 + 3 * j];
-      // 2 dE (symmetric), then dS by the cubic Hooke law on 2 dE with the halved moduli
-      float E2[9];
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int i = 0; i <= j; ++i) {
-          float v = 0.0f;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) v += Fep[k + 3 * i] * dFe[k + 3 * j] + dFe[k + 3 * i] * Fep[k + 3 * j];
-          E2[i + 3 * j] = v; E2[j + 3 * i] = v;
-        }
-      float dS[9];
-      const float ct = mp.hC12_f * (E2[0] + E2[4] + E2[8]);
-      dS[0] = fmaf(mp.hC11mC12_f, E2[0], ct);
-      dS[4] = fmaf(mp.hC11mC12_f, E2[4], ct);
-      dS[8] = fmaf(mp.hC11mC12_f, E2[8], ct);
-      dS[5] = dS[7] = mp.C44_f * E2[7];
-      dS[2] = dS[6] = mp.C44_f * E2[6];
-      dS[1] = dS[3] = mp.C44_f * E2[3];
-      float tp[NSLIP], dtt[NSLIP];
-      resolved_shear(Sp, tp);
-      resolved_shear(dS, dtt);
-#pragma unroll
-      for (int a = 0; a < NSLIP; ++a) {
-        const float px = mp.pval_f * rcp(to_f32(state[a]));
-        const float r = fabsf(tp[a]) * px;
-        pred_s->r[a] = r;
-        pred_s->prxi[a] = px;
-        pred_s->g[a] = mp.n_f * px * pow_nm1_f(r, mp) * dtt[a];
-      }
-#pragma unroll
-      for (int k = 0; k < 9; ++k) pred_s->Fe[k] = Fep[k];
-      pred_s->mode = 2;
-      pred_s->valid = true;
+    for (int k = 0; k < 9; ++k) {
+      dF[k] = to_f32(F[k] - wp->F[k * wp->ld]);
+      Fep[k] = to_f32(wp->Fe[k * wp->ld]);
+      Sp[k] = to_f32(wp->S[k * wp->ld]);
+      B[k] = ((k % 4) == 0 ? 1.0f : 0.0f) - to_f32(dt) * to_f32(Lp[k]);
+      M[k] = to_f32(invFp0[k]);
     }
-  }
-  if (!seeded) {
+    float IB[9];
 #pragma unroll
-    for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
-    if constexpr (MX) {
-      float gf[NSLIP];
-      kinetics_abs_f(mp, S, prxi, gf);
-      dot_state_f(mp, state, gf, dot);
-    } else {
-      dot_state(mp, S, state, prxi, dot);
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) IB[i + 3 * j] = M[i] * B[3 * j] + M[i + 3] * B[1 + 3 * j] + M[i + 6] * B[2 + 3 * j];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) dFe[i + 3 * j] = dF[i] * IB[3 * j] + dF[i + 3] * IB[1 + 3 * j] + dF[i + 6] * IB[2 + 3 * j];
+    float E2[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i <= j; ++i) {
+        float v = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v += Fep[k + 3 * i] * dFe[k + 3 * j] + dFe[k + 3 * i] * Fep[k + 3 * j];
+        E2[i + 3 * j] = v; E2[j + 3 * i] = v;
+      }
+    float dS[9];
+    const float ct = mp.hC12_f * (E2[0] + E2[4] + E2[8]);
+    dS[0] = fmaf(mp.hC11mC12_f, E2[0], ct);
+    dS[4] = fmaf(mp.hC11mC12_f, E2[4], ct);
+    dS[8] = fmaf(mp.hC11mC12_f, E2[8], ct);
+    dS[5] = dS[7] = mp.C44_f * E2[7];
+    dS[2] = dS[6] = mp.C44_f * E2[6];
+    dS[1] = dS[3] = mp.C44_f * E2[3];
+    float tp[NSLIP], dtt[NSLIP];
+    resolved_shear(Sp, tp);
+    resolved_shear(dS, dtt);
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) {
+      const float px = mp.pval_f * rcp(to_f32(wp->st[a * wp->ld]));
+      const float r = fabsf(tp[a]) * px;
+      pred_s->r[a] = r;
+      pred_s->g[a] = mp.n_f * px * pow_nm1_f(r, mp) * dtt[a];
     }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) pred_s->Fe[k] = Fep[k];
+    pred_s->mode = 2;
+    pred_s->valid = true;
+  } else {
+    // explicit predictor: the rates of the restored state and stress
+    double xi[NSLIP], prxi[NSLIP];
+    float gf[NSLIP];
+#pragma unroll
+    for (int a = 0; a < NSLIP; ++a) { xi[a] = state0[a]; prxi[a] = mp.pval * rcp(xi[a]); }
+    kinetics_abs_f(mp, S, prxi, gf);
+    dot_state_f(mp, xi, gf, dot);
     bool nan = false;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
     if (nan) return true;
-#pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(to_f64(dot[i]), dt, state0[i]);
   }
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
+    double prxi[NSLIP];
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) { hist.l2(i) = it > 1 ? hist.l1(i) : DT(0); hist.l1(i) = dot[i]; }
+    for (int i = 0; i < 2 * NSLIP; ++i) { hist.l2(i) = it > 1 ? hist.l1(i) : 0.0f; hist.l1(i) = dot[i]; }
 #pragma unroll
-    for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
+    for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(fma(to_f64(dot[a]), dt, state0[a]));
     (*fpi_iters)++;
-    if (integrate_stress<MX>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters, MX ? pred_s : nullptr)) return true;
-    if constexpr (MX) {
+    if (integrate_stress<true>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters, pred_s, ls)) return true;
+    {
       float gf[NSLIP];
+      double xi[NSLIP];
 #pragma unroll
-      for (int a = 0; a < NSLIP; ++a) gf[a] = to_f32(fabs(gdot[a]));
-      dot_state_f(mp, state, gf, dot);
-    } else {
-      dot_state(mp, S, state, prxi, dot, gdot);
+      for (int a = 0; a < NSLIP; ++a) { gf[a] = to_f32(fabs(gdot[a])); xi[a] = fma(to_f64(hist.l1(a)), dt, state0[a]); }
+      dot_state_f(mp, xi, gf, dot);
     }
     bool nan = false;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
     if (nan) return true;
-    const DT z = damper(dot, hist);
+    const float z = damper(dot, hist);
     bool conv = true;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) {
-      const DT d = dot[i] * z + hist.l1(i) * (DT(1) - z);
-      double r = state[i] - state0[i] - to_f64(d) * dt;
-      state[i] = state[i] - r;
-      // |r| <= max(atol, eps |state|), compared exactly as integers (r and state are
-      // not NaN here: a NaN dot state ended the iteration above)
+      const float d1 = hist.l1(i);
+      const float d = dot[i] * z + d1 * (1.0f - z);
+      const double s0 = state0[i];
+      const double xn = fma(to_f64(d), dt, s0);
+      const double r = fma(to_f64(d1), dt, s0) - xn;
+      // |r| <= max(atol, eps |x_new|), compared exactly as integers (not NaN here)
       const long long atol = absbits(i < NSLIP ? mp.atol_xi : mp.atol_gamma);
-      conv &= absbits(r) <= max(atol, absbits(mp.eps_rel_state * state[i]));
+      conv &= absbits(r) <= max(atol, absbits(mp.eps_rel_state * xn));
+      state[i] = xn;
       dot[i] = d;
-      if constexpr (MX) {
-        if (i < NSLIP) pred_s->dxi[i] = to_f32(r);   // xi - xi' of this update
-      }
+      if (i < NSLIP) pred_s->g[i] *= mp.n_f * to_f32(r);   // n g_a (xi - xi') of this update
     }
     if (conv) return false;
   }
@@ -1073,12 +1163,18 @@ template <bool MX>
 __device__ __noinline__ bool sub_step(const MatParams& mp, const double* Fsub, const double* Fp0, StateRef state0,
                                          double dt, double* state, double* Lp, double* S, double* P, double* Fp,
                                          double* Fe, const Hist<typename std::conditional<MX, float, double>::type>& hist,
-                                         LpPredictor* pred, unsigned* c, const WarmPrev* wp) {
+                                         LpPredictor* pred, unsigned* c, const WarmPrev* wp, const LsBuf* ls) {
   double invFp0[9], A[9];
   if (!sub_step_maps(Fsub, Fp0, invFp0, A)) { c[1]++; return false; }   // counted as an attempted integration
-  if (integrate_state<MX>(mp, Fsub, A, invFp0, state0, dt, state, Lp, S, hist, pred, &c[0], &c[2], &c[1], &c[3], wp))
-    return false;
-  return !stress_outputs(Fsub, invFp0, dt, Lp, S, P, Fp, Fe);
+  if constexpr (MX) {
+    if (integrate_state_mx(mp, Fsub, A, invFp0, state0, dt, state, Lp, S, hist, pred, &c[0], &c[2], &c[1], &c[3], wp,
+                           ls))
+      return false;
+    return !stress_outputs_mx(A, invFp0, dt, Lp, S, P, Fp, Fe);
+  } else {
+    if (integrate_state(mp, A, state0, dt, state, Lp, S, hist, &c[0], &c[2], &c[1], &c[3])) return false;
+    return !stress_outputs(Fsub, invFp0, dt, Lp, S, P, Fp, Fe);
+  }
 }
 
 // The reference's sub-step cut-back driver (phase_mechanical_constitutive,
@@ -1132,8 +1228,9 @@ __device__ __noinline__ bool cutback_driver(const MatParams& mp, const PointStat
     if (todo) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) Fsub[k] = F0c[k] + step * (F[k] - Fphase0[k]);
+      const LsBuf ls{ps.P + e, ps.Fp + e, ps.ld};
       converged = sub_step<MX>(mp, Fsub, Fp0, StateRef{state0, 1}, step * dt, state, Lp, S, P, Fp, Fe, hist, pred, c,
-                               nullptr);
+                               nullptr, &ls);
     }
   }
   return converged;
@@ -1183,8 +1280,9 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
     for (int i = 0; i < 2 * NSLIP; ++i) state[i] = st0[i];
     const WarmPrev wp{ps.F + e, ps.Fe + e, ps.S + e, ps.st + e, ps.ld};
     if (step1 > mp.r_cutback_min) {
+      const LsBuf ls{ps.P + e, ps.Fp + e, ps.ld};
       ok = sub_step<MX>(mp, Fsub, Fp0, st0, step1 * dt, state, Lp, S, P, Fp, Fe, hist, pred, c,
-                        (MX && warm) ? &wp : nullptr);
+                        (MX && warm) ? &wp : nullptr, &ls);
       if (!ok) ok = cutback_driver<MX>(mp, ps, Fin, ldF, e, dt, state, Lp, S, P, Fp, Fe, hist, pred, c);
     } else {
       ok = false;
