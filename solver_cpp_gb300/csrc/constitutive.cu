@@ -106,6 +106,15 @@ __device__ __forceinline__ double to_f64(float x) {
   else if (e == 255) hi = s | 0x7ff00000u | ((u >> 3) & 0xfffffu);
   return __hiloint2double((int)hi, (int)lo);
 }
+// x to FP32 from its high word alone (20 mantissa bits, relative error below 2^-20),
+// for tolerance scales: magnitudes below the FP32 normal range give signed zero, above
+// it infinity.  Five integer instructions instead of to_f32's dozen.
+__device__ __forceinline__ float hi_f32(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), s = hi & 0x80000000u, a = hi & 0x7fffffffu;
+  const unsigned e = a >> 20;
+  const unsigned u = e <= 896u ? 0u : e >= 1151u ? 0x7f800000u : (a - (896u << 20)) << 3;
+  return __uint_as_float(u | s);
+}
 template <typename R> __device__ __forceinline__ R to_R(double x);
 template <> __device__ __forceinline__ double to_R<double>(double x) { return x; }
 template <> __device__ __forceinline__ float to_R<float>(double x) { return to_f32(x); }
@@ -829,7 +838,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       res_old_n = nr2b;
       if constexpr (MX) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) ls->old[k * ls->ld] = Lpg[k];
+        for (int k = 0; k < 9; ++k) __stcs(ls->old + k * ls->ld, Lpg[k]);
       } else {
 #pragma unroll
         for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
@@ -864,7 +873,7 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       if (!ok) return true;
       if constexpr (MX) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) ls->dir[k * ls->ld] = dLp[k];
+        for (int k = 0; k < 9; ++k) __stcs(ls->dir + k * ls->ld, dLp[k]);
       }
     } else if constexpr (MX) {
 #pragma unroll
@@ -1009,10 +1018,12 @@ __device__ bool integrate_state(const MatParams& mp, const double* A, StateRef s
 // Mixed form of integrateStateFPI.  The iterate is not held between the state
 // updates: with the current FP32 rate D (the damper's newest history entry, in shared
 // memory) it is x = state0 + D dt, formed in FP64 where it is needed (the slip
-// resistances of a pass, the update and its test), so the Lp Newton between two
+// resistances of a pass and the converged state), so the Lp Newton between two
 // updates keeps none of the 24 state values in registers.  The iteration is the FP64
-// form's: the damped rate d, x_new = state0 + d dt, the residual r = x - x_new and the
-// test |r| <= max(atol, eps |x_new|) in FP64.  A guess (warm start) enters as its rate
+// form's: the damped rate d, x_new = state0 + d dt, the residual r = x - x_new = (D - d)
+// dt and the test |r| <= max(atol, eps |x_new|), the residual and its test in FP32 (the
+// state accumulates in FP64; FP32 resolves r to 1e-7 of itself, the tolerances are
+// 1 Pa / 1e-6 of xi and 1e-6 of gamma).  A guess (warm start) enters as its rate
 // (guess - state0) / dt in FP32, i.e. as state0 + D dt (within FP32 rounding of the
 // increment, far below the tolerances).  On entry state holds state0 (the callers
 // restore it); on success it receives the converged state.  Returns true if broken.
@@ -1033,21 +1044,23 @@ __device__ bool integrate_state_mx(const MatParams& mp, const double* F, const d
     bool ok = true;
 #pragma unroll
     for (int i = 0; i < 2 * NSLIP; ++i) {
-      const double g = wp->st[i * wp->ld];
+      const double g = __ldcs(wp->st + i * wp->ld);
       dot[i] = to_f32(g - state0[i]) * rdt;
       ok &= !bad_rate(dot[i]) && (i >= NSLIP || g > 0.0);
     }
     seeded = ok;
   }
   if (seeded) {
-    // first-order start of the first pass (as in integrate_state): R(Lp; F) ~ -dLp_c,
-    // dLp_c the change of Lp(S) from dF = F - F_prev at the guess's slip resistances
+    // first-order start of the first pass: the previous evaluation converged at Lp for
+    // F_prev and the guess's slip resistances, so R(Lp; F) ~ -dLp_c with dLp_c the change
+    // of Lp(S) from dF = F - F_prev: dFe = dF Fp0^-1 (I - dt Lp), 2 dE = Fe^T dFe +
+    // dFe^T Fe, dS = C : dE, dt_a = d_a . (dS n_a), u_a = n prxi r^(n-1) dt_a (FP32)
     float M[9], dF[9], dFe[9], Fep[9], Sp[9], B[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      dF[k] = to_f32(F[k] - wp->F[k * wp->ld]);
-      Fep[k] = to_f32(wp->Fe[k * wp->ld]);
-      Sp[k] = to_f32(wp->S[k * wp->ld]);
+      dF[k] = to_f32(F[k] - __ldcs(wp->F + k * wp->ld));
+      Fep[k] = to_f32(__ldcs(wp->Fe + k * wp->ld));
+      Sp[k] = to_f32(__ldcs(wp->S + k * wp->ld));
       B[k] = ((k % 4) == 0 ? 1.0f : 0.0f) - to_f32(dt) * to_f32(Lp[k]);
       M[k] = to_f32(invFp0[k]);
     }
@@ -1083,7 +1096,7 @@ __device__ bool integrate_state_mx(const MatParams& mp, const double* F, const d
     resolved_shear(dS, dtt);
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) {
-      const float px = mp.pval_f * rcp(to_f32(wp->st[a * wp->ld]));
+      const float px = mp.pval_f * rcp(to_f32(__ldcs(wp->st + a * wp->ld)));
       const float r = fabsf(tp[a]) * px;
       pred_s->r[a] = r;
       pred_s->g[a] = mp.n_f * px * pow_nm1_f(r, mp) * dtt[a];
@@ -1105,6 +1118,8 @@ __device__ bool integrate_state_mx(const MatParams& mp, const double* F, const d
     for (int i = 0; i < 2 * NSLIP; ++i) nan |= bad_rate(dot[i]);
     if (nan) return true;
   }
+  const float dtf = to_f32(dt), eps_f = to_f32(mp.eps_rel_state);
+  const int atol_xi = absbits(to_f32(mp.atol_xi)), atol_gamma = absbits(to_f32(mp.atol_gamma));
   for (int it = 1; it <= mp.N_iter_state_max; ++it) {
     double prxi[NSLIP];
 #pragma unroll
@@ -1130,17 +1145,21 @@ __device__ bool integrate_state_mx(const MatParams& mp, const double* F, const d
     for (int i = 0; i < 2 * NSLIP; ++i) {
       const float d1 = hist.l1(i);
       const float d = dot[i] * z + d1 * (1.0f - z);
-      const double s0 = state0[i];
-      const double xn = fma(to_f64(d), dt, s0);
-      const double r = fma(to_f64(d1), dt, s0) - xn;
-      // |r| <= max(atol, eps |x_new|), compared exactly as integers (not NaN here)
-      const long long atol = absbits(i < NSLIP ? mp.atol_xi : mp.atol_gamma);
-      conv &= absbits(r) <= max(atol, absbits(mp.eps_rel_state * xn));
-      state[i] = xn;
+      // the update's residual r = x - x_new = (D - d) dt and the test |r| <= max(atol,
+      // eps |x_new|) in FP32 (x_new = state0 + d dt to FP32 precision: a tolerance
+      // scale); integer compares of the magnitudes (not NaN here)
+      const float r = (d1 - d) * dtf;
+      const float xn = fmaf(d, dtf, hi_f32(state0[i]));
+      conv &= absbits(r) <= max(i < NSLIP ? atol_xi : atol_gamma, absbits(eps_f * xn));
       dot[i] = d;
-      if (i < NSLIP) pred_s->g[i] *= mp.n_f * to_f32(r);   // n g_a (xi - xi') of this update
+      if (i < NSLIP) pred_s->g[i] *= mp.n_f * r;   // n g_a (xi - xi') of this update
     }
-    if (conv) return false;
+    if (conv) {
+      // the converged state, accumulated in FP64: state0 + d dt
+#pragma unroll
+      for (int i = 0; i < 2 * NSLIP; ++i) state[i] = fma(to_f64(dot[i]), dt, state0[i]);
+      return false;
+    }
   }
   return true;
 }
@@ -1266,11 +1285,11 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
     double Fsub[9], Fp0[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double f0 = ldp(ps.F0, ps.ld, k, e);
+      const double f0 = __ldcs(ps.F0 + k * ps.ld + e);
       Fsub[k] = f0 + step1 * (Fin[k * ldF + e] - f0);
-      Fp0[k] = ldp(ps.Fp0, ps.ld, k, e);
-      Lp[k] = step1 < 1.0 ? ldp(ps.Lp0, ps.ld, k, e) : ldp(ps.Lp, ps.ld, k, e);
-      S[k] = ldp(ps.S0, ps.ld, k, e);
+      Fp0[k] = __ldcs(ps.Fp0 + k * ps.ld + e);
+      Lp[k] = step1 < 1.0 ? __ldcs(ps.Lp0 + k * ps.ld + e) : __ldcs(ps.Lp + k * ps.ld + e);
+      S[k] = __ldcs(ps.S0 + k * ps.ld + e);
       P[k] = 0.0;
       Fe[k] = 0.0;
       Fp[k] = Fp0[k];
@@ -1289,15 +1308,15 @@ __device__ __forceinline__ void cons_tile(const MatParams& mp, const PointState&
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      ps.F[k * ps.ld + e] = Fin[k * ldF + e];
-      ps.Fp[k * ps.ld + e] = Fp[k];
-      ps.Lp[k * ps.ld + e] = Lp[k];
-      ps.S[k * ps.ld + e] = S[k];
-      ps.Fe[k * ps.ld + e] = Fe[k];
-      ps.P[k * ps.ld + e] = P[k];
+      __stcs(ps.F + k * ps.ld + e, Fin[k * ldF + e]);
+      __stcs(ps.Fp + k * ps.ld + e, Fp[k]);
+      __stcs(ps.Lp + k * ps.ld + e, Lp[k]);
+      __stcs(ps.S + k * ps.ld + e, S[k]);
+      __stcs(ps.Fe + k * ps.ld + e, Fe[k]);
+      __stcs(ps.P + k * ps.ld + e, P[k]);
     }
 #pragma unroll
-    for (int i = 0; i < 2 * NSLIP; ++i) ps.st[i * ps.ld + e] = state[i];
+    for (int i = 0; i < 2 * NSLIP; ++i) __stcs(ps.st + i * ps.ld + e, state[i]);
     ps.status[e] = ok ? 0 : 1;
     if (!ok) atomicOr(ill, 1);
   } else {

@@ -45,9 +45,10 @@ struct MatParams {
   int n_int;                 // n if it is an integer in [1, 64], else -1
   int a_quarters;            // 4a if it is an integer in [1, 256], else -1
   // mixed-precision constitutive form (numerics precision 1): the Lp Newton's residual,
-  // updates and convergence test, the state update and its test stay FP64; the Newton
-  // Jacobian, its first-order starts, the hardening and gamma rates and the damper are
-  // evaluated in FP32, and later evaluations of a step start from the previous one.
+  // updates and convergence test and the state's accumulation stay FP64; the Newton
+  // Jacobian, its first-order starts, the hardening and gamma rates, the damper and the
+  // state update's residual and test are evaluated in FP32, and later evaluations of a
+  // step start from the previous one.
   // 0 for the plain FP64 form.
   int mixed;
   float h0h_f[7];            // h0h in FP32 (hardening rate of the mixed form)
@@ -102,16 +103,20 @@ constexpr double FLOPS_LP = 378.0, FLOPS_JAC = 923.0, FLOPS_STATE = 860.0, FLOPS
 // of its scale factors: 918 flops); in every dot state the hardening rate and the gamma
 // rate (FP64 31 flops per slip system -> FP32 24; x = 1 - xi / xi_inf stays FP64); the
 // predictor's slip rates (13 per system); the damper's three dot products (144) and
-// the blended rate (72).  Per counted unit:
-//   state: FP64 860 - 156 - 372 = 332, FP32 156 + 288 = 444
-//   fpi:   FP64 755 - 372 - 144 - 72 = 167, FP32 288 + 144 + 72 = 504
+// the blended rate (72); the fixed-point update's residual (D - d) dt, x_new to FP32
+// and eps |x_new| (5 per state entry: 120), while the state itself accumulates in FP64
+// once the iteration has converged (state0 + d dt: 48).  The iterate is formed from the
+// rate history: xi = state0 + D dt and pval / xi at the head of a pass (48), xi again
+// and x = 1 - xi / xi_inf after its Newton (48).  Per counted unit:
+//   state: FP64 860 - 156 - 372 + 48 = 380, FP32 156 + 288 = 444
+//   fpi:   FP64 48 + 48 = 96, FP32 288 + 144 + 72 + 120 = 624
 // A first-order Newton start counts as one Jacobian unit (its own right-hand side, at
 // most ~300 FP32 flops, is not counted), and a warm-started state integration still
 // counts the explicit predictor it skips (156 FP32 flops and 12 FP64 reciprocals), so
 // the mixed model counts cold evaluations exactly and warm ones approximately.
 constexpr double FLOPS_MX_JAC64 = 5.0, FLOPS_MX_JAC32 = FLOPS_JAC - FLOPS_MX_JAC64;
-constexpr double FLOPS_MX_STATE64 = 332.0, FLOPS_MX_STATE32 = 444.0;
-constexpr double FLOPS_MX_FPI64 = 167.0, FLOPS_MX_FPI32 = 504.0;
+constexpr double FLOPS_MX_STATE64 = 380.0, FLOPS_MX_STATE32 = 444.0;
+constexpr double FLOPS_MX_FPI64 = 96.0, FLOPS_MX_FPI32 = 624.0;
 
 // Stress boundary condition of one RVE's solve, resident on the device so that the
 // BC step of a residual evaluation (form_residual) needs no host round trip.
