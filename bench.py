@@ -40,9 +40,9 @@ UNIT = "point-updates/s"
 SEED = 42
 
 # DRAM traffic of one constitutive launch per cell, from an ncu capture of this
-# workload (dram__bytes.sum.per_second x gpu__time_duration.sum of one launch / 262,144
-# cells: 170.4 GB/s x 2.985 ms = 0.509 GB; profiles/constitutive_64cube.md)
-TRAFFIC_BYTES_PER_CELL = 1940.0
+# workload (dram__bytes_read.sum + dram__bytes_write.sum of the 41st launch / 262,144
+# cells: 0.152 + 0.249 GB = 0.401 GB; profiles/constitutive_64cube.md)
+TRAFFIC_BYTES_PER_CELL = 1530.0
 
 
 def args_():
