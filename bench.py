@@ -681,15 +681,15 @@ def gpu_arm(a):
                 line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": threads, "kind": "port",
                                         "sample": f"failed: {ex}"}
     if rank == 0:
-        ratios = north_star_ratios(line)
+        ratios = mixed_vs_fp64_ratios(line)
         if ratios:
-            line["north_star_ratios"] = ratios
+            line["mixed_vs_fp64_ratios"] = ratios
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def north_star_ratios(line):
+def mixed_vs_fp64_ratios(line):
     """The mixed form against the plain FP64 form, from the legs of this run that
     measured both on equal work: the 64^3 workload's whole load case, the 128^3
     configuration, the batched population in both forms, the batched population's
