@@ -677,61 +677,14 @@ struct LsBuf {
 };
 
 // integrateStress with Fi = I for fixed F and Fp0 (A = F Fp0^-1) and slip resistances
-// xi (prxi = pval / xi): the Lp Newton iteration.  Returns true if broken.  On success
-// writes S, Lp and the slip rates of S; Fp, Fe and P follow from stress_outputs().
-// Mixed form (pr not null): a converged previous pass of the same state integration
-// (pr->valid) gives the Newton a first-order start, Lp + J^-1 dLp_c with dLp_c the
-// change of Lp(S) from the new slip resistances, dg_a / dprxi_a = n g_a / prxi_a, and J
-// the FP32 Jacobian at the previous solution; on convergence the solution's data are
-// stored for the next pass.  The iteration from that start is the same FP64 Newton;
-// its line-search data (last accepted iterate, last direction) live in the planes of
-// ls (not null in the mixed form).
-template <bool MX>
+// xi (prxi = pval / xi): the Lp Newton iteration (plain FP64 form).  Returns true if
+// broken.  On success writes S, Lp and the slip rates of S; Fp, Fe and P follow from
+// stress_outputs().
 __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt, const double* prxi, double* Lp,
-                                 double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters,
-                                 LpPredictor* pr = nullptr, const LsBuf* ls = nullptr) {
-  double Lpg[9], Lpg_old[MX ? 1 : 9], dLp[9], B[9], Fe_[9];
-  float Af[MX ? 9 : 1], prxi_f[MX ? NSLIP : 1];
-  if constexpr (MX) {
+                                 double* S, double* gdot_out, unsigned* lp_iters, unsigned* jac_iters) {
+  double Lpg[9], Lpg_old[9], dLp[9], B[9], Fe_[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Af[k] = to_f32(A[k]);
-#pragma unroll
-    for (int a = 0; a < NSLIP; ++a) prxi_f[a] = to_f32(prxi[a]);
-  }
-#pragma unroll
-  for (int k = 0; k < 9; ++k) Lpg[k] = Lp[k];
-  if constexpr (MX) {
-    if (pr && pr->valid) {
-      // u_a = n g_a rho_a, rho_a = prxi'_a / prxi_a - 1 = (xi_a - xi'_a) / xi'_a; the
-      // derivative at the previous solution prxi r^(n-1) takes the new prxi' (the two
-      // differ by rho, which only scales the start's correction)
-      float u[NSLIP], dg0[NSLIP], dLc[9];
-      double delta_[9], delta[9];
-#pragma unroll
-      for (int a = 0; a < NSLIP; ++a) {
-        u[a] = pr->mode == 2 ? pr->g[a] : pr->g[a] * (prxi_f[a] * mp.rpval_f);
-        dg0[a] = prxi_f[a] * pow_nm1_f(pr->r[a], mp);
-      }
-      plane_butterfly(u, dLc);
-#pragma unroll
-      for (int k = 0; k < 9; ++k) delta_[k] = to_f64(-mp.pgdot0_f * dLc[k]);   // R(Lp, xi') ~ -dLp_c
-      (*jac_iters)++;
-      if (jacobian_step_f32(mp, Af, pr->Fe, dt, dg0, delta_, delta)) {
-        bool finite = true;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) finite &= !nan_bits(delta[k]) && absbits(delta[k]) != 0x7ff0000000000000LL;
-        if (finite) {
-#pragma unroll
-          for (int k = 0; k < 9; ++k) Lpg[k] += delta[k];
-        }
-      }
-      pr->valid = false;
-    }
-  }
-  if constexpr (!MX) {
-#pragma unroll
-    for (int k = 0; k < 9; ++k) { Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
-  }
+  for (int k = 0; k < 9; ++k) { Lpg[k] = Lp[k]; Lpg_old[k] = Lpg[k]; dLp[k] = 0.0; }
   long long res_old_n = 0;
   double step = 1.0;
   int jaco = 0;
@@ -742,73 +695,42 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
     for (int k = 0; k < 9; ++k) B[k] = ((k % 4) == 0 ? 1.0 : 0.0) - dt * Lpg[k];
     mm(A, B, Fe_);
     hooke_S(mp, Fe_, S);
-    float Fef[MX ? 9 : 1];                     // mixed form: Fe for the FP32 Jacobian and the predictor
-    if constexpr (MX) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) Fef[k] = to_f32(Fe_[k]);
-    }
-    // slip rates (units of gdot0) and what the Jacobian needs of them: plain form
-    // r^(n-1) (dg = prxi r^(n-1) is formed with the Jacobian), mixed form r in FP32
-    using KT = typename std::conditional<MX, float, double>::type;
-    double gdot[NSLIP];
-    KT kaux[NSLIP];
-    if constexpr (MX) {
-      double t[NSLIP];
-      resolved_shear(S, t);
-#pragma unroll
-      for (int a = 0; a < NSLIP; ++a) {
-        const double r = fabs(t[a]) * prxi[a];
-        gdot[a] = copysign(pow_n(r, mp), t[a]);
-        kaux[a] = to_f32(r);
-      }
-    } else {
-      kinetics(mp, S, prxi, gdot, nullptr, kaux);
-    }
+    // slip rates (units of gdot0) and r^(n-1) (dg = prxi r^(n-1) is formed with the Jacobian)
+    double gdot[NSLIP], kaux[NSLIP];
+    kinetics(mp, S, prxi, gdot, nullptr, kaux);
     // Lp = pval gdot0 sum_a gdot_a d_a (x) n_a (gdot in units of gdot0) with the cF signs
     // folded at compile time: the three systems of a slip plane share n, so the plane
     // sums Y_p = sum_a gdot_a d_a come first, then L(k, l) = sum_p n_p(l) Y_p(k)
     double res[9], Lpc[9];
     double nLg2 = 0.0, nLc2 = 0.0, nr2 = 0.0;
-    if constexpr (MX) {
-      // plane sums and the butterfly over the four normals (plane_butterfly); the
-      // factor pval gdot0 folded into the residual (one FMA per entry) and the norm
-      plane_butterfly(gdot, Lpc);
+    double Y[4][3];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) res[k] = fma(-mp.pgdot0, Lpc[k], Lpg[k]);
-      double nL2 = 0.0;
+    for (int p = 0; p < 4; ++p)
 #pragma unroll
-      for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nL2 = fma(Lpc[k], Lpc[k], nL2); nr2 = fma(res[k], res[k], nr2); }
-      nLc2 = mp.pgdot0_sq * nL2;
-    } else {
-      double Y[4][3];
+      for (int k = 0; k < 3; ++k) {
+        Y[p][k] = -0.0;
 #pragma unroll
-      for (int p = 0; p < 4; ++p)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          Y[p][k] = -0.0;
-#pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            if (fcc_d(3 * p + j, k) > 0) Y[p][k] += gdot[3 * p + j];
-            else if (fcc_d(3 * p + j, k) < 0) Y[p][k] -= gdot[3 * p + j];
-          }
+        for (int j = 0; j < 3; ++j) {
+          if (fcc_d(3 * p + j, k) > 0) Y[p][k] += gdot[3 * p + j];
+          else if (fcc_d(3 * p + j, k) < 0) Y[p][k] -= gdot[3 * p + j];
         }
+      }
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int l = 0; l < 3; ++l) {
-          double sm = -0.0;
+      for (int l = 0; l < 3; ++l) {
+        double sm = -0.0;
 #pragma unroll
-          for (int p = 0; p < 4; ++p) {
-            if (fcc_n(3 * p, l) > 0) sm += Y[p][k];
-            else sm -= Y[p][k];
-          }
-          Lpc[k + 3 * l] = mp.pgdot0 * sm;
+        for (int p = 0; p < 4; ++p) {
+          if (fcc_n(3 * p, l) > 0) sm += Y[p][k];
+          else sm -= Y[p][k];
         }
+        Lpc[k + 3 * l] = mp.pgdot0 * sm;
+      }
 #pragma unroll
-      for (int k = 0; k < 9; ++k) res[k] = Lpg[k] - Lpc[k];
+    for (int k = 0; k < 9; ++k) res[k] = Lpg[k] - Lpc[k];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nLc2 = fma(Lpc[k], Lpc[k], nLc2); nr2 = fma(res[k], res[k], nr2); }
-    }
+    for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nLc2 = fma(Lpc[k], Lpc[k], nLc2); nr2 = fma(res[k], res[k], nr2); }
     // convergence tests on squared norms (no square roots); the norms are non-negative
     // and, past the NaN test, not NaN, so they compare exactly as integers
     if (nan_bits(nr2)) return true;
@@ -820,67 +742,151 @@ __device__ bool integrate_stress(const MatParams& mp, const double* A, double dt
       for (int a = 0; a < NSLIP; ++a) gdot_out[a] = gdot[a];   // slip rates of the final S
 #pragma unroll
       for (int k = 0; k < 9; ++k) Lp[k] = Lpg[k];
-      if constexpr (MX) {
-        if (pr) {
-#pragma unroll
-          for (int k = 0; k < 9; ++k) pr->Fe[k] = Fef[k];
-#pragma unroll
-          for (int a = 0; a < NSLIP; ++a) {
-            pr->r[a] = kaux[a]; pr->g[a] = to_f32(gdot[a]);
-          }
-          pr->valid = true;
-          pr->mode = 1;
-        }
-      }
       return false;
     }
     if (it == 1 || nr2b < res_old_n) {
       res_old_n = nr2b;
-      if constexpr (MX) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) __stcs(ls->old + k * ls->ld, Lpg[k]);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
-      }
+      for (int k = 0; k < 9; ++k) Lpg_old[k] = Lpg[k];
       step = 1.0;
     } else {
       step *= mp.r_linesearch_Lp;
-      if constexpr (MX) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Lpg[k] = fma(ls->dir[k * ls->ld], step, ls->old[k * ls->ld]);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg_old[k]);
-      }
+      for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg_old[k]);
       continue;
     }
     if (jaco % mp.f_update_jacobi_Lp == 0) {
       ++jaco;
       (*jac_iters)++;
-      bool ok;
-      KT dg[NSLIP];                             // |dgdot/dtau| up to the factor n gdot0 / pval
+      double dg[NSLIP];                         // |dgdot/dtau| up to the factor n gdot0 / pval
 #pragma unroll
-      for (int a = 0; a < NSLIP; ++a) {
-        if constexpr (MX) dg[a] = prxi_f[a] * pow_nm1_f(kaux[a], mp);
-        else dg[a] = prxi[a] * kaux[a];
-      }
-      if constexpr (MX) {
-        ok = jacobian_step_f32(mp, Af, Fef, dt, dg, res, dLp);
-      } else {
-        ok = jacobian_step<double, double>(mp, A, Fe_, dt, dg, res, dLp);
-      }
-      if (!ok) return true;
-      if constexpr (MX) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) __stcs(ls->dir + k * ls->ld, dLp[k]);
-      }
-    } else if constexpr (MX) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) dLp[k] = ls->dir[k * ls->ld];
+      for (int a = 0; a < NSLIP; ++a) dg[a] = prxi[a] * kaux[a];
+      if (!jacobian_step<double, double>(mp, A, Fe_, dt, dg, res, dLp)) return true;
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) Lpg[k] = fma(dLp[k], step, Lpg[k]);
+  }
+}
+
+// Mixed form of integrateStress: the same FP64 Newton (residual, updates, line search
+// and test in FP64) with the FP32 Jacobian step.  A valid predictor record gives the
+// Newton a first-order start (Lp + J^-1 dLp_c, see integrate_stress); that start is a
+// Jacobian step of its own right-hand side taken at the loop's one Jacobian call site
+// before the first Newton iteration, so the kernel holds one inlined copy of the step.
+// On convergence the record receives Fe, r and the slip rates of the final S (FP32).
+__device__ bool integrate_stress_mx(const MatParams& mp, const double* A, double dt, const double* prxi, double* Lp,
+                                    double* S, unsigned* lp_iters, unsigned* jac_iters, LpPredictor* pr,
+                                    const LsBuf* ls) {
+  double Lpg[9], B[9], Fe_[9];
+  float Af[9], prxi_f[NSLIP];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Af[k] = to_f32(A[k]);
+#pragma unroll
+  for (int a = 0; a < NSLIP; ++a) prxi_f[a] = to_f32(prxi[a]);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Lpg[k] = Lp[k];
+  bool pre = pr->valid;
+  pr->valid = false;
+  long long res_old_n = 0;
+  double step = 1.0;
+  int jaco = 0, it = 0;
+  for (;;) {
+    float Fj[9], dgj[NSLIP];                    // the Jacobian step's Fe and |dgdot/dtau| / (n gdot0 / pval)
+    double rhs[9];
+    if (pre) {
+      // u_a = n g_a rho_a, rho_a = (xi_a - xi'_a) / xi'_a (mode 1) or given (mode 2); the
+      // derivative at the previous solution takes the new prxi'
+      float u[NSLIP], dLc[9];
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) {
+        u[a] = pr->mode == 2 ? pr->g[a] : pr->g[a] * (prxi_f[a] * mp.rpval_f);
+        dgj[a] = prxi_f[a] * pow_nm1_f(pr->r[a], mp);
+      }
+      plane_butterfly(u, dLc);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) rhs[k] = to_f64(-mp.pgdot0_f * dLc[k]);   // R(Lp, xi') ~ -dLp_c
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Fj[k] = pr->Fe[k];
+    } else {
+      if (++it > mp.N_iter_Lp_max) return true;
+      (*lp_iters)++;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) B[k] = ((k % 4) == 0 ? 1.0 : 0.0) - dt * Lpg[k];
+      mm(A, B, Fe_);
+      hooke_S(mp, Fe_, S);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Fj[k] = to_f32(Fe_[k]);
+      double gdot[NSLIP], t[NSLIP];
+      float kaux[NSLIP];
+      resolved_shear(S, t);
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) {
+        const double r = fabs(t[a]) * prxi[a];
+        gdot[a] = copysign(pow_n(r, mp), t[a]);
+        kaux[a] = to_f32(r);
+      }
+      double res[9], Lpc[9];
+      plane_butterfly(gdot, Lpc);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) res[k] = fma(-mp.pgdot0, Lpc[k], Lpg[k]);
+      double nLg2 = 0.0, nL2 = 0.0, nr2 = 0.0;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) { nLg2 = fma(Lpg[k], Lpg[k], nLg2); nL2 = fma(Lpc[k], Lpc[k], nL2); nr2 = fma(res[k], res[k], nr2); }
+      const double nLc2 = mp.pgdot0_sq * nL2;
+      if (nan_bits(nr2)) return true;
+      const long long nr2b = absbits(nr2);
+      const long long atol2 = max(absbits(mp.eps_rel_Lp2 * __longlong_as_double(max(absbits(nLg2), absbits(nLc2)))),
+                                  absbits(mp.eps_abs_Lp2));
+      if (nr2b < atol2) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) { Lp[k] = Lpg[k]; pr->Fe[k] = Fj[k]; }
+#pragma unroll
+        for (int a = 0; a < NSLIP; ++a) { pr->r[a] = kaux[a]; pr->g[a] = to_f32(gdot[a]); }
+        pr->valid = true;
+        pr->mode = 1;
+        return false;
+      }
+      if (it == 1 || nr2b < res_old_n) {
+        res_old_n = nr2b;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) __stcs(ls->old + k * ls->ld, Lpg[k]);
+        step = 1.0;
+      } else {
+        step *= mp.r_linesearch_Lp;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Lpg[k] = fma(ls->dir[k * ls->ld], step, ls->old[k * ls->ld]);
+        continue;
+      }
+      if (jaco % mp.f_update_jacobi_Lp != 0) {          // the previous direction, kept
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Lpg[k] = fma(ls->dir[k * ls->ld], step, Lpg[k]);
+        continue;
+      }
+      ++jaco;
+#pragma unroll
+      for (int a = 0; a < NSLIP; ++a) dgj[a] = prxi_f[a] * pow_nm1_f(kaux[a], mp);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) rhs[k] = res[k];
+    }
+    (*jac_iters)++;
+    double d[9];
+    const bool ok = jacobian_step_f32(mp, Af, Fj, dt, dgj, rhs, d);
+    if (pre) {
+      pre = false;
+      bool finite = ok;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) finite &= !nan_bits(d[k]) && absbits(d[k]) != 0x7ff0000000000000LL;
+      if (finite) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Lpg[k] += d[k];
+      }
+      continue;
+    }
+    if (!ok) return true;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) __stcs(ls->dir + k * ls->ld, d[k]);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Lpg[k] = fma(d[k], step, Lpg[k]);
   }
 }
 
@@ -991,7 +997,7 @@ __device__ bool integrate_state(const MatParams& mp, const double* A, StateRef s
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(state[a]);
     (*fpi_iters)++;
-    if (integrate_stress<false>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters)) return true;
+    if (integrate_stress(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters)) return true;
     dot_state(mp, S, state, prxi, dot, gdot);
     nan = false;
 #pragma unroll
@@ -1033,7 +1039,6 @@ __device__ bool integrate_state_mx(const MatParams& mp, const double* F, const d
                                    unsigned* jac_iters, unsigned* st_iters, unsigned* fpi_iters,
                                    const WarmPrev* wp, const LsBuf* ls) {
   float dot[2 * NSLIP];
-  double gdot[NSLIP];
   pred_s->valid = false;
   (*st_iters)++;
   bool seeded = false;
@@ -1127,12 +1132,12 @@ __device__ bool integrate_state_mx(const MatParams& mp, const double* F, const d
 #pragma unroll
     for (int a = 0; a < NSLIP; ++a) prxi[a] = mp.pval * rcp(fma(to_f64(dot[a]), dt, state0[a]));
     (*fpi_iters)++;
-    if (integrate_stress<true>(mp, A, dt, prxi, Lp, S, gdot, lp_iters, jac_iters, pred_s, ls)) return true;
+    if (integrate_stress_mx(mp, A, dt, prxi, Lp, S, lp_iters, jac_iters, pred_s, ls)) return true;
     {
       float gf[NSLIP];
       double xi[NSLIP];
 #pragma unroll
-      for (int a = 0; a < NSLIP; ++a) { gf[a] = to_f32(fabs(gdot[a])); xi[a] = fma(to_f64(hist.l1(a)), dt, state0[a]); }
+      for (int a = 0; a < NSLIP; ++a) { gf[a] = fabsf(pred_s->g[a]); xi[a] = fma(to_f64(hist.l1(a)), dt, state0[a]); }
       dot_state_f(mp, xi, gf, dot);
     }
     bool nan = false;
