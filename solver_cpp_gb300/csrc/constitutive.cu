@@ -938,9 +938,9 @@ __device__ bool stress_outputs_mx(const double* A, const double* invFp0, double 
 
 // Per-thread scratch of the state integration in shared memory (one record per thread
 // of the block, entry i of thread t at base[i * BS + t]): the damper's two previous
-// rates (FP64 in the plain form, FP32 in the mixed form).  Kept out of registers, as
-// they are touched once per fixed-point pass while the Lp Newton between passes needs
-// every register.
+// rates (FP64 in the plain form, FP32 in the mixed form, where the newest one also
+// defines the iterate, state0 + D dt).  Kept out of registers, as they are touched once
+// per fixed-point pass while the Lp Newton between passes needs every register.
 template <typename DT>
 struct Hist {
   DT* h;
