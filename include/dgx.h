@@ -361,7 +361,9 @@ dgx_status dgx_measure_fp64_peak(double* tflops, double* ms);
  * CUDA library functions; no reference counterpart): fn 0 the Newton-Raphson
  * reciprocal 1/x, fn 1 x^(9/4) (slip-resistance saturation, a = 2.25), fn 2 x^19
  * (the power law's x^(n-1), n = 20), fn 3 the mixed form's FP64 -> FP32 -> FP64 round
- * trip on the integer pipe (FP32 rounded toward zero, subnormals flushed). */
+ * trip on the integer pipe (FP32 rounded toward zero, subnormals flushed), fn 4 the
+ * mixed form's FP32 tolerance scale of a state value (the high word's 20 mantissa bits,
+ * below the FP32 normal range signed zero, above it or NaN signed infinity). */
 dgx_status dgx_device_math(int32_t fn, int64_t n, const double* x, double* out);
 
 #ifdef __cplusplus

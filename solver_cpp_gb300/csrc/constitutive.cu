@@ -108,7 +108,7 @@ __device__ __forceinline__ double to_f64(float x) {
 }
 // x to FP32 from its high word alone (20 mantissa bits, relative error below 2^-20),
 // for tolerance scales: magnitudes below the FP32 normal range give signed zero, above
-// it infinity.  Five integer instructions instead of to_f32's dozen.
+// it (and NaN) infinity.  Five integer instructions instead of to_f32's dozen.
 __device__ __forceinline__ float hi_f32(double x) {
   const unsigned hi = (unsigned)__double2hiint(x), s = hi & 0x80000000u, a = hi & 0x7fffffffu;
   const unsigned e = a >> 20;
@@ -1836,12 +1836,13 @@ __global__ void k_device_math(int fn, int64_t n, const double* __restrict__ x, d
   MatParams mp{};
   mp.n = 20.0; mp.n_int = 20; mp.a = 2.25; mp.a_quarters = 9;
   const double v = x[i];
-  out[i] = fn == 0 ? rcp(v) : fn == 1 ? pow_a(v, mp) : fn == 2 ? pow_nm1(v, mp) : to_f64(to_f32(v));
+  out[i] = fn == 0 ? rcp(v) : fn == 1 ? pow_a(v, mp) : fn == 2 ? pow_nm1(v, mp) : fn == 3 ? to_f64(to_f32(v))
+                                                                                  : to_f64(hi_f32(v));
 }
 }  // namespace dgx
 
 extern "C" dgx_status dgx_device_math(int32_t fn, int64_t n, const double* x, double* out) {
-  if (fn < 0 || fn > 3 || n < 0 || (n > 0 && (!x || !out))) return DGX_ERR_ARG;
+  if (fn < 0 || fn > 4 || n < 0 || (n > 0 && (!x || !out))) return DGX_ERR_ARG;
   if (n == 0) return DGX_OK;
   double* d = nullptr;
   if (cudaMalloc(&d, 2 * sizeof(double) * (size_t)n) != cudaSuccess) return DGX_ERR_NOMEM;

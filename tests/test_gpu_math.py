@@ -78,3 +78,28 @@ def test_integer_pipe_conversions(dm):
     ref = f32_toward_zero(x)
     assert np.array_equal(got.view(np.int64), ref.view(np.int64))
     assert np.isnan(dm(3, np.array([np.nan]))[0])
+
+
+def hi_word_f32(x):
+    """The mixed form's tolerance-scale conversion restated in numpy: the FP64 value with
+    its low 32 bits cleared (20 mantissa bits, exact in FP32), signed zero below the FP32
+    normal range, signed infinity above it and for NaN."""
+    bits = x.view(np.uint64)
+    e = (bits >> np.uint64(52)) & np.uint64(0x7ff)
+    cut = (bits & np.uint64(0xffffffff00000000)).view(np.float64)
+    with np.errstate(invalid="ignore"):
+        sign = np.where(np.signbit(x), -1.0, 1.0)
+    return np.where(e <= 896, sign * 0.0, np.where(e >= 1151, sign * np.inf, cut))
+
+
+def test_tolerance_scale_conversion(dm):
+    rng = np.random.default_rng(8)
+    x = np.concatenate([rng.uniform(2.5e7, 7e7, 20000), 10.0 ** rng.uniform(-37, 38, 20000),
+                        -(10.0 ** rng.uniform(-37, 38, 5000)), 2.0 ** np.arange(-126, 128.0),
+                        np.nextafter(2.0 ** np.arange(-126, 128.0), 0.0),
+                        [0.0, -0.0, 1e-40, -1e-45, 1e-300, 3.5e38, -1e39, 1e300, np.inf, -np.inf, np.nan]])
+    got = dm(4, x)
+    ref = hi_word_f32(x)
+    assert np.array_equal(got.view(np.int64), ref.view(np.int64))
+    fin = np.isfinite(x) & (np.abs(x) >= np.finfo(np.float32).tiny) & (np.abs(x) < 2.0 ** 128)
+    assert np.max(np.abs(got[fin] - x[fin]) / np.abs(x[fin])) < 2.0 ** -20
