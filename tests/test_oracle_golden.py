@@ -137,3 +137,44 @@ def test_update_coords_identity(knowns):
                 assert np.allclose(un[node] + step * [i, j, kk], x_n[:, i, j, kk], rtol=0, atol=1e-20)
     for i in range(2):
         assert np.allclose(up[i] + step * (np.array([i, 0, 0]) + 0.5), x_p[:, i, 0, 0], rtol=0, atol=1e-20)
+
+
+def test_basic_forward(knowns):
+    """TestBasicForward (test_mech_solver_basic.cpp): dot_F_xx = 1e-3 with P_yy = P_zz = 0
+    prescribed, dt = 100.2, dt_old = 1, t_remaining = 1002, no guess: F_aim = I +
+    dot_F dt and the forwarded field is that aim in every cell."""
+    import ctypes as C
+    k = knowns["basic_forward"]
+    ls = dgo.loadstep("tensionX", t=k["t_remaining"], N=10, rate=k["deformation_values"][0][0])
+    # the fixture's masks are the tensionX load step's (deformation 'x' where stress prescribed)
+    assert [[int(ls.def_mask[i + 3 * j]) for j in range(3)] for i in range(3)] == k["deformation_mask"]
+    assert [[int(ls.stress_mask[i + 3 * j]) for j in range(3)] for i in range(3)] == k["stress_mask"]
+    s = dgo.Solver((2, 1, 1), (2e-5, 1e-5, 1e-5), [0, 0], [[1.0, 0.0, 0.0, 0.0]])
+    L = dgo.lib()
+    L.dgo_solver_init_state(s.h)
+    assert L.dgo_solver_forward(s.h, 0, 0, k["delta_t"], k["delta_t_old"], k["t_remaining"], C.byref(ls)) == 0
+    aim = dgo.from_fortran9(s.get("F_aim"))
+    assert np.allclose(aim, np.array(k["expected_aim"]), rtol=0, atol=1e-15)
+    F = s.get("F")
+    for c in range(2):
+        assert np.allclose(dgo.from_fortran9(F[c]), aim, rtol=0, atol=1e-15)
+    last = np.array(k["expected_field_last_inc"])[:, :, :, 0, 0]     # [i][j][cell]: I in both cells
+    assert np.array_equal(last[:, :, 0], np.eye(3)) and np.array_equal(last[:, :, 1], np.eye(3))
+
+
+def test_ip_and_node_coordinates(knowns):
+    """DiscretizationGrid coordinates (test_discretization_grid.cpp): cell centres and
+    nodes of 2 x 1 x 1 cells of 1e-5, as the coordinate update leaves them at F = I."""
+    k = knowns["ip_node_coords_2x1x1"]
+    cells, geom = k["cells"], k["geom"]
+    F9 = dgo.fortran9(np.tile(np.eye(3), (2, 1, 1)))
+    un, up = dgo.update_coords(cells, geom, F9)
+    step = np.array(geom) / np.array(cells)
+    ip = np.array(k["ip"])                 # (3, cells): x, y, z of each cell centre
+    node = np.array(k["node"])             # (3, nodes), x fastest
+    for c in range(2):
+        assert np.allclose(step * (np.array([c, 0, 0]) + 0.5) + up[c], ip[:, c], rtol=0, atol=1e-20)
+    N0, N1, N2 = (n + 1 for n in cells)
+    for n in range(N0 * N1 * N2):
+        i, j, kk = n % N0, (n // N0) % N1, n // (N0 * N1)
+        assert np.allclose(step * [i, j, kk] + un[n], node[:, n], rtol=0, atol=1e-20)
