@@ -178,3 +178,17 @@ def test_ip_and_node_coordinates(knowns):
     for n in range(N0 * N1 * N2):
         i, j, kk = n % N0, (n // N0) % N1, n // (N0 * N1)
         assert np.allclose(step * [i, j, kk] + un[n], node[:, n], rtol=0, atol=1e-20)
+
+
+def test_loop_over_loadcase_result_and_no_solution():
+    """TestDamaskGridLoopOverLoadcase (test_damask_grid.cpp): one increment of a 1 s step
+    ends at t = 1 with its record; with at most one iteration and no cut-back allowed
+    the loop reports that no solution was found (the reference throws)."""
+    import pytest
+    q = [[1.0, 0.0, 0.0, 0.0], [0.7936696712125002, -0.28765777461664166, -0.3436487135089419, 0.4113964260949434]]
+    step = dgo.loadstep("tensionX", t=1.0, N=1)
+    recs = dgo.Solver((2, 1, 1), (2e-5, 1e-5, 1e-5), [0, 1], q).run([step])
+    assert len(recs) == 1 and recs[0]["t"] == 1.0 and recs[0]["iterations"] >= 1
+    s = dgo.Solver((2, 1, 1), (2e-5, 1e-5, 1e-5), [0, 1], q, num=dgo.numerics(itmax=1, max_cut_back=0))
+    with pytest.raises(RuntimeError, match="no solution"):
+        s.run([step])
