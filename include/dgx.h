@@ -53,7 +53,8 @@ typedef struct dgx_numerics {
   int32_t stag_iter_max, max_cut_back;
   int32_t solver;                 /* 0 NGMRES (PETSc SNESNGMRES defaults), 1 fixed point */
   int32_t ngmres_m, snes_max_it;
-  int32_t precision;              /* 0 FP64 everywhere, 1 mixed: FP32 FFT/Gamma */
+  int32_t precision;              /* 0 FP64 everywhere, 1 mixed: FP32 FFT/Gamma, FP32 Lp Jacobian,
+                                     rates and state test around the FP64 Lp Newton */
   int32_t lazy_tangent;           /* 1: tangent only where C_volAvg/C_minMaxAvg are consumed */
 } dgx_numerics;
 
