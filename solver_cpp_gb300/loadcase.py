@@ -241,6 +241,8 @@ def parse_load_yaml(text):
             sv, sm = np.zeros((3, 3)), np.ones((3, 3), dtype=int)
         disc = item["discretization"]
         rot = bc.get("R", (1.0, 0.0, 0.0, 0.0))
+        if not isinstance(rot, (list, tuple)) or len(rot) != 4:
+            raise ValueError("R of a load step must have exactly 4 elements (quaternion w, x, y, z)")
         steps.append(make_step(defs[0], dv, dm, strs[0], sv, sm, disc["t"], disc["N"], r=disc.get("r", 1.0),
                                f_out=item.get("f_out", 1), estimate_rate=item.get("estimate_rate", True), rot=rot))
     return steps

@@ -110,6 +110,9 @@ def main(ref):
     m = re.search(r'vti_file_content = \(R""""\((.*?)\)""""\);', dg, re.S)
     out["vti_16x16x16"] = {"content": m.group(1), "cells": [16, 16, 16], "size": [1, 1, 1],
                            "origin": [0, 0, 0]}
+    cf = rd("test_config.cpp")
+    raw = re.findall(r'write_to_file\(R""""\((.*?)\)""""\);', cf, re.S)
+    out["config_yaml"] = {"numerics": raw[0], "load": raw[1]}
     ex = os.path.join(ref, "examples", "grid")
     out["examples_grid"] = {n: open(os.path.join(ex, n)).read()
                             for n in ("tensionX.yaml", "shearXY.yaml", "shearZX.yaml", "material.yaml", "numerics.yaml")}
